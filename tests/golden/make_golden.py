@@ -1,0 +1,257 @@
+"""Generate golden fixtures by running the REFERENCE's own Python sources.
+
+The reference (MandoCT-Taichi) is a set of Python scripts whose kernels are
+Taichi DSL.  Taichi is not installable here, so this script puts
+``tests/golden/refshim`` (a small stand-in for the ``taichi``, ``crip.io`` and
+``matplotlib`` APIs that executes kernel bodies sequentially in float64) ahead
+of the reference directory on ``sys.path`` and drives the reference classes
+exactly as its entry points do (run_mgfbp.py:18-47, run_mgfpj_v3.py:45-77,
+run_mgfbp_iterative_recon_IRN_CGLS.py:14-49, ..._piccs.py:13-45).
+
+Usage (needs the reference checkout; writes tests/golden/*.npz):
+    python tests/golden/make_golden.py /path/to/reference [case ...]
+
+Each fixture holds the jsonc config (as text), the inputs and the reference's
+outputs, plus intermediate arrays read back from the reference objects.
+"""
+import contextlib
+import copy
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# ---------------------------------------------------------------- cases
+BASE_FAN = {
+    "InputFiles": "sgm_.*.raw", "OutputFilePrefix": "", "OutputFileReplace": ["sgm", "rec"],
+    "DetectorElementCountHorizontal": 40, "DetectorElementWidth": 1.2, "DetectorOffsetHorizontal": 0.7,
+    "DetectorElementCountVertical": 2, "Views": 30, "TotalScanAngle": 360,
+    "SourceIsocenterDistance": 300, "SourceDetectorDistance": 600,
+    "ImageDimension": 16, "PixelSize": 1.5, "ImageRotation": 15, "ImageCenter": [1.0, -0.5],
+    "HammingFilter": 1,
+}
+BASE_CONE = {
+    "InputFiles": "sgm_.*.raw", "OutputFilePrefix": "", "OutputFileReplace": ["sgm", "rec"],
+    "DetectorElementCountHorizontal": 28, "DetectorElementWidth": 1.6, "DetectorOffsetHorizontal": -0.4,
+    "DetectorElementCountVertical": 14, "DetectorElementHeight": 1.6, "DetectorOffsetVertical": 0.5,
+    "Views": 20, "TotalScanAngle": 360, "SourceIsocenterDistance": 200, "SourceDetectorDistance": 400,
+    "ImageDimension": 12, "PixelSize": 1.2, "ImageDimensionZ": 8, "VoxelHeight": 1.2,
+    "ConeBeam": True, "HammingFilter": 1,
+}
+
+
+def _upd(base, **kw):
+    d = copy.deepcopy(base)
+    d.update(kw)
+    return d
+
+
+FBP_CASES = {
+    "fbp2d_ramp": _upd(BASE_FAN),
+    "fbp2d_curved_short": _upd(BASE_FAN, CurvedDetector=True, TotalScanAngle=250, Views=36,
+                               HammingFilter=0.6, BeamHardeningCorrectionCoefficients=[1.0, 0.05]),
+    "fbp2d_gauss_dbt_hu": _upd(BASE_FAN, TotalScanAngle=720, Views=48, DBTMode=True, WaterMu=0.02,
+                               HammingFilter=None, GaussianApodizedRamp=1.3),
+    "fdk_cone": _upd(BASE_CONE),
+    "fdk_cone_postlog_coronal": _upd(BASE_CONE, InputFileForm="post_log_images", ReconViewMode="coronal",
+                                     DetectorElementVerticalReconRange=[1, 12],
+                                     DetectorElementVerticalGaussFilterSize=1.5, ImageCenterZ=0.3,
+                                     HammingFilter=0.8),
+    "fdk_cone_sagittal_curved_short": _upd(BASE_CONE, ReconViewMode="sagittal", CurvedDetector=True,
+                                           TotalScanAngle=200, Views=24, ImageRotation=30,
+                                           FirstSinogramSliceIsDetectorTopRow=True),
+}
+
+BASE_FPJ = {
+    "InputFiles": "img_.*.raw", "OutputFilePrefix": "", "OutputFileReplace": ["img", "sgm"],
+    "DetectorElementCountHorizontal": 24, "DetectorElementWidth": 1.6, "DetectorOffsetHorizontal": 0.5,
+    "DetectorElementCountVertical": 12, "DetectorElementHeight": 1.6, "DetectorOffsetVertical": -0.3,
+    "Views": 12, "TotalScanAngle": 360, "SourceIsocenterDistance": 200, "SourceDetectorDistance": 400,
+    "ImageDimension": 14, "PixelSize": 1.2, "ImageDimensionZ": 8, "VoxelHeight": 1.2,
+    "ImageRotation": 10, "ImageCenter": [0.5, -0.4], "ImageCenterZ": 0.2,
+    "ConeBeam": True, "ForwardProjectionStepSize": 0.4,
+}
+
+FPJ_CASES = {
+    "fpj_cone": _upd(BASE_FPJ),
+    "fpj_cone_postlog_curved": _upd(BASE_FPJ, OutputFileForm="post_log_images", CurvedDetector=True,
+                                    ImageCenterZ=None),
+    "fpj_fan_oversample2": _upd(BASE_FPJ, ConeBeam=False, DetectorElementCountVertical=3,
+                                ImageDimensionZ=3, OversampleSize=2, DetectorElementHeight=None,
+                                DetectorOffsetVertical=None, VoxelHeight=None, ImageCenterZ=None,
+                                ImageDimension=12),
+    "fpj_helical": _upd(BASE_FPJ, HelicalPitch=0.5, TotalScanAngle=720, Views=16),
+}
+
+BASE_IR = {
+    "InputFiles": "sgm_.*.raw", "OutputFilePrefix": "", "OutputFileReplace": ["sgm", "rec"],
+    "InputFileForm": "post_log_images",
+    "DetectorElementCountHorizontal": 16, "DetectorElementWidth": 1.6, "DetectorOffsetHorizontal": 0.3,
+    "DetectorElementCountVertical": 10, "DetectorElementHeight": 2.0, "DetectorOffsetVertical": 0.4,
+    "Views": 10, "TotalScanAngle": 360, "SourceIsocenterDistance": 200, "SourceDetectorDistance": 400,
+    "ImageDimension": 10, "PixelSize": 1.2, "ImageDimensionZ": 6, "VoxelHeight": 1.2,
+    "ConeBeam": True, "HammingFilter": 1, "ForwardProjectionStepSize": 0.5,
+    "WaterMu": 0.02, "Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 1, "NumberOfIterations": 2,
+}
+
+IR_CASES = {
+    "ir_tv": _upd(BASE_IR),
+    "ir_piccs": _upd(BASE_IR, Alpha=0.5),
+}
+
+
+def _clean(cfg):
+    return {k: v for k, v in cfg.items() if v is not None}
+
+
+@contextlib.contextmanager
+def _chdir(d):
+    old = os.getcwd()
+    os.chdir(d)
+    try:
+        yield
+    finally:
+        os.chdir(old)
+
+
+def _arr(field):
+    return np.asarray(field.to_numpy(), dtype=np.float64)
+
+
+def _smooth_volume(rng, nz, n):
+    """A few random blobs, so that projections are smooth and non-trivial."""
+    z, y, x = np.meshgrid(np.linspace(-1, 1, nz), np.linspace(-1, 1, n), np.linspace(-1, 1, n), indexing="ij")
+    v = np.zeros((nz, n, n))
+    for _ in range(4):
+        c = rng.uniform(-0.5, 0.5, 3)
+        s = rng.uniform(0.2, 0.5)
+        v += rng.uniform(0.5, 1.5) * np.exp(-((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) / s ** 2)
+    return (v * 0.02 + rng.uniform(0, 0.002, v.shape)).astype(np.float32)
+
+
+def run_fbp_case(name, cfg, R, rng):
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("sgm")
+        cfg.update(InputDir=d + "/sgm", OutputDir=d + "/rec")
+        nu = cfg["DetectorElementCountHorizontal"]
+        nv = cfg["DetectorElementCountVertical"]
+        nb = cfg["Views"]
+        sgm = rng.uniform(0.0, 1.0, (nv, nb, nu)).astype(np.float32)
+        if cfg.get("InputFileForm") == "post_log_images":
+            sgm.transpose(1, 0, 2).tofile("sgm/sgm_a.raw")
+        else:
+            sgm.tofile("sgm/sgm_a.raw")
+        json.dump(cfg, open("config.jsonc", "w"))
+        conf = R.ReadConfigFile("config.jsonc")
+        fbp = R.Mgfbp(conf)
+        img = fbp.MainFunction()
+        out = dict(config=json.dumps(cfg), input_sgm=sgm, recon=np.asarray(img, np.float64),
+                   taps=_arr(fbp.array_recon_kernel_taichi), u=_arr(fbp.array_u_taichi),
+                   v=_arr(fbp.array_v_taichi), angles=_arr(fbp.array_angle_taichi),
+                   weighted=np.asarray(fbp.img_sgm, np.float64), filtered=_arr(fbp.img_sgm_filtered_taichi))
+        if fbp.apply_gauss_vertical:
+            out["gauss_v"] = _arr(fbp.array_kernel_gauss_vertical_taichi)
+        return out
+
+
+def run_fpj_case(name, cfg, R3, rng):
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("img")
+        cfg.update(InputDir=d + "/img", OutputDir=d + "/sgm")
+        vol = _smooth_volume(rng, cfg.get("ImageDimensionZ", cfg["DetectorElementCountVertical"]),
+                             cfg["ImageDimension"])
+        if not cfg.get("ConeBeam", False):
+            vol = _smooth_volume(rng, cfg["DetectorElementCountVertical"], cfg["ImageDimension"])
+        vol.tofile("img/img_a.raw")
+        json.dump(cfg, open("config.jsonc", "w"))
+        conf = R3.ReadConfigFile("config.jsonc")
+        fpj = R3.Mgfpj_v3(conf)
+        sgm = fpj.MainFunction()
+        return dict(config=json.dumps(cfg), input_vol=vol, sgm=np.asarray(sgm, np.float64),
+                    u=_arr(fpj.array_u_taichi), v=_arr(fpj.array_v_taichi),
+                    angles=_arr(fpj.array_angle_taichi), cz=_arr(fpj.array_img_center_z_taichi).ravel())
+
+
+def run_ir_case(name, cfg, RI, RP, R, rng):
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("sgm")
+        cfg.update(InputDir=d + "/sgm", OutputDir=d + "/rec")
+        n, nz = cfg["ImageDimension"], cfg["ImageDimensionZ"]
+        nu, nv, nb = cfg["DetectorElementCountHorizontal"], cfg["DetectorElementCountVertical"], cfg["Views"]
+        sgm = (rng.uniform(0.0, 0.4, (nv, nb, nu)) + 0.1).astype(np.float32)
+        sgm.transpose(1, 0, 2).tofile("sgm/sgm_a.raw")  # post_log_images layout [views, rows, cols]
+        out = dict(input_sgm=sgm)
+        if "Alpha" in cfg:
+            prior = (rng.uniform(-200, 200, (nz, n, n))).astype(np.float32)  # HU
+            prior.tofile("prior.raw")
+            cfg["PriorImageFile"] = d + "/prior.raw"
+            out["prior"] = prior
+        json.dump(cfg, open("config.jsonc", "w"))
+        conf = R.ReadConfigFile("config.jsonc")
+        if "Alpha" in cfg:
+            obj = RP.Mgfbp_ir_piccs(conf)
+            img = obj.MainFunction()
+        else:
+            seed = R.Mgfbp(R.ReadConfigFile("config.jsonc")).MainFunction()
+            out["fbp_seed"] = np.asarray(seed, np.float64)
+            obj = RI.Mgfbp_ir(conf)
+            img = obj.MainFunction(seed)
+        out.update(config=json.dumps(cfg), recon=np.asarray(img, np.float64),
+                   emap=np.asarray(obj.img_fp_effective_map, np.float64),
+                   bp_b=np.asarray(obj.img_bp_b, np.float64),
+                   u=_arr(obj.array_u_taichi), v=_arr(obj.array_v_taichi),
+                   angles=_arr(obj.array_angle_taichi), cz=_arr(obj.array_img_center_z_taichi).ravel(),
+                   ptp_calls=obj.num_iter_runned)
+        # single-operator probes on the same object
+        xt = rng.uniform(0.0, 0.03, (nz, n, n))
+        out["probe_x"] = xt
+        out["probe_fp"] = np.asarray(obj.ForwardProjection(xt), np.float64)
+        out["probe_ptp"] = np.asarray(obj.ForwardProjectionAndBackProjection(xt), np.float64)
+        wr = obj.GenerateWR(xt, cfg["BetaTV"])
+        out["probe_wr"] = np.asarray(wr, np.float64)
+        out["probe_dtwd"] = np.asarray(obj.Dt_W_D(xt, wr), np.float64)
+        out["probe_tv"] = float(obj.TVPenaltyVal(xt))
+        return out
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MANDOCT_REFERENCE", "")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py /path/to/reference [case ...]")
+    only = set(sys.argv[2:])
+    sys.path.insert(0, ref)
+    sys.path.insert(0, os.path.join(HERE, "refshim"))
+    import taichi as ti_shim  # the stand-in
+    import run_mgfbp as R
+    import run_mgfpj_v3 as R3
+    import run_mgfbp_iterative_recon_IRN_CGLS as RI
+    import run_mgfbp_iterative_recon_IRN_CGLS_piccs as RP
+    jobs = [(k, v, "fbp") for k, v in FBP_CASES.items()] + [(k, v, "fpj") for k, v in FPJ_CASES.items()] \
+        + [(k, v, "ir") for k, v in IR_CASES.items()]
+    for i, (name, cfg, kind) in enumerate(jobs):
+        if only and name not in only:
+            continue
+        rng = np.random.default_rng(1000 + i)
+        ti_shim.seed(1000 + i)
+        t = time.time()
+        with open(os.devnull, "w") as devnull, contextlib.redirect_stdout(devnull):
+            if kind == "fbp":
+                out = run_fbp_case(name, cfg, R, rng)
+            elif kind == "fpj":
+                out = run_fpj_case(name, cfg, R3, rng)
+            else:
+                out = run_ir_case(name, cfg, RI, RP, R, rng)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(f"{name}: {time.time() - t:.1f}s")
+
+
+if __name__ == "__main__":
+    main()
