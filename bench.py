@@ -1,0 +1,422 @@
+"""Benchmark of the MandoCT hot path on GB300: cone-beam FDK + forward projection.
+
+Workload (one step): FDK reconstruction (cosine weighting, Toeplitz ramp/Hann
+filter, packing, backprojection) of a resident 1024x256x1080 sinogram into a
+512x512x256 volume, then the trilinear ray-driven forward projection of that volume
+back to 1080 views.  Synthetic data: 20 seeded random ellipsoids, exact line
+integrals, Poisson noise at 1e5 photons.  Metric: GUPS = (voxel x view updates of
+the backprojection + voxel x view equivalents of the forward projection) / s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--storage f32|bf16]
+  python bench.py --impl reference ...   # the CPU implementation (OpenMP C port)
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(nu=1024, nv=256, views=1080, nx=512, nz=256, du=0.8, dv=0.8, px=0.4, pz=0.4, sid=600.0,
+                sdd=1100.0, step=0.2, n_ell=20, photons=1e5, seed=2024)
+SMALL = dict(WORKLOAD, nu=256, nv=64, views=270, nx=128, nz=64, du=3.2, dv=3.2, px=1.6, pz=1.6)
+
+
+def make_config(w):
+    return {"InputDir": "/tmp", "OutputDir": "/tmp/mandoct_bench", "InputFiles": "none", "OutputFilePrefix": "",
+            "OutputFileReplace": ["sgm", "rec"], "DetectorElementCountHorizontal": w["nu"],
+            "DetectorElementWidth": w["du"], "DetectorOffsetHorizontal": 0.0,
+            "DetectorElementCountVertical": w["nv"], "DetectorElementHeight": w["dv"],
+            "DetectorOffsetVertical": 0.0, "Views": w["views"], "TotalScanAngle": 360,
+            "SourceIsocenterDistance": w["sid"], "SourceDetectorDistance": w["sdd"], "ImageDimension": w["nx"],
+            "PixelSize": w["px"], "ImageDimensionZ": w["nz"], "VoxelHeight": w["pz"], "ConeBeam": True,
+            "HammingFilter": 1, "ForwardProjectionStepSize": w["step"]}
+
+
+def hann_from_ramp(ramp):
+    """Ramp x Hann window in the spatial domain: h = r/2 + (r[n-1] + r[n+1])/4."""
+    h = 0.5 * ramp.copy()
+    h[1:] += 0.25 * ramp[:-1]
+    h[:-1] += 0.25 * ramp[1:]
+    return h
+
+
+def ellipsoids(w):
+    rng = np.random.default_rng(w["seed"])
+    fov = w["nx"] * w["px"] / 2
+    zext = w["nz"] * w["pz"] / 2
+    out = []
+    for _ in range(w["n_ell"]):
+        r, a = 0.6 * fov * math.sqrt(rng.uniform()), rng.uniform(0, 2 * math.pi)
+        ax, ay = rng.uniform(0.05, 0.4, 2) * fov
+        az = rng.uniform(0.05, 0.4) * zext
+        out.append([r * math.cos(a), r * math.sin(a), rng.uniform(-0.4, 0.4) * zext, ax, ay, az,
+                    rng.uniform(0, math.pi), 0.0, 0.0, rng.uniform(0.01, 0.05)])
+    return np.asarray(out, dtype=np.float32)
+
+
+class Obj:
+    verbose = False
+
+
+def parse(w):
+    from reconstruction_program_taichi_gb300 import config
+    o = Obj()
+    cfg = make_config(w)
+    config.parse_fbp(o, cfg)
+    config.parse_fpj(o, cfg)
+    config.parse_fpj_v3(o, cfg)
+    return o
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_gpu(args, w):
+    import torch
+    from reconstruction_program_taichi_gb300 import _lib, fbp, geometry, ops
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    o = parse(w)
+    pipe = fbp.FdkPipeline(o, device=dev, storage=args.storage)
+    pipe.taps.copy_(torch.tensor(hann_from_ramp(geometry.recon_taps(o)), dtype=torch.float32))
+    fpg = geometry.fpj_geometry(o, device=dev)
+    # synthetic data (not timed)
+    ell = ellipsoids(w)
+    line = ops.project_ellipsoids(pipe.dg, ell)
+    gen = torch.Generator(device=dev).manual_seed(w["seed"])
+    counts = torch.poisson(w["photons"] * torch.exp(-line.double()), generator=gen).clamp_(min=1.0)
+    sgm = torch.log(w["photons"] / counts).float().contiguous()
+    del line, counts
+    fp_out = torch.empty(fpg.sgm_shape, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(evs=None):
+        if evs:
+            evs[0].record(stream)
+        filt = pipe.filter(sgm)
+        if evs:
+            evs[1].record(stream)
+        packed = ops.pack(pipe.dg, filt, pipe.dtype, out=pipe.packed)
+        if evs:
+            evs[2].record(stream)
+        vol = ops.fdk_bp(pipe.dg, packed, pipe.dtype, out=pipe.vol)
+        if evs:
+            evs[3].record(stream)
+        ops.fp(fpg, vol, out=fp_out)
+        if evs:
+            evs[4].record(stream)
+        return vol
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    nstage = 5
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(nstage)] for _ in range(args.steps)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _lib.launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        t_start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        t_end.record(stream)
+        barrier()
+    launches = _lib.launch_count() - launches0
+    total_ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / args.steps
+    stage = np.array([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(nstage - 1)] for k in range(args.steps)])
+    st = stage.mean(axis=0)  # filter, pack, bp, fp
+    nvox = w["nx"] * w["nx"] * w["nz"]
+    units = 2.0 * nvox * w["views"] * world
+    value = units / (ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (bp or fp), algorithmic bytes per launch
+    hbm, _, peak_kind = peaks()
+    n_samples = ops.fp_count_samples(fpg)
+    bp_bytes = nvox * w["views"] * (8 if pipe.dtype == 1 else 16) + nvox * 4
+    fp_bytes = n_samples * 32 + fpg.geom.nv * fpg.geom.views * fpg.geom.nu * 4
+    dom = "fp_kernel" if st[3] >= st[2] else "fdk_bp_kernel"
+    dom_ms, dom_bytes = (st[3], fp_bytes) if dom == "fp_kernel" else (st[2], bp_bytes)
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    traffic = None
+    tj = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(tj):
+        traffic = json.load(open(tj)).get(dom)
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes": int(dom_bytes)}
+
+    # end to end through the public API: pinned host sinogram in, volume + projections out
+    host_sgm = torch.empty(sgm.shape, dtype=torch.float32, pin_memory=True)
+    host_sgm.copy_(sgm.cpu())
+    host_vol = torch.empty(pipe.vol.shape, dtype=torch.float32, pin_memory=True)
+    host_fp = torch.empty(fp_out.shape, dtype=torch.float32, pin_memory=True)
+    dev_sgm = torch.empty_like(sgm)
+
+    def e2e_step():
+        dev_sgm.copy_(host_sgm, non_blocking=True)
+        vol = pipe.run(dev_sgm)
+        ops.fp(fpg, vol, out=fp_out)
+        host_vol.copy_(vol, non_blocking=True)
+        host_fp.copy_(fp_out, non_blocking=True)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e = {"value": round(units / (e2e_ms / 1e3) / 1e9, 3), "unit": "GUPS", "ms_per_step": round(e2e_ms, 3),
+           "h2d_bytes_per_step": int(host_sgm.numel() * 4),
+           "d2h_bytes_per_step": int(host_vol.numel() * 4 + host_fp.numel() * 4)}
+
+    # mixed-precision storage variant of the FDK (bf16 backprojection operand)
+    mixed = None
+    if args.storage == "f32" and not args.no_mixed:
+        pm = fbp.FdkPipeline(o, device=dev, storage="bf16")
+        pm.taps.copy_(pipe.taps)
+        ref_vol = pipe.run(sgm).clone()
+        for _ in range(2):
+            mv = pm.run(sgm)
+        barrier()
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for _ in range(args.steps):
+            mv = pm.run(sgm)
+        m1.record(stream)
+        barrier()
+        mms = m0.elapsed_time(m1) / args.steps
+        rel = float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol))
+        mixed = {"fdk_ms": round(mms, 3), "fdk_plain_ms": round(float(st[0] + st[1] + st[2]), 3),
+                 "speedup_fdk": round(float(st[0] + st[1] + st[2]) / mms, 3), "rel_l2_vs_plain": rel,
+                 "storage": "bf16 packed backprojection operand"}
+        del pm
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(w, o, budget_s=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": "GUPS (cone-beam FDK + forward projection, voxel x view updates per second)",
+            "value": round(value, 3), "unit": "GUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.storage == "f32" else "bf16-storage/f32-compute",
+            "data": "synthetic: 20 seeded ellipsoids, exact line integrals, Poisson noise at 1e5 photons",
+            "config": {"workload": f"FDK+FP {w['nx']}x{w['nx']}x{w['nz']} vol @{w['px']}mm, {w['views']} views/360deg, "
+                                   f"{w['nu']}x{w['nv']} flat det @{w['du']}mm, SID {w['sid']:.0f} SDD {w['sdd']:.0f}",
+                       "filter": "ramp x Hann (spatial composition of the reference ramp)",
+                       "fp_step": w["step"], "l2": "inputs larger than L2 (sinogram 1.13 GB, volume 268 MB)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU"},
+            "stages_ms": {"weight_filter": round(float(st[0]), 3), "pack": round(float(st[1]), 3),
+                          "backproject": round(float(st[2]), 3), "forward_project": round(float(st[3]), 3)},
+            "fdk_gups": round(nvox * w["views"] / ((st[0] + st[1] + st[2]) / 1e3) / 1e9, 2),
+            "bp_gups": round(nvox * w["views"] / (st[2] / 1e3) / 1e9, 2),
+            "fp_gups": round(nvox * w["views"] / (st[3] / 1e3) / 1e9, 2),
+            "fp_samples_per_s": round(n_samples / (st[3] / 1e3), 1), "fp_in_volume_samples": n_samples,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk.summary(), "mixed": mixed,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------- CPU (reference) arm
+
+def cpu_sample(w, o, bp_views, fp_views, filt_rows):
+    """Time the OpenMP C restatement on a bounded sample of one step; returns
+    (seconds for the full step extrapolated, threads, description)."""
+    from oracle import cpu_ref
+    from reconstruction_program_taichi_gb300 import geometry
+    from reconstruction_program_taichi_gb300._lib import MCT_CONE, Geom
+    u, v, ang = geometry.fbp_arrays(o)
+    g = Geom()
+    g.nu, g.nv, g.views, g.nx, g.nz, g.flags = w["nu"], w["nv"], w["views"], w["nx"], w["nz"], MCT_CONE
+    g.du, g.dv, g.px, g.pz, g.sid, g.sdd = w["du"], w["dv"], w["px"], w["pz"], w["sid"], w["sdd"]
+    g.u0, g.u_step, g.v0, g.v_step = u[0], u[1] - u[0], v[0], v[1] - v[0]
+    g.total_scan_angle, g.cz = o.total_scan_angle, o.img_center_z
+    g.fp_step = w["step"]
+    g.fp_steps = geometry.count_steps_v3(w["nx"], w["nz"], w["px"], w["pz"], w["step"])
+    rng = np.random.default_rng(1)
+    rows = w["nv"] * w["views"]
+    x = rng.uniform(0, 1, (filt_rows, w["nu"])).astype(np.float32)
+    y = np.empty_like(x)
+    taps = hann_from_ramp(geometry.recon_taps(o)).astype(np.float32)
+    t0 = time.perf_counter()
+    cpu_ref.filter_rows(g, x, taps, y, 0, filt_rows)
+    t_f = (time.perf_counter() - t0) * rows / filt_rows
+    F = rng.uniform(0, 1, (w["nv"], w["views"], w["nu"])).astype(np.float32)
+    vol = np.zeros((w["nz"], w["nx"], w["nx"]), np.float32)
+    alive = np.ones(vol.shape, np.uint8)
+    angf = ang.astype(np.float32)
+    t0 = time.perf_counter()
+    cpu_ref.fdk_bp(g, angf, F, vol, alive, 0, bp_views)
+    t_bp = (time.perf_counter() - t0) * w["views"] / bp_views
+    fpu, fpv, _ = geometry.fpj_arrays(o)
+    out = np.zeros((w["nv"], w["views"], w["nu"]), np.float32)
+    vol = rng.uniform(0, 0.02, vol.shape).astype(np.float32)
+    step = max(1, w["views"] // fp_views)
+    t0 = time.perf_counter()
+    for j in range(0, step * fp_views, step):
+        cpu_ref.fp(g, angf, fpu.astype(np.float32), fpv.astype(np.float32), vol, out, j, j + 1)
+    t_fp = (time.perf_counter() - t0) * w["views"] / fp_views
+    desc = (f"OpenMP C restatement, {cpu_ref.threads()} threads: filter {filt_rows} of {rows} rows, "
+            f"backprojection {bp_views} of {w['views']} views, forward projection {fp_views} evenly spaced of "
+            f"{w['views']} views; each extrapolated linearly to the full step")
+    return t_f + t_bp + t_fp, cpu_ref.threads(), desc, dict(filter_s=t_f, bp_s=t_bp, fp_s=t_fp)
+
+
+def cpu_baseline(w, o, budget_s=20.0):
+    from oracle import cpu_ref
+    cpu_ref.build()
+    scale = min(1.0, budget_s / 20.0)
+    bp_views = max(2, int(round(48 * scale)))
+    fp_views = max(1, int(round(6 * scale)))
+    t, thr, desc, parts = cpu_sample(w, o, bp_views, fp_views, max(64, int(2048 * scale)))
+    units = 2.0 * w["nx"] * w["nx"] * w["nz"] * w["views"]
+    return {"value": round(units / t / 1e9, 4), "unit": "GUPS", "cores": thr, "kind": "port", "sample": desc,
+            "extrapolated_step_s": round(t, 2), "parts_s": {k: round(v, 2) for k, v in parts.items()}}
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    o = parse(w)
+    from oracle import cpu_ref
+    cpu_ref.build()
+    for _ in range(args.warmup):
+        cpu_sample(w, o, 2, 1, 64)
+    times = []
+    for _ in range(args.steps):
+        t, thr, desc, parts = cpu_sample(w, o, 8, 1, 256)
+        times.append(t)
+    t = float(np.mean(times))
+    units = 2.0 * w["nx"] * w["nx"] * w["nz"] * w["views"]
+    value = units / t / 1e9
+    line = {"impl": "reference", "metric": "GUPS (cone-beam FDK + forward projection, voxel x view updates per second)",
+            "value": round(value, 4), "unit": "GUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t * 1e3, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (uniform random sinogram / volume; cost is data independent)",
+            "config": {"workload": f"FDK+FP {w['nx']}x{w['nx']}x{w['nz']} vol, {w['views']} views, "
+                                   f"{w['nu']}x{w['nv']} det (bounded sample per step, extrapolated)"},
+            "cpu_baseline": {"value": round(value, 4), "unit": "GUPS", "cores": thr, "kind": "port", "sample": desc},
+            "e2e": {"value": round(value, 4), "unit": "GUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's Taichi kernels cannot run here (no taichi); this is the OpenMP C restatement "
+                    "of the same kernels on all host threads"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "bf16"])
+    ap.add_argument("--small", action="store_true", help="4x smaller workload (profiling / quick checks)")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    w = SMALL if args.small else WORKLOAD
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    main()

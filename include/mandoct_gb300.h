@@ -1,0 +1,226 @@
+/*
+ * mandoct_gb300.h -- C ABI of the GB300 (sm_103a) MandoCT reconstruction kernels.
+ *
+ * The reference (MandoCT-Taichi) has no native ABI: its hot path is Taichi kernels
+ * that are methods of Python classes.  Each entry point below replaces one of those
+ * kernels (cited per function as file:line in the reference).  The Python drop-in
+ * (package reconstruction_program_taichi_gb300) binds this library with ctypes;
+ * INTEGRATION.md shows the binding.
+ *
+ * Conventions
+ *   - Every pointer to bulk data is a DEVICE pointer owned by the caller.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Every function returns 0 (MCT_OK) or a negative MCT_E_* code and never
+ *     synchronises the stream; mct_last_error_string() describes the last failure
+ *     of the calling host thread.
+ *   - No function allocates device memory; intermediate buffers are passed in and
+ *     sized by the *_size queries.
+ *   - Sinograms are [rows][views][cols] float32 unless stated otherwise, volumes
+ *     are [z][y][x] float32 (the reference's array layouts).
+ */
+#ifndef MANDOCT_GB300_H
+#define MANDOCT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCT_OK 0
+#define MCT_E_INVALID (-1)     /* bad argument, size or geometry */
+#define MCT_E_CUDA (-2)        /* CUDA runtime error (launch or device) */
+#define MCT_E_UNSUPPORTED (-3) /* option not supported by this build */
+#define MCT_E_TIMEOUT (-4)     /* a bounded device-side wait gave up */
+
+/* geometry flags (mct_geom.flags) */
+#define MCT_CONE 1        /* ConeBeam */
+#define MCT_CURVED 2      /* CurvedDetector */
+#define MCT_SHORT_SCAN 4  /* |TotalScanAngle| mod 360 >= 0.01 deg */
+#define MCT_PMATRIX 8     /* PMatrixFile geometry */
+
+/* storage types of packed / reduced-precision buffers */
+#define MCT_F32 0
+#define MCT_BF16 1
+#define MCT_F16 2
+
+/* Scan and image geometry; every field mirrors a member of the reference's
+ * Mgfbp / Mgfpj / Mgfbp_ir objects (run_mgfbp.py:87-719, run_mgfpj_v2.py:113-214). */
+typedef struct mct_geom {
+    int32_t nu;          /* detector columns of this call (det_elem_count_horizontal[*oversample]) */
+    int32_t nv;          /* detector rows of this call (det_elem_count_vertical_actual) */
+    int32_t views;       /* view_num */
+    int32_t nv_total;    /* det_elem_count_vertical (full detector) */
+    int32_t row_begin;   /* det_elem_vertical_recon_range_begin */
+    int32_t nx;          /* img_dim (square slices) */
+    int32_t nz;          /* img_dim_z */
+    int32_t flags;       /* MCT_CONE | MCT_CURVED | MCT_SHORT_SCAN | MCT_PMATRIX */
+    int32_t view_mode;   /* recon_view_mode: 1 axial, 2 coronal, 3 sagittal */
+    int32_t fp_steps;    /* ray-march step count K of the forward projector */
+    float du, dv;        /* det_elem_width, det_elem_height [mm] */
+    float u0, u_step;    /* array_u[0], array_u[1]-array_u[0] (backprojectors) */
+    float v0, v_step;    /* array_v[0], array_v[1]-array_v[0] (backprojectors) */
+    float px, pz;        /* img_pix_size, img_voxel_height [mm] */
+    float cx, cy, cz;    /* img_center_x, img_center_y, img_center_z [mm] */
+    float sid, sdd;      /* source_isocenter_dis, source_det_dis [mm] */
+    float img_rot;       /* img_rot [rad] */
+    float total_scan_angle; /* [rad] */
+    float fp_step;       /* fpj_step_size, as a fraction of the voxel diagonal */
+    float fp_z_per_view; /* helical gantry advance per view [mm] (0: circular) */
+} mct_geom;
+
+/* Per-view and per-element tables (DEVICE pointers, float32). */
+typedef struct mct_tables {
+    const float* angles;  /* [views]  array_angle (includes img_rot) */
+    const float* u;       /* [nu]     array_u (forward projector) */
+    const float* v;       /* [nv]     array_v (forward projector) */
+    const float* cz;      /* [views]  per-view image centre z, or NULL for geom.cz */
+    const float* pmatrix; /* [views*12] projection matrices (backprojectors), or NULL */
+    const float* pmat_a;  /* [views*9]  matrix A = inv(P[:, :3]) (forward projector), or NULL */
+    const float* pmat_xs; /* [views*3]  source positions (forward projector), or NULL */
+} mct_tables;
+
+/* ---------------------------------------------------------------- library */
+const char* mct_version(void);
+const char* mct_last_error_string(void);
+/* Number of kernels this library has launched since load (all threads). */
+uint64_t mct_launch_count(void);
+
+/* ---------------------------------------------------------------- FBP / FDK */
+
+/* Beam-hardening polynomial (optional) and cosine (+ Parker) weighting.
+ * Replaces Mgfbp.BHCorrection run_mgfbp.py:946-954 and Mgfbp.WeightSgm :956-1011.
+ * sgm element (row r, view j, col c) is read at sgm[r*row_stride + j*view_stride + c]
+ * (sinogram files: row_stride = views*nu, view_stride = nu; post-log image stacks:
+ * row_stride = nu, view_stride = nv*nu).  bh_coeffs is a device array of n_bh
+ * coefficients or NULL.  weighted is [nv][views][nu]. */
+int mct_weight(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t row_stride,
+               int64_t view_stride, const float* bh_coeffs, int32_t n_bh, float* weighted,
+               void* stream);
+
+/* Vertical Gaussian smoothing over +-10 rows (DetectorElementVerticalGaussFilterSize).
+ * Replaces the first loop of Mgfbp.ConvolveSgmAndKernel run_mgfbp.py:1019-1029.
+ * gauss_taps: [2*nv-1] device taps from GenerateGassianKernel. */
+int mct_vgauss(const mct_geom* g, const float* weighted, const float* gauss_taps, float* out,
+               void* stream);
+
+/* Row convolution y[k] = du * sum_m x[m] h[k-m+nu-1] as a Toeplitz product, float32
+ * SIMT path.  Replaces Mgfbp.ConvolveSgmAndKernel run_mgfbp.py:1030-1046.
+ * weighted: [nv][views][nu]; taps: [2*nu-1]; filtered: VIEW-MAJOR [views][nv][nu]. */
+int mct_filter(const mct_geom* g, const float* weighted, const float* taps, float* filtered,
+               void* stream);
+
+/* Bytes of the packed backprojection operand for storage type dtype. */
+size_t mct_packed_size(const mct_geom* g, int32_t dtype);
+
+/* Pack a view-major filtered sinogram into the gather layout of mct_fdk_bp:
+ * cone beam: per (view, row r<nv-1, col c<nu-1) the 2x2 bilinear stencil
+ * {F[r][c], F[r][c+1], F[r+1][c], F[r+1][c+1]}; fan beam: per (view, row, col<nu-1)
+ * the pair {F[r][c], F[r][c+1]}.  dtype MCT_F32 or MCT_BF16. */
+int mct_pack(const mct_geom* g, const float* filtered, void* packed, int32_t dtype, void* stream);
+
+/* Pixel-driven FDK / fan-beam backprojection of a packed filtered sinogram into
+ * vol [nz][nx][nx] (overwritten).  Replaces Mgfbp.BackProjectionPixelDriven
+ * run_mgfbp.py:1062-1187, including its rule that a voxel projecting outside the
+ * detector in any view is zero. */
+int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype, float* vol,
+               void* stream);
+
+/* ---------------------------------------------------------------- forward projection */
+
+/* Ray-driven trilinear forward projection of vol [nz][nx][nx] for all views into
+ * sgm [nv][views][nu] (overwritten).  Rays with mask != 1 (mask [nv][views][nu], or
+ * NULL for none) give 0.  Replaces Mgfpj_v3.ForwardProjectionBilinear
+ * run_mgfpj_v3.py:184-366 and Mgfbp_ir.ForwardProjectionBilinear
+ * run_mgfbp_iterative_recon_IRN_CGLS.py:494-676. */
+int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
+           void* stream);
+
+/* Exact transpose of mct_fp: vol += P^T sgm (vol is accumulated, not cleared).
+ * No counterpart in the reference (its CGLS pairs mct_fp with the unmatched
+ * backprojector below); used for matched-adjoint CGLS and autograd. */
+int mct_fp_adjoint(const mct_geom* g, const mct_tables* t, const float* sgm, const float* mask,
+                   float* vol, void* stream);
+
+/* *count (device uint64) = number of trilinear samples of mct_fp whose stencil lies
+ * inside the volume (rays with mask != 1 excluded): the forward projector's
+ * algorithmic work.  No counterpart in the reference. */
+int mct_fp_count_samples(const mct_geom* g, const mct_tables* t, const float* mask, uint64_t* count,
+                         void* stream);
+
+/* Effective ray map [nv][views][nu]: 0 where a sample inside the inscribed cylinder
+ * leaves the volume through z, else 1.  Replaces
+ * Mgfbp_ir.GenEffectiveMapForwardProjectionAgent
+ * run_mgfbp_iterative_recon_IRN_CGLS.py:679-833. */
+int mct_effective_map(const mct_geom* g, const mct_tables* t, float* mask, void* stream);
+
+/* Oversample binning (mean of `bin` sub-columns) and optional noise:
+ * in [nv][views][nu*bin] -> out [nv][views][nu]; photons > 0 adds
+ * N0 e^{-p} + sqrt(.)*N(0,1) noise (clamped at 1e-6) then -log, with a counter-based
+ * generator seeded by `seed`.  Replaces Mgfpj_v3.BinSinogram run_mgfpj_v3.py:368-375
+ * and AddPossionNoise :381-391. */
+int mct_bin_noise(const mct_geom* g, const float* in, int32_t bin, float photons, uint64_t seed,
+                  float* out, void* stream);
+
+/* ---------------------------------------------------------------- iterative reconstruction */
+
+/* The reference CGLS "P^T": sum over views of a bilinear gather weighted by
+ * distance_factor*pixel_size, then zero voxels whose u left the detector in any view.
+ * sgm [nv][views][nu] (rows at mask==0 should already be zero); vol [nz][nx][nx]
+ * overwritten.  Replaces Mgfbp_ir.BackProjectionPixelDrivenPerView
+ * run_mgfbp_iterative_recon_IRN_CGLS.py:372-474 driven by :319-336 and
+ * SetTruncatedRegionToZero :477-481. */
+int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sgm, float* vol,
+                         void* stream);
+
+/* TV reweighting WR = 1/sqrt(|D x|^2 + beta) (forward differences, zero at the far
+ * edge; z differences only when nz > 2).  Replaces Mgfbp_ir.GenerateWR
+ * run_mgfbp_iterative_recon_IRN_CGLS.py:234-243.  x, wr: [nz][nx][nx]. */
+int mct_tv_weights(const mct_geom* g, const float* x, float beta, float* wr, void* stream);
+
+/* out = a*out_in + s * D^T W D x with interior-only backward differences
+ * (a = 0 ignores out_in).  Replaces Mgfbp_ir.Dt_W_D
+ * run_mgfbp_iterative_recon_IRN_CGLS.py:267-286. */
+int mct_dtwd(const mct_geom* g, const float* x, const float* wr, float s, const float* out_in,
+             float a, float* out, void* stream);
+
+/* sum sqrt(|D x|^2 + beta) accumulated in float64 into *result (device, overwritten).
+ * Replaces Mgfbp_ir.TVPenaltyVal run_mgfbp_iterative_recon_IRN_CGLS.py:245-254.
+ * partials: device scratch of mct_reduce_scratch_size() bytes. */
+int mct_tv_penalty(const mct_geom* g, const float* x, float beta, double* partials, double* result,
+                   void* stream);
+
+/* Scratch bytes needed by the float64 reductions below. */
+size_t mct_reduce_scratch_size(void);
+
+/* *result = sum a[i]*b[i] in float64 (device scalar).  Replaces the np.sum inner
+ * products of TikhonovSol run_mgfbp_iterative_recon_IRN_CGLS.py:202-203, 216. */
+int mct_dot_f64(const float* a, const float* b, int64_t n, double* partials, double* result,
+                void* stream);
+
+/* One fused CGLS step on device scalars (no host round trip), following
+ * TikhonovSol run_mgfbp_iterative_recon_IRN_CGLS.py:198-217:
+ *   alpha = rr / dq;  x += alpha d;  r -= alpha q;  rr_new = sum r^2 (float64);
+ * rr and dq are device float64 scalars; rr_new receives sum r^2 of the updated r.
+ * The second call, mct_cgls_direction, finishes beta = rr_new/rr and d = r + beta d. */
+int mct_cgls_update(int64_t n, const double* rr, const double* dq, float* x, float* r,
+                    const float* d, const float* q, double* partials, double* rr_new, void* stream);
+int mct_cgls_direction(int64_t n, const double* rr, const double* rr_new, const float* r, float* d,
+                       void* stream);
+
+/* ---------------------------------------------------------------- synthetic data */
+
+/* Exact line integrals of ellipsoids for the forward projector's ray geometry
+ * (no counterpart in the reference; it generates seeded phantoms for benchmarks).
+ * ell: [n_ell][10] = {cx, cy, cz, ax, ay, az, phi, theta?, psi?, mu}: centre [mm],
+ * semi-axes [mm], rotation about z [rad] (indices 7, 8 reserved = 0), attenuation
+ * [1/mm].  sgm [nv][views][nu] overwritten. */
+int mct_project_ellipsoids(const mct_geom* g, const mct_tables* t, const float* ell, int32_t n_ell,
+                           float* sgm, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MANDOCT_GB300_H */

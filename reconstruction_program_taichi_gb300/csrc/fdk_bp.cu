@@ -1,0 +1,300 @@
+// Pixel-driven FDK / fan-beam backprojection (run_mgfbp.py:1062-1187).
+//
+// Design (sm_103a):
+//   * one thread owns one (x, y) column and ZC consecutive slices, accumulating every
+//     view in registers (the reference does a global read-modify-write per view);
+//   * the filtered sinogram is pre-packed so that the 2x2 bilinear stencil of a
+//     detector position is ONE 16-byte (f32) or 8-byte (bf16) load;
+//   * per-view cos/sin/weight tables live in shared memory;
+//   * axial slices share u across the column, so u, the distance weight and the
+//     magnification are evaluated once per (column, view) and v is an affine
+//     function of the slice index.
+// Voxels that project outside the detector in any view are written as 0, as in the
+// reference (the view loop "breaks" with the voxel set to 0).
+#include <cmath>
+
+#include "common.cuh"
+
+namespace mct {
+namespace {
+
+constexpr int BP_TX = 32, BP_TY = 8, BP_ZC = 16, BP_VCHUNK = 1024;
+
+struct BpParams {
+    int nx, nz, nu, nv, views, cone, curved;
+    float sid, sdd, img_rot;
+    float u0, inv_ustep;   // uidx = (u - u0) * inv_ustep
+    float v0, kv;          // vidx = (mag*z - v0) * kv, kv = sign(v_step)/dv
+    float div;             // redundancy factor
+    // voxel centre of (ix, iy, iz) = P + ix*EX + iy*EY + iz*EZ (rotated frame)
+    float px_x, px_y, px_z;  // EX
+    float py_x, py_y, py_z;  // EY
+    float pz_x, pz_y, pz_z;  // EZ
+    float o_x, o_y, o_z;     // P
+};
+
+template <typename QT>
+struct Quad;
+template <>
+struct Quad<float4> {
+    static __device__ __forceinline__ void load(const float4* p, float& a, float& b, float& c, float& d) {
+        float4 q = __ldg(p);
+        a = q.x; b = q.y; c = q.z; d = q.w;
+    }
+};
+template <>
+struct Quad<uint2> {
+    static __device__ __forceinline__ void load(const uint2* p, float& a, float& b, float& c, float& d) {
+        uint2 q = __ldg(p);
+        a = __uint_as_float(q.x << 16);
+        b = __uint_as_float(q.x & 0xffff0000u);
+        c = __uint_as_float(q.y << 16);
+        d = __uint_as_float(q.y & 0xffff0000u);
+    }
+};
+template <typename PT>
+struct Pair;
+template <>
+struct Pair<float2> {
+    static __device__ __forceinline__ void load(const float2* p, float& a, float& b) {
+        float2 q = __ldg(p);
+        a = q.x; b = q.y;
+    }
+};
+template <>
+struct Pair<uint32_t> {
+    static __device__ __forceinline__ void load(const uint32_t* p, float& a, float& b) {
+        uint32_t q = __ldg(p);
+        a = __uint_as_float(q << 16);
+        b = __uint_as_float(q & 0xffff0000u);
+    }
+};
+
+// MODE 0: axial, flat or curved detector, no projection matrix (u hoisted per column)
+// MODE 1: any view mode, no projection matrix (per-voxel u)
+// MODE 2: projection matrix geometry
+template <int MODE, bool CONE, typename QT, typename PT>
+__global__ void __launch_bounds__(BP_TX* BP_TY)
+fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
+              const void* __restrict__ packed, float* __restrict__ vol) {
+    __shared__ float4 tab[BP_VCHUNK];  // {cos b, sin b, dbeta*div, unused}
+    const int ix = blockIdx.x * BP_TX + threadIdx.x;
+    const int iy = blockIdx.y * BP_TY + threadIdx.y;
+    const int zb = blockIdx.z * BP_ZC;
+    const int tid = threadIdx.y * BP_TX + threadIdx.x;
+    const bool active = ix < p.nx && iy < p.nx;
+    const int nq = p.nu - 1;                // packed columns
+    const int rq = CONE ? p.nv - 1 : p.nv;  // packed rows
+
+    // voxel centres of the ZC slices of this column: c_k = c0 + k * dc
+    const float c0x = p.o_x + ix * p.px_x + iy * p.py_x + zb * p.pz_x;
+    const float c0y = p.o_y + ix * p.px_y + iy * p.py_y + zb * p.pz_y;
+    const float c0z = p.o_z + ix * p.px_z + iy * p.py_z + zb * p.pz_z;
+
+    float acc[BP_ZC];
+#pragma unroll
+    for (int k = 0; k < BP_ZC; ++k) acc[k] = 0.0f;
+    uint32_t dead = 0;  // bit k: slice zb+k projected off the detector in some view
+
+    for (int jc = 0; jc < p.views; jc += BP_VCHUNK) {
+        const int nvc = min(BP_VCHUNK, p.views - jc);
+        __syncthreads();
+        for (int q = tid; q < nvc; q += BP_TX * BP_TY) {
+            int j = jc + q;
+            float s, c;
+            sincosf(angles[j] - p.img_rot, &s, &c);
+            float db = (j == p.views - 1) ? fabsf(angles[p.views - 1] - angles[0]) / (p.views - 1)
+                                          : fabsf(angles[j + 1] - angles[j]);
+            tab[q] = make_float4(c, s, db * p.div, 0.0f);
+        }
+        __syncthreads();
+        if (!active || dead == 0xffffffffu) continue;
+
+        for (int q = 0; q < nvc; ++q) {
+            const int j = jc + q;
+            const float4 tb = tab[q];
+            const float cb = tb.x, sb = tb.y;
+            if (MODE == 0) {
+                // u is shared by the whole column
+                const float L = p.sid - c0x * cb - c0y * sb;
+                const float t = -c0x * sb + c0y * cb;
+                const float mag = p.sdd / L;
+                const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
+                const float ui = (u - p.u0) * p.inv_ustep;
+                if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {  // NaN counts as off-detector
+                    dead = 0xffffffffu;
+                    break;
+                }
+                const float uf = floorf(ui);
+                const float ru = ui - uf;
+                const int uc = (int)uf;
+                const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+                const float w = (p.sid * dw) * tb.z;
+                if (CONE) {
+                    const float vA = (mag * c0z - p.v0) * p.kv;
+                    const float vB = (mag * p.pz_z) * p.kv;
+                    const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * rq * nq + uc;
+#pragma unroll
+                    for (int k = 0; k < BP_ZC; ++k) {
+                        const float vi = fmaf((float)k, vB, vA);
+                        const float vf = floorf(vi);
+                        int vr = (int)vf;
+                        if (vr < 0 || vr > p.nv - 2) dead |= 1u << k;
+                        vr = min(max(vr, 0), p.nv - 2);
+                        const float rv = vi - vf;
+                        float a, b, c2, d;
+                        Quad<QT>::load(base + (int64_t)vr * nq, a, b, c2, d);
+                        const float top = fmaf(ru, b - a, a);
+                        const float bot = fmaf(ru, d - c2, c2);
+                        acc[k] = fmaf(w, fmaf(rv, bot - top, top), acc[k]);
+                    }
+                } else {
+                    const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * rq + zb) * nq + uc;
+#pragma unroll
+                    for (int k = 0; k < BP_ZC; ++k) {
+                        if (zb + k < p.nz) {
+                            float a, b;
+                            Pair<PT>::load(base + (int64_t)k * nq, a, b);
+                            acc[k] = fmaf(w, fmaf(ru, b - a, a), acc[k]);
+                        }
+                    }
+                }
+            } else {
+                const float* P = pmat + 12 * j;
+                float P0 = 0, P1 = 0, P2 = 0, P3 = 0, P4 = 0, P5 = 0, P6 = 0, P7 = 0, P8 = 0, P9 = 0, P10 = 0, P11 = 0;
+                if (MODE == 2) {
+                    P0 = __ldg(P + 0); P1 = __ldg(P + 1); P2 = __ldg(P + 2); P3 = __ldg(P + 3);
+                    P4 = __ldg(P + 4); P5 = __ldg(P + 5); P6 = __ldg(P + 6); P7 = __ldg(P + 7);
+                    P8 = __ldg(P + 8); P9 = __ldg(P + 9); P10 = __ldg(P + 10); P11 = __ldg(P + 11);
+                }
+#pragma unroll
+                for (int k = 0; k < BP_ZC; ++k) {
+                    if (zb + k >= p.nz || (dead >> k) & 1u) continue;
+                    const float x = fmaf((float)k, p.pz_x, c0x);
+                    const float y = fmaf((float)k, p.pz_y, c0y);
+                    const float z = fmaf((float)k, p.pz_z, c0z);
+                    const float L = p.sid - x * cb - y * sb;
+                    const float t = -x * sb + y * cb;
+                    float mag, ui;
+                    if (MODE == 2) {
+                        mag = 1.0f / (P8 * x + P9 * y + P10 * z + P11);
+                        ui = (P0 * x + P1 * y + P2 * z + P3) * mag;
+                    } else {
+                        mag = p.sdd / L;
+                        const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
+                        ui = (u - p.u0) * p.inv_ustep;
+                    }
+                    if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {
+                        dead |= 1u << k;
+                        continue;
+                    }
+                    const float uf = floorf(ui);
+                    const float ru = ui - uf;
+                    const int uc = (int)uf;
+                    const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+                    const float w = (p.sid * dw) * tb.z;
+                    if (CONE) {
+                        const float vi = (MODE == 2) ? (P4 * x + P5 * y + P6 * z + P7) * mag : (mag * z - p.v0) * p.kv;
+                        const float vf = floorf(vi);
+                        const int vr = (int)vf;
+                        if (vr < 0 || vr > p.nv - 2) {
+                            dead |= 1u << k;
+                            continue;
+                        }
+                        const float rv = vi - vf;
+                        float a, b, c2, d;
+                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * rq + vr) * nq + uc, a, b, c2, d);
+                        const float top = fmaf(ru, b - a, a);
+                        const float bot = fmaf(ru, d - c2, c2);
+                        acc[k] = fmaf(w, fmaf(rv, bot - top, top), acc[k]);
+                    } else {
+                        float a, b;
+                        Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * rq + zb + k) * nq + uc, a, b);
+                        acc[k] = fmaf(w, fmaf(ru, b - a, a), acc[k]);
+                    }
+                }
+            }
+        }
+    }
+    if (!active) return;
+    const int64_t plane = (int64_t)p.nx * p.nx;
+    float* out = vol + (int64_t)zb * plane + (int64_t)iy * p.nx + ix;
+#pragma unroll
+    for (int k = 0; k < BP_ZC; ++k) {
+        if (zb + k < p.nz) out[(int64_t)k * plane] = ((dead >> k) & 1u) ? 0.0f : acc[k];
+    }
+}
+
+template <int MODE, bool CONE>
+void launch_bp(const BpParams& p, dim3 grid, dim3 block, cudaStream_t s, const float* angles, const float* pmat,
+               const void* packed, int dtype, float* vol) {
+    if (dtype == MCT_BF16)
+        fdk_bp_kernel<MODE, CONE, uint2, uint32_t><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol);
+    else
+        fdk_bp_kernel<MODE, CONE, float4, float2><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol);
+}
+
+}  // namespace
+}  // namespace mct
+
+using namespace mct;
+
+extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype, float* vol,
+                          void* stream) {
+    MCT_TRY(check_geom(g, "mct_fdk_bp"));
+    MCT_REQUIRE(t && t->angles && packed && vol, "mct_fdk_bp: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_fdk_bp: dtype must be MCT_F32 or MCT_BF16");
+    const bool cone = (g->flags & MCT_CONE) != 0;
+    const bool pm = (g->flags & MCT_PMATRIX) != 0;
+    MCT_REQUIRE(!pm || (cone && t->pmatrix), "mct_fdk_bp: projection matrices need cone beam and the table");
+    MCT_REQUIRE(!cone || g->nv >= 2, "mct_fdk_bp: cone beam needs at least 2 detector rows");
+    MCT_REQUIRE(cone || g->nz <= g->nv, "mct_fdk_bp: fan beam needs nz <= detector rows");
+    MCT_REQUIRE(g->u_step != 0.0f, "mct_fdk_bp: zero detector spacing");
+    BpParams p{};
+    p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views;
+    p.cone = cone; p.curved = (g->flags & MCT_CURVED) != 0;
+    p.sid = g->sid; p.sdd = g->sdd; p.img_rot = g->img_rot;
+    p.u0 = g->u0; p.inv_ustep = (float)(1.0 / (double)g->u_step);
+    p.v0 = g->v0;
+    if (cone && !pm) {
+        MCT_REQUIRE(g->v_step != 0.0f && g->dv != 0.0f, "mct_fdk_bp: zero row spacing");
+        p.kv = (float)((g->v_step > 0 ? 1.0 : -1.0) / (double)g->dv);
+    }
+    p.div = (float)div_factor(*g);
+    // voxel coordinates, run_mgfbp.py:1090-1104, as an affine map of (ix, iy, iz)
+    const double nx = g->nx, nz = g->nz, px = g->px, pz = g->pz;
+    const double cr = std::cos((double)g->img_rot), sr = std::sin((double)g->img_rot);
+    double ax[3] = {0, 0, 0}, ay[3] = {0, 0, 0}, az[3] = {0, 0, 0}, a0[3] = {0, 0, 0};  // (xa, ya, z) per unit index
+    if (g->view_mode == 1) {
+        ax[0] = px; a0[0] = -px * (nx - 1) / 2.0 + g->cx;
+        ay[1] = -px; a0[1] = px * (nx - 1) / 2.0 + g->cy;
+        az[2] = pz; a0[2] = -(nz - 1) / 2.0 * pz + g->cz;
+    } else if (g->view_mode == 2) {
+        ax[0] = px; a0[0] = -px * (nx - 1) / 2.0 + g->cx;
+        ay[2] = -px; a0[2] = px * (nx - 1) / 2.0 + g->cz;
+        az[1] = -pz; a0[1] = (nz - 1) / 2.0 * pz + g->cy;
+    } else {
+        ay[2] = -px; a0[2] = px * (nx - 1) / 2.0 + g->cz;
+        ax[1] = -px; a0[1] = px * (nx - 1) / 2.0 + g->cy;
+        az[0] = pz; a0[0] = -(nz - 1) / 2.0 * pz + g->cx;
+    }
+    auto rot = [&](const double* a, float& x, float& y, float& z) {
+        x = (float)(a[0] * cr + a[1] * sr);
+        y = (float)(-a[0] * sr + a[1] * cr);
+        z = (float)a[2];
+    };
+    rot(ax, p.px_x, p.px_y, p.px_z);
+    rot(ay, p.py_x, p.py_y, p.py_z);
+    rot(az, p.pz_x, p.pz_y, p.pz_z);
+    rot(a0, p.o_x, p.o_y, p.o_z);
+    dim3 block(BP_TX, BP_TY);
+    dim3 grid((g->nx + BP_TX - 1) / BP_TX, (g->nx + BP_TY - 1) / BP_TY, (g->nz + BP_ZC - 1) / BP_ZC);
+    cudaStream_t s = as_stream(stream);
+    const bool axial_fast = g->view_mode == 1 && !pm;
+    if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol);
+    else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
+    else if (axial_fast) launch_bp<0, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
+    else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
+    else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
+    return launched("fdk_bp_kernel");
+}

@@ -1,0 +1,309 @@
+// Sinogram weighting, vertical Gaussian, Toeplitz row filter and BP operand packing.
+//
+// Reference kernels replaced (run_mgfbp.py): BHCorrection :946-954, WeightSgm
+// :956-1011, ConvolveSgmAndKernel :1013-1046.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace mct {
+namespace {
+
+struct WeightParams {
+    int nu, nv, views, curved, short_scan, n_bh;
+    int64_t row_stride, view_stride;
+    float u0, u_step, v0, v_step, sdd, scan;
+    float num_rounds, remain;  // short-scan constants
+};
+
+// Parker / over-scan weight of one (view, column), run_mgfbp.py:971-1011.
+__device__ float parker(const WeightParams& p, float beta, float u) {
+    const float PI = (float)kPI;
+    float rot_dir = fabsf(p.scan) / p.scan;
+    float gamma = p.curved ? ((-1.0f) * u / p.sdd) * rot_dir : atan2f(-u, p.sdd) * rot_dir;
+    float gmax = p.remain - PI;
+    float nr = p.num_rounds, ra = p.remain;
+    float w = 0.0f;
+    if (ra <= PI && nr == 0.0f) {
+        w = 1.0f;
+    } else if (ra <= PI && nr >= 1.0f) {
+        if (0.0f <= beta && beta < ra) w = beta / ra;
+        else if (ra <= beta && beta < 2 * PI * nr) w = 1.0f;
+        else if (2 * PI * nr <= beta && beta <= (2 * PI * nr + ra)) w = (2 * PI * nr + ra - beta) / ra;
+    } else if (PI < ra && ra <= 2 * PI) {
+        if (0.0f <= beta && beta < (gmax - 2 * gamma)) {
+            w = sinf(PI / 2 * beta / (gmax - 2 * gamma));
+            w = w * w;
+        } else if ((gmax - 2 * gamma) <= beta && beta < (PI * (2 * nr + 1) - 2 * gamma)) {
+            w = 1.0f;
+        } else if ((PI * (2 * nr + 1) - 2 * gamma) <= beta && beta <= (PI * (2 * nr + 1) + gmax)) {
+            w = sinf(PI / 2 * (PI + gmax - (beta - PI * 2 * nr)) / (gmax + 2 * gamma));
+            w = w * w;
+        }
+    } else {
+        w = 1.0f;
+    }
+    return w;
+}
+
+__global__ void weight_kernel(WeightParams p, const float* __restrict__ in, const float* __restrict__ bh,
+                              const float* __restrict__ angles, float* __restrict__ out) {
+    int64_t n = (int64_t)p.nv * p.views * p.nu;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int c = (int)(i % p.nu);
+        int64_t rj = i / p.nu;
+        int j = (int)(rj % p.views);
+        int r = (int)(rj / p.views);
+        float val = in[r * p.row_stride + j * p.view_stride + c];
+        if (p.n_bh > 0) {
+            float acc = 0.0f, pw = val;
+            for (int t = 0; t < p.n_bh; ++t) {
+                acc += bh[t] * pw;
+                pw *= val;
+            }
+            val = acc;
+        }
+        float u = p.u0 + c * p.u_step;
+        float v = p.v0 + r * p.v_step;
+        float sdd = p.sdd;
+        if (p.curved) val = val * sdd * cosf((-1.0f) * u / sdd) * sdd / sqrtf(sdd * sdd + v * v);
+        else val = (val * sdd * sdd) / sqrtf(sdd * sdd + u * u + v * v);
+        if (p.short_scan) val *= parker(p, fabsf(angles[j] - angles[0]), u);
+        out[i] = val;
+    }
+}
+
+__global__ void vgauss_kernel(int nu, int nv, int views, float dv, const float* __restrict__ in,
+                              const float* __restrict__ g, float* __restrict__ out) {
+    int64_t n = (int64_t)nv * views * nu;
+    int64_t plane = (int64_t)views * nu;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
+        int i = (int)(idx / plane);
+        int64_t jk = idx % plane;
+        float acc = 0.0f;
+        int n0 = max(0, i - 10), n1 = min(nv - 1, i + 10);
+        for (int m = n0; m <= n1; ++m) acc += in[m * plane + jk] * g[i + (nv - 1) - m];
+        out[idx] = acc * dv;
+    }
+}
+
+// ---------------------------------------------------------------- Toeplitz filter
+// Y[R][k] = du * sum_m X[R][m] * h[k - m + nu - 1] for R = r*views + j, written to the
+// view-major output F[j][r][k].  Block tile 128 rows x 128 columns, 32-deep m slices,
+// 256 threads with an 8x8 register tile each.  Along m the Toeplitz operand is a
+// sliding window of the taps, so each thread keeps 8 taps in registers and loads one
+// new tap per m step.
+constexpr int FBM = 128, FBN = 128, FBK = 32, FAPAD = 4;
+
+__global__ void __launch_bounds__(256, 2)
+toeplitz_filter_kernel(int nu, int nv, int views, float du, const float* __restrict__ X,
+                       const float* __restrict__ h, float* __restrict__ F) {
+    __shared__ __align__(16) float As[FBK][FBM + FAPAD];
+    __shared__ float hs[FBN + FBK];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int64_t rows = (int64_t)nv * views;
+    const int64_t row0 = (int64_t)blockIdx.y * FBM;
+    const int k0 = blockIdx.x * FBN;
+    const int ntaps = 2 * nu - 1;
+
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) acc[i][jj] = 0.0f;
+
+    for (int m0 = 0; m0 < nu; m0 += FBK) {
+        // A tile: X[row0 .. +127][m0 .. +31] -> As[m][row]
+#pragma unroll
+        for (int it = 0; it < (FBM * FBK) / 256; ++it) {
+            int e = tid + it * 256;
+            int rr = e / FBK, mm = e % FBK;
+            int64_t R = row0 + rr;
+            int m = m0 + mm;
+            As[mm][rr] = (R < rows && m < nu) ? X[R * nu + m] : 0.0f;
+        }
+        // taps window: hs[i] = h[base + i], base = k0 - m0 - (FBK-1) + nu - 1
+        int base = k0 - m0 - (FBK - 1) + nu - 1;
+        for (int i = tid; i < FBN + FBK; i += 256) {
+            int hi = base + i;
+            hs[i] = (hi >= 0 && hi < ntaps) ? h[hi] : 0.0f;
+        }
+        __syncthreads();
+        float b[8];
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) b[jj] = hs[(FBK - 1) + tx * 8 + jj];
+#pragma unroll
+        for (int mm = 0; mm < FBK; ++mm) {
+            if (mm > 0) {
+#pragma unroll
+                for (int jj = 7; jj > 0; --jj) b[jj] = b[jj - 1];
+                b[0] = hs[(FBK - 1) + tx * 8 - mm];
+            }
+            float4 a0 = *reinterpret_cast<const float4*>(&As[mm][ty * 8]);
+            float4 a1 = *reinterpret_cast<const float4*>(&As[mm][ty * 8 + 4]);
+            float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) acc[i][jj] = fmaf(a[i], b[jj], acc[i][jj]);
+        }
+        __syncthreads();
+    }
+    // epilogue: scale by du, write view-major
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        int64_t R = row0 + ty * 8 + i;
+        if (R >= rows) continue;
+        int r = (int)(R / views), j = (int)(R % views);
+        float* dst = F + ((int64_t)j * nv + r) * nu;
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+            int k = k0 + tx * 8 + jj;
+            if (k < nu) dst[k] = acc[i][jj] * du;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- packing
+template <typename QT>
+__device__ __forceinline__ QT make_quad(float a, float b, float c, float d);
+template <>
+__device__ __forceinline__ float4 make_quad<float4>(float a, float b, float c, float d) {
+    return make_float4(a, b, c, d);
+}
+template <>
+__device__ __forceinline__ uint2 make_quad<uint2>(float a, float b, float c, float d) {
+    __nv_bfloat162 lo = __floats2bfloat162_rn(a, b);
+    __nv_bfloat162 hi = __floats2bfloat162_rn(c, d);
+    uint2 r;
+    r.x = *reinterpret_cast<uint32_t*>(&lo);
+    r.y = *reinterpret_cast<uint32_t*>(&hi);
+    return r;
+}
+template <typename PT>
+__device__ __forceinline__ PT make_pair(float a, float b);
+template <>
+__device__ __forceinline__ float2 make_pair<float2>(float a, float b) { return make_float2(a, b); }
+template <>
+__device__ __forceinline__ uint32_t make_pair<uint32_t>(float a, float b) {
+    __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&p);
+}
+
+// cone: Q[j][r][c] = {F[j][r][c], F[j][r][c+1], F[j][r+1][c], F[j][r+1][c+1]}, r<nv-1, c<nu-1
+template <typename QT>
+__global__ void pack_quad_kernel(int nu, int nv, int views, const float* __restrict__ F, QT* __restrict__ Q) {
+    const int nq = nu - 1, rq = nv - 1;
+    int64_t n = (int64_t)views * rq * nq;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int c = (int)(i % nq);
+        int64_t jr = i / nq;
+        int r = (int)(jr % rq);
+        int j = (int)(jr / rq);
+        const float* f = F + ((int64_t)j * nv + r) * nu + c;
+        Q[i] = make_quad<QT>(f[0], f[1], f[nu], f[nu + 1]);
+    }
+}
+
+// fan: P[j][r][c] = {F[j][r][c], F[j][r][c+1]}, c<nu-1
+template <typename PT>
+__global__ void pack_pair_kernel(int nu, int nv, int views, const float* __restrict__ F, PT* __restrict__ P) {
+    const int nq = nu - 1;
+    int64_t n = (int64_t)views * nv * nq;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int c = (int)(i % nq);
+        int64_t jr = i / nq;
+        const float* f = F + jr * nu + c;
+        P[i] = make_pair<PT>(f[0], f[1]);
+    }
+}
+
+inline int grid_for(int64_t n, int block = 256) {
+    int64_t b = (n + block - 1) / block;
+    return (int)(b < 152 * 64 ? (b < 1 ? 1 : b) : 152 * 64);
+}
+
+}  // namespace
+}  // namespace mct
+
+using namespace mct;
+
+extern "C" {
+
+int mct_weight(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t row_stride, int64_t view_stride,
+               const float* bh_coeffs, int32_t n_bh, float* weighted, void* stream) {
+    MCT_TRY(check_geom(g, "mct_weight"));
+    MCT_REQUIRE(sgm && weighted, "mct_weight: NULL buffer");
+    MCT_REQUIRE(n_bh >= 0 && (n_bh == 0 || bh_coeffs), "mct_weight: bad BH coefficients");
+    bool short_scan = (g->flags & MCT_SHORT_SCAN) != 0;
+    MCT_REQUIRE(!short_scan || (t && t->angles), "mct_weight: short scan needs the angle table");
+    WeightParams p{};
+    p.nu = g->nu; p.nv = g->nv; p.views = g->views;
+    p.curved = (g->flags & MCT_CURVED) != 0;
+    p.short_scan = short_scan;
+    p.n_bh = n_bh;
+    p.row_stride = row_stride; p.view_stride = view_stride;
+    p.u0 = g->u0; p.u_step = g->u_step; p.v0 = g->v0; p.v_step = g->v_step;
+    p.sdd = g->sdd; p.scan = g->total_scan_angle;
+    float PI = (float)kPI;
+    p.num_rounds = floorf(fabsf(p.scan) / (PI * 2));
+    p.remain = fabsf(p.scan) - p.num_rounds * PI * 2;
+    int64_t n = sgm_elems(*g);
+    weight_kernel<<<grid_for(n), 256, 0, as_stream(stream)>>>(p, sgm, bh_coeffs, t ? t->angles : nullptr, weighted);
+    return launched("weight_kernel");
+}
+
+int mct_vgauss(const mct_geom* g, const float* weighted, const float* gauss_taps, float* out, void* stream) {
+    MCT_TRY(check_geom(g, "mct_vgauss"));
+    MCT_REQUIRE(weighted && gauss_taps && out && weighted != out, "mct_vgauss: bad buffers");
+    int64_t n = sgm_elems(*g);
+    vgauss_kernel<<<grid_for(n), 256, 0, as_stream(stream)>>>(g->nu, g->nv, g->views, g->dv, weighted, gauss_taps, out);
+    return launched("vgauss_kernel");
+}
+
+int mct_filter(const mct_geom* g, const float* weighted, const float* taps, float* filtered, void* stream) {
+    MCT_TRY(check_geom(g, "mct_filter"));
+    MCT_REQUIRE(weighted && taps && filtered && weighted != filtered, "mct_filter: bad buffers");
+    int64_t rows = (int64_t)g->nv * g->views;
+    MCT_REQUIRE((rows + FBM - 1) / FBM < 2147483647LL, "mct_filter: too many rows");
+    dim3 grid((g->nu + FBN - 1) / FBN, (unsigned)((rows + FBM - 1) / FBM));
+    toeplitz_filter_kernel<<<grid, 256, 0, as_stream(stream)>>>(g->nu, g->nv, g->views, g->du, weighted, taps, filtered);
+    return launched("toeplitz_filter_kernel");
+}
+
+size_t mct_packed_size(const mct_geom* g, int32_t dtype) {
+    if (!g || g->nu < 2 || g->nv < 1 || g->views < 1) return 0;
+    size_t esz;
+    if (g->flags & MCT_CONE) {
+        if (g->nv < 2) return 0;
+        esz = dtype == MCT_BF16 ? 8 : 16;
+        return (size_t)g->views * (g->nv - 1) * (g->nu - 1) * esz;
+    }
+    esz = dtype == MCT_BF16 ? 4 : 8;
+    return (size_t)g->views * g->nv * (g->nu - 1) * esz;
+}
+
+int mct_pack(const mct_geom* g, const float* filtered, void* packed, int32_t dtype, void* stream) {
+    MCT_TRY(check_geom(g, "mct_pack"));
+    MCT_REQUIRE(filtered && packed, "mct_pack: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_pack: dtype must be MCT_F32 or MCT_BF16");
+    cudaStream_t s = as_stream(stream);
+    if (g->flags & MCT_CONE) {
+        MCT_REQUIRE(g->nv >= 2, "mct_pack: cone beam needs at least 2 detector rows");
+        int64_t n = (int64_t)g->views * (g->nv - 1) * (g->nu - 1);
+        if (dtype == MCT_F32)
+            pack_quad_kernel<float4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (float4*)packed);
+        else
+            pack_quad_kernel<uint2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (uint2*)packed);
+    } else {
+        int64_t n = (int64_t)g->views * g->nv * (g->nu - 1);
+        if (dtype == MCT_F32)
+            pack_pair_kernel<float2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (float2*)packed);
+        else
+            pack_pair_kernel<uint32_t><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (uint32_t*)packed);
+    }
+    return launched("pack_kernel");
+}
+
+}  // extern "C"

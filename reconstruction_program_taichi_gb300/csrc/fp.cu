@@ -1,0 +1,465 @@
+// Ray-driven trilinear forward projector, its exact adjoint, the effective ray map,
+// binning/noise, and analytic ellipsoid projections.
+//
+// Reference kernels replaced: Mgfpj_v3.ForwardProjectionBilinear
+// (run_mgfpj_v3.py:184-366), its masked copy in Mgfbp_ir
+// (run_mgfbp_iterative_recon_IRN_CGLS.py:494-676), the effective-map agent (:679-833),
+// BinSinogram / AddPossionNoise (run_mgfpj_v3.py:368-391).
+//
+// All views are projected in ONE launch (the reference launches once per view).
+// A ray's sample positions are affine in the step index k, so each ray first clips
+// its step range to the volume's bounding box (with a one-step margin) and then
+// applies the reference's per-sample inside test exactly; samples outside the box
+// contribute 0 in the reference too.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace mct {
+namespace {
+
+struct FpParams {
+    int nx, nz, nu, nv, views, K, cone, curved, pmat;
+    float sid, sdd, cx, cy, cz;
+    float stepvd, l_min, inv_px, inv_pz;
+    float x0, y0, zoff;  // voxel (0,0) centre x, y; z0 = zoff + cz_view
+    float zpv;
+};
+
+struct Ray {
+    float fx0, dfx, fy0, dfy, fz0, dfz;  // fractional voxel index = f0 + k*df
+    int ks, ke;                          // clipped step range [ks, ke]
+};
+
+// Ray set-up shared by all ray kernels, following run_mgfpj_v3.py:221-324.
+__device__ __forceinline__ bool setup_ray(const FpParams& p, int iu, int iv, int j, const float* __restrict__ angles,
+                                          const float* __restrict__ u_arr, const float* __restrict__ v_arr,
+                                          const float* __restrict__ czv, const float* __restrict__ pa,
+                                          const float* __restrict__ pxs, bool clip_z, Ray& r) {
+    float sb, cb;
+    sincosf(angles[j], &sb, &cb);
+    const float zj = p.zpv * (float)j;
+    const float uval = u_arr[iu];
+    float dx, dy;
+    if (p.curved) {
+        const float g = (-uval) / p.sdd;
+        float sg, cg;
+        sincosf(g, &sg, &cg);
+        dx = -p.sdd * cg + p.sid;
+        dy = -p.sdd * sg;
+    } else {
+        dx = -(p.sdd - p.sid);
+        dy = uval;
+    }
+    const float dz = v_arr[iv] + zj;
+    const float ex = dx - p.sid, ey = dy, ez = dz - zj;
+    const float dist = sqrtf(ex * ex + ey * ey + ez * ez);
+    float Ox, Oy, Oz, Dx, Dy, Dz;
+    if (p.pmat) {
+        float s0, c0;
+        sincosf(angles[0], &s0, &c0);
+        const float* A = pa + 9 * j;
+        const float* xs = pxs + 3 * j;
+        const float fu = (float)iu, fv = (float)iv;
+        const float ax = A[0] * fu + A[1] * fv + A[2];
+        const float ay = A[3] * fu + A[4] * fv + A[5];
+        const float az = A[6] * fu + A[7] * fv + A[8];
+        Ox = xs[0] * c0 - xs[1] * s0;
+        Oy = xs[1] * c0 + xs[0] * s0;
+        Oz = xs[2] + zj;
+        Dx = (ax * c0 - ay * s0) / dist;
+        Dy = (ay * c0 + ax * s0) / dist;
+        Dz = az / dist;
+    } else {
+        const float ux = ex / dist, uy = ey / dist, uz = ez / dist;
+        Ox = p.sid * cb;
+        Oy = p.sid * sb;
+        Oz = zj;
+        Dx = ux * cb - uy * sb;
+        Dy = uy * cb + ux * sb;
+        Dz = uz;
+    }
+    const float z0 = p.zoff + (czv ? czv[j] : p.cz);
+    r.fx0 = (Ox + p.l_min * Dx - p.x0) * p.inv_px;
+    r.dfx = p.stepvd * Dx * p.inv_px;
+    r.fy0 = (Oy + p.l_min * Dy - p.y0) * (-p.inv_px);
+    r.dfy = p.stepvd * Dy * (-p.inv_px);
+    r.fz0 = (Oz + p.l_min * Dz - z0) * p.inv_pz;
+    r.dfz = p.stepvd * Dz * p.inv_pz;
+    // clip k so that f in [0, n-1) on each axis (conservative by one step)
+    float klo = -1.0f, khi = (float)p.K;
+    auto clip = [&](float f0, float df, float n) -> bool {
+        if (fabsf(df) < 1e-20f) return f0 >= 0.0f && f0 < n - 1.0f;
+        float t1 = (0.0f - f0) / df, t2 = (n - 1.0f - f0) / df;
+        klo = fmaxf(klo, fminf(t1, t2));
+        khi = fminf(khi, fmaxf(t1, t2));
+        return true;
+    };
+    bool any = clip(r.fx0, r.dfx, (float)p.nx) && clip(r.fy0, r.dfy, (float)p.nx);
+    if (clip_z && p.cone) any = any && clip(r.fz0, r.dfz, (float)p.nz);
+    if (!any || !(klo <= khi)) {
+        r.ks = 0;
+        r.ke = -1;
+        return false;
+    }
+    r.ks = max(0, (int)floorf(klo) - 1);
+    r.ke = min(p.K - 1, (int)ceilf(khi) + 1);
+    return r.ks <= r.ke;
+}
+
+__global__ void __launch_bounds__(256)
+fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
+          const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
+          const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ mask,
+          float* __restrict__ sgm) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.z;
+    if (iu >= p.nu || iv >= p.nv) return;
+    const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
+    if (mask && mask[oidx] != 1.0f) {
+        sgm[oidx] = 0.0f;
+        return;
+    }
+    Ray r;
+    float acc = 0.0f;
+    if (setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) {
+        const int nx = p.nx;
+        const int64_t plane = (int64_t)nx * nx;
+        for (int k = r.ks; k <= r.ke; ++k) {
+            const float fk = (float)k;
+            const float fx = fmaf(fk, r.dfx, r.fx0);
+            const float fy = fmaf(fk, r.dfy, r.fy0);
+            const float xf = floorf(fx), yf = floorf(fy);
+            if (!(xf >= 0.0f && xf + 1.0f < (float)nx && yf >= 0.0f && yf + 1.0f < (float)nx)) continue;
+            const float xw = fx - xf, yw = fy - yf;
+            int zi;
+            float zw = 0.0f;
+            if (p.cone) {
+                const float fz = fmaf(fk, r.dfz, r.fz0);
+                const float zf = floorf(fz);
+                if (!(zf >= 0.0f && zf + 1.0f < (float)p.nz)) continue;
+                zi = (int)zf;
+                zw = fz - zf;
+            } else {
+                zi = iv;
+            }
+            const float* b = vol + (int64_t)zi * plane + (int64_t)(int)yf * nx + (int)xf;
+            const float a00 = __ldg(b), a01 = __ldg(b + 1), a10 = __ldg(b + nx), a11 = __ldg(b + nx + 1);
+            const float l0 = fmaf(xw, a01 - a00, a00);
+            const float l1 = fmaf(xw, a11 - a10, a10);
+            float val = fmaf(yw, l1 - l0, l0);
+            if (p.cone) {
+                const float* c = b + plane;
+                const float c00 = __ldg(c), c01 = __ldg(c + 1), c10 = __ldg(c + nx), c11 = __ldg(c + nx + 1);
+                const float m0 = fmaf(xw, c01 - c00, c00);
+                const float m1 = fmaf(xw, c11 - c10, c10);
+                const float hi = fmaf(yw, m1 - m0, m0);
+                val = fmaf(zw, hi - val, val);
+            }
+            acc += val;
+        }
+    }
+    sgm[oidx] = acc * p.stepvd;
+}
+
+// Exact transpose of fp_kernel: every in-volume sample scatters its trilinear weights
+// times the ray value into the volume.
+__global__ void __launch_bounds__(256)
+fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
+                  const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
+                  const float* __restrict__ pxs, const float* __restrict__ sgm, const float* __restrict__ mask,
+                  float* __restrict__ vol) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.z;
+    if (iu >= p.nu || iv >= p.nv) return;
+    const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
+    if (mask && mask[oidx] != 1.0f) return;
+    const float yv = sgm[oidx] * p.stepvd;
+    if (yv == 0.0f) return;
+    Ray r;
+    if (!setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) return;
+    const int nx = p.nx;
+    const int64_t plane = (int64_t)nx * nx;
+    for (int k = r.ks; k <= r.ke; ++k) {
+        const float fk = (float)k;
+        const float fx = fmaf(fk, r.dfx, r.fx0);
+        const float fy = fmaf(fk, r.dfy, r.fy0);
+        const float xf = floorf(fx), yf = floorf(fy);
+        if (!(xf >= 0.0f && xf + 1.0f < (float)nx && yf >= 0.0f && yf + 1.0f < (float)nx)) continue;
+        const float xw = fx - xf, yw = fy - yf;
+        int zi;
+        float zw = 0.0f;
+        if (p.cone) {
+            const float fz = fmaf(fk, r.dfz, r.fz0);
+            const float zf = floorf(fz);
+            if (!(zf >= 0.0f && zf + 1.0f < (float)p.nz)) continue;
+            zi = (int)zf;
+            zw = fz - zf;
+        } else {
+            zi = iv;
+        }
+        float* b = vol + (int64_t)zi * plane + (int64_t)(int)yf * nx + (int)xf;
+        const float wl = p.cone ? (1.0f - zw) * yv : yv;
+        const float w00 = (1.0f - xw) * (1.0f - yw), w01 = xw * (1.0f - yw);
+        const float w10 = (1.0f - xw) * yw, w11 = xw * yw;
+        atomicAdd(b, w00 * wl);
+        atomicAdd(b + 1, w01 * wl);
+        atomicAdd(b + nx, w10 * wl);
+        atomicAdd(b + nx + 1, w11 * wl);
+        if (p.cone) {
+            const float wh = zw * yv;
+            float* c = b + plane;
+            atomicAdd(c, w00 * wh);
+            atomicAdd(c + 1, w01 * wh);
+            atomicAdd(c + nx, w10 * wh);
+            atomicAdd(c + nx + 1, w11 * wh);
+        }
+    }
+}
+
+// Effective ray map, run_mgfbp_iterative_recon_IRN_CGLS.py:749-833.
+__global__ void __launch_bounds__(256)
+emap_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
+            const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
+            const float* __restrict__ pxs, float* __restrict__ mask) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.z;
+    if (iu >= p.nu || iv >= p.nv) return;
+    const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
+    float m = 1.0f;
+    Ray r;
+    if (p.cone && setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, false, r)) {
+        const float h = (float)p.nx / 2.0f;
+        for (int k = r.ks; k <= r.ke; ++k) {
+            const float fk = (float)k;
+            const float xf = floorf(fmaf(fk, r.dfx, r.fx0));
+            const float yf = floorf(fmaf(fk, r.dfy, r.fy0));
+            if (!(xf >= 0.0f && xf + 1.0f < (float)p.nx && yf >= 0.0f && yf + 1.0f < (float)p.nx)) continue;
+            if ((xf - h) * (xf - h) + (yf - h) * (yf - h) < h * h) {
+                const float zf = floorf(fmaf(fk, r.dfz, r.fz0));
+                if (zf < 0.0f || zf + 1.0f >= (float)p.nz) {
+                    m = 0.0f;
+                    break;
+                }
+            }
+        }
+    }
+    mask[oidx] = m;
+}
+
+// Number of in-volume trilinear samples (the forward projector's algorithmic work).
+__global__ void __launch_bounds__(256)
+fp_count_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
+                const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
+                const float* __restrict__ pxs, const float* __restrict__ mask, unsigned long long* __restrict__ count) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.z;
+    unsigned long long c = 0;
+    Ray r;
+    if (iu < p.nu && iv < p.nv && !(mask && mask[((int64_t)iv * p.views + j) * p.nu + iu] != 1.0f) &&
+        setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) {
+        for (int k = r.ks; k <= r.ke; ++k) {
+            const float fk = (float)k;
+            const float xf = floorf(fmaf(fk, r.dfx, r.fx0)), yf = floorf(fmaf(fk, r.dfy, r.fy0));
+            if (!(xf >= 0.0f && xf + 1.0f < (float)p.nx && yf >= 0.0f && yf + 1.0f < (float)p.nx)) continue;
+            if (p.cone) {
+                const float zf = floorf(fmaf(fk, r.dfz, r.fz0));
+                if (!(zf >= 0.0f && zf + 1.0f < (float)p.nz)) continue;
+            }
+            ++c;
+        }
+    }
+    // warp-aggregate, one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Oversample binning + Gaussian-approximated photon noise, run_mgfpj_v3.py:368-391.
+__global__ void bin_noise_kernel(int64_t n_out, int nu, int bin, float photons, uint64_t seed,
+                                 const float* __restrict__ in, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_out; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t rowv = i / nu;
+        const int c = (int)(i % nu);
+        const float* src = in + rowv * (int64_t)nu * bin + (int64_t)c * bin;
+        float s = 0.0f;
+        for (int b = 0; b < bin; ++b) s += src[b];
+        float val = s / (float)bin;
+        if (photons > 0.0f) {
+            uint64_t h1 = splitmix64(seed ^ (uint64_t)(2 * i));
+            uint64_t h2 = splitmix64(seed ^ (uint64_t)(2 * i + 1) ^ 0x5851F42D4C957F2Dull);
+            float u1 = ((h1 >> 40) + 1.0f) * (1.0f / 16777217.0f);
+            float u2 = (h2 >> 40) * (1.0f / 16777216.0f);
+            float g = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+            float t = photons * expf(-val);
+            t = t + g * sqrtf(t);
+            if (t <= 0.0f) t = 1e-6f;
+            val = logf(photons / t);
+        }
+        out[i] = val;
+    }
+}
+
+// Exact line integrals of rotated ellipsoids along the forward projector's rays.
+__global__ void __launch_bounds__(256)
+ellipsoid_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
+                 const float* __restrict__ v_arr, const float* __restrict__ ell, int n_ell,
+                 float* __restrict__ sgm) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.z;
+    if (iu >= p.nu || iv >= p.nv) return;
+    float sb, cb;
+    sincosf(angles[j], &sb, &cb);
+    const float zj = p.zpv * (float)j;
+    const float uval = u_arr[iu];
+    float dx, dy;
+    if (p.curved) {
+        float sg, cg;
+        sincosf((-uval) / p.sdd, &sg, &cg);
+        dx = -p.sdd * cg + p.sid;
+        dy = -p.sdd * sg;
+    } else {
+        dx = -(p.sdd - p.sid);
+        dy = uval;
+    }
+    const float ex = dx - p.sid, ey = dy, ez = v_arr[iv];
+    const float dist = sqrtf(ex * ex + ey * ey + ez * ez);
+    const double ux = ex / dist, uy = ey / dist, uz = ez / dist;
+    // source and direction in the object frame (object rotated by +beta)
+    const double Ox = p.sid * (double)cb, Oy = p.sid * (double)sb, Oz = zj;
+    const double Dx = ux * cb - uy * sb, Dy = uy * cb + ux * sb, Dz = uz;
+    double total = 0.0;
+    for (int e = 0; e < n_ell; ++e) {
+        const float* E = ell + 10 * e;
+        const double cph = cos((double)E[6]), sph = sin((double)E[6]);
+        const double qx = Ox - E[0], qy = Oy - E[1], qz = Oz - E[2];
+        const double px_ = (qx * cph + qy * sph) / E[3], py_ = (-qx * sph + qy * cph) / E[4], pz_ = qz / E[5];
+        const double dx_ = (Dx * cph + Dy * sph) / E[3], dy_ = (-Dx * sph + Dy * cph) / E[4], dz_ = Dz / E[5];
+        const double a = dx_ * dx_ + dy_ * dy_ + dz_ * dz_;
+        const double b = px_ * dx_ + py_ * dy_ + pz_ * dz_;
+        const double c = px_ * px_ + py_ * py_ + pz_ * pz_ - 1.0;
+        const double disc = b * b - a * c;
+        if (disc > 0.0) total += E[9] * 2.0 * sqrt(disc) / a;
+    }
+    sgm[((int64_t)iv * p.views + j) * p.nu + iu] = (float)total;
+}
+
+int make_params(const mct_geom* g, FpParams& p, const char* who) {
+    MCT_TRY(check_geom(g, who));
+    p = FpParams{};
+    p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views; p.K = g->fp_steps;
+    p.cone = (g->flags & MCT_CONE) != 0;
+    p.curved = (g->flags & MCT_CURVED) != 0;
+    p.pmat = (g->flags & MCT_PMATRIX) != 0;
+    MCT_REQUIRE(p.K >= 0, "%s: negative step count", who);
+    MCT_REQUIRE(g->views <= 65535, "%s: at most 65535 views per launch", who);
+    MCT_REQUIRE(p.cone || g->nz >= g->nv, "%s: fan beam needs one image slice per detector row", who);
+    MCT_REQUIRE(!p.cone || g->pz > 0.0f, "%s: cone beam needs a positive voxel height", who);
+    MCT_REQUIRE(g->px > 0.0f, "%s: pixel size must be positive", who);
+    p.sid = g->sid; p.sdd = g->sdd; p.cx = g->cx; p.cy = g->cy; p.cz = g->cz;
+    // run_mgfpj_v3.py:210-239 in double, then rounded
+    const double px = g->px, pz = p.cone ? g->pz : 0.0;
+    const double img_dimension = g->nx * px, image_dimension_z = g->nz * (double)g->pz;
+    const double vd = std::sqrt(2 * px * px + (double)g->pz * g->pz);
+    p.stepvd = (float)(g->fp_step * vd);
+    p.l_min = (float)(g->sid - std::sqrt(2 * img_dimension * img_dimension + image_dimension_z * image_dimension_z) / 2.0);
+    p.inv_px = (float)(1.0 / px);
+    p.inv_pz = p.cone ? (float)(1.0 / pz) : 0.0f;
+    p.x0 = (float)(-(g->nx - 1.0) / 2.0 * px + g->cx);
+    p.y0 = (float)(-(g->nx - 1.0) / 2.0 * (-px) + g->cy);
+    p.zoff = (float)(-(g->nz - 1.0) / 2.0 * (double)g->pz);
+    p.zpv = g->fp_z_per_view;
+    return MCT_OK;
+}
+
+}  // namespace
+}  // namespace mct
+
+using namespace mct;
+
+extern "C" {
+
+int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* stream) {
+    FpParams p;
+    MCT_TRY(make_params(g, p, "mct_fp"));
+    MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp: NULL buffer");
+    MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp: projection-matrix tables missing");
+    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    fp_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
+                                                     mask, sgm);
+    return launched("fp_kernel");
+}
+
+int mct_fp_adjoint(const mct_geom* g, const mct_tables* t, const float* sgm, const float* mask, float* vol,
+                   void* stream) {
+    FpParams p;
+    MCT_TRY(make_params(g, p, "mct_fp_adjoint"));
+    MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp_adjoint: NULL buffer");
+    MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp_adjoint: projection-matrix tables missing");
+    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    fp_adjoint_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
+                                                             sgm, mask, vol);
+    return launched("fp_adjoint_kernel");
+}
+
+int mct_fp_count_samples(const mct_geom* g, const mct_tables* t, const float* mask, uint64_t* count, void* stream) {
+    FpParams p;
+    MCT_TRY(make_params(g, p, "mct_fp_count_samples"));
+    MCT_REQUIRE(t && t->angles && t->u && t->v && count, "mct_fp_count_samples: NULL buffer");
+    MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp_count_samples: projection-matrix tables missing");
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint64_t), as_stream(stream));
+    if (e != cudaSuccess) {
+        set_error("mct_fp_count_samples: %s", cudaGetErrorString(e));
+        return MCT_E_CUDA;
+    }
+    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    fp_count_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, mask,
+                                                           (unsigned long long*)count);
+    return launched("fp_count_kernel");
+}
+
+int mct_effective_map(const mct_geom* g, const mct_tables* t, float* mask, void* stream) {
+    FpParams p;
+    MCT_TRY(make_params(g, p, "mct_effective_map"));
+    MCT_REQUIRE(t && t->angles && t->u && t->v && mask, "mct_effective_map: NULL buffer");
+    MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_effective_map: projection-matrix tables missing");
+    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    emap_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, mask);
+    return launched("emap_kernel");
+}
+
+int mct_bin_noise(const mct_geom* g, const float* in, int32_t bin, float photons, uint64_t seed, float* out,
+                  void* stream) {
+    MCT_TRY(check_geom(g, "mct_bin_noise"));
+    MCT_REQUIRE(in && out && bin >= 1, "mct_bin_noise: bad arguments");
+    MCT_REQUIRE(bin == 1 || in != out, "mct_bin_noise: binning cannot run in place");
+    int64_t n = sgm_elems(*g);
+    int64_t blocks = (n + 255) / 256;
+    bin_noise_kernel<<<(int)(blocks < 152 * 64 ? (blocks < 1 ? 1 : blocks) : 152 * 64), 256, 0, as_stream(stream)>>>(
+        n, g->nu, bin, photons, seed, in, out);
+    return launched("bin_noise_kernel");
+}
+
+int mct_project_ellipsoids(const mct_geom* g, const mct_tables* t, const float* ell, int32_t n_ell, float* sgm,
+                           void* stream) {
+    FpParams p;
+    MCT_TRY(make_params(g, p, "mct_project_ellipsoids"));
+    MCT_REQUIRE(t && t->angles && t->u && t->v && ell && sgm && n_ell >= 0, "mct_project_ellipsoids: bad arguments");
+    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    ellipsoid_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, ell, n_ell, sgm);
+    return launched("ellipsoid_kernel");
+}
+
+}  // extern "C"

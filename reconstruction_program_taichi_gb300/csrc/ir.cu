@@ -1,0 +1,347 @@
+// Iterative-reconstruction kernels: the reference CGLS backprojector, TV operators,
+// float64 reductions and fused CGLS vector updates.
+//
+// Reference code replaced (run_mgfbp_iterative_recon_IRN_CGLS.py):
+// BackProjectionPixelDrivenPerView :372-474 + SetTruncatedRegionToZero :477-481,
+// GenerateWR :234-243, TVPenaltyVal :245-254, Dt_W_D :267-286, and the NumPy vector
+// algebra of TikhonovSol :188-232.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace mct {
+namespace {
+
+constexpr int UB_TX = 32, UB_TY = 8, UB_ZC = 8, UB_VCHUNK = 512;
+constexpr int RED_BLOCKS = 152 * 4, RED_THREADS = 256;
+
+struct UbParams {
+    int nx, nz, nu, nv, views, cone, curved;
+    float sid, sdd, img_rot, px;
+    float u0, inv_ustep, v0, kv;
+    float ex_x, ex_y, ey_x, ey_y, ez_x, ez_y;  // (x, y) per unit (ix, iy, iz), rotated
+    float o_x, o_y;
+    float zx, zy, zz, z0;                      // z (without the per-view centre) per unit index
+};
+
+// All views of the per-view backprojector, accumulated in registers in view order.
+__global__ void __launch_bounds__(UB_TX* UB_TY)
+bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
+                    const float* __restrict__ sgm, float* __restrict__ vol) {
+    __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, unused}
+    const int ix = blockIdx.x * UB_TX + threadIdx.x;
+    const int iy = blockIdx.y * UB_TY + threadIdx.y;
+    const int zb = blockIdx.z * UB_ZC;
+    const int tid = threadIdx.y * UB_TX + threadIdx.x;
+    const bool active = ix < p.nx && iy < p.nx;
+    const float bx = p.o_x + ix * p.ex_x + iy * p.ey_x + zb * p.ez_x;
+    const float by = p.o_y + ix * p.ex_y + iy * p.ey_y + zb * p.ez_y;
+    const float bz = p.z0 + ix * p.zx + iy * p.zy + zb * p.zz;
+    const int64_t rowstride = (int64_t)p.views * p.nu;
+    float acc[UB_ZC];
+#pragma unroll
+    for (int k = 0; k < UB_ZC; ++k) acc[k] = 0.0f;
+    uint32_t trunc = 0;
+
+    for (int jc = 0; jc < p.views; jc += UB_VCHUNK) {
+        const int nvc = min(UB_VCHUNK, p.views - jc);
+        __syncthreads();
+        for (int q = tid; q < nvc; q += UB_TX * UB_TY) {
+            float s, c;
+            sincosf(angles[jc + q] - p.img_rot, &s, &c);
+            tab[q] = make_float4(c, s, czv ? czv[jc + q] : cz_const, 0.0f);
+        }
+        __syncthreads();
+        if (!active) continue;
+        for (int q = 0; q < nvc; ++q) {
+            const int j = jc + q;
+            const float4 tb = tab[q];
+            const float cb = tb.x, sb = tb.y;
+            const float scb = p.sid * cb, ssb = p.sid * sb;
+#pragma unroll
+            for (int k = 0; k < UB_ZC; ++k) {
+                if (zb + k >= p.nz) continue;
+                const float x = fmaf((float)k, p.ez_x, bx);
+                const float y = fmaf((float)k, p.ez_y, by);
+                const float z = fmaf((float)k, p.zz, bz) + tb.z;
+                const float L = p.sid - x * cb - y * sb;
+                const float qx = x - scb, qy = y - ssb;
+                const float aqx = fabsf(qx), aqy = fabsf(qy);
+                const float dfac = sqrtf(qx * qx + qy * qy + z * z) / (aqx > aqy ? aqx : aqy);
+                const float mag = p.sdd / L;
+                const float t = -x * sb + y * cb;
+                const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
+                const float ui = (u - p.u0) * p.inv_ustep;
+                if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {
+                    trunc |= 1u << k;
+                    continue;
+                }
+                const float uf = floorf(ui);
+                const float ru = ui - uf;
+                const int uc = (int)uf;
+                const float w = dfac * p.px;
+                if (p.cone) {
+                    const float vi = (mag * z - p.v0) * p.kv;
+                    const float vf = floorf(vi);
+                    if (!(vf >= 0.0f && vf + 1.0f <= (float)(p.nv - 1))) continue;
+                    const float rv = vi - vf;
+                    const float* s0 = sgm + (int64_t)(int)vf * rowstride + (int64_t)j * p.nu + uc;
+                    const float a = __ldg(s0), b = __ldg(s0 + 1), c = __ldg(s0 + rowstride), d = __ldg(s0 + rowstride + 1);
+                    const float p0 = a * (1 - ru) + b * ru;
+                    const float p1 = c * (1 - ru) + d * ru;
+                    acc[k] += ((1 - rv) * p0 + rv * p1) * w;
+                } else {
+                    const float* s0 = sgm + (int64_t)(zb + k) * rowstride + (int64_t)j * p.nu + uc;
+                    acc[k] += ((1 - ru) * __ldg(s0) + ru * __ldg(s0 + 1)) * w;
+                }
+            }
+        }
+    }
+    if (!active) return;
+    const int64_t plane = (int64_t)p.nx * p.nx;
+#pragma unroll
+    for (int k = 0; k < UB_ZC; ++k)
+        if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = ((trunc >> k) & 1u) ? 0.0f : acc[k];
+}
+
+// Forward differences (y, x, z) with zero at the far edge; z only when nz > 2.
+struct Grad {
+    float gy, gx, gz;
+};
+__device__ __forceinline__ Grad grad_at(const float* __restrict__ x, int nx, int nz, int iz, int iy, int ix) {
+    const int64_t plane = (int64_t)nx * nx;
+    const int64_t i = (int64_t)iz * plane + (int64_t)iy * nx + ix;
+    const float c = x[i];
+    Grad g;
+    g.gy = (iy < nx - 1) ? x[i + nx] - c : 0.0f;
+    g.gx = (ix < nx - 1) ? x[i + 1] - c : 0.0f;
+    g.gz = (nz > 2 && iz < nz - 1) ? x[i + plane] - c : 0.0f;
+    return g;
+}
+
+__global__ void tv_weights_kernel(int nx, int nz, float beta, const float* __restrict__ x, float* __restrict__ wr) {
+    const int64_t n = (int64_t)nz * nx * nx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % nx);
+        const int iy = (int)((i / nx) % nx);
+        const int iz = (int)(i / ((int64_t)nx * nx));
+        Grad g = grad_at(x, nx, nz, iz, iy, ix);
+        wr[i] = 1.0f / sqrtf(g.gy * g.gy + g.gx * g.gx + g.gz * g.gz + beta);
+    }
+}
+
+// out = a*out_in + s * (D^T W D x), run_mgfbp_iterative_recon_IRN_CGLS.py:267-286.
+__global__ void dtwd_kernel(int nx, int nz, const float* __restrict__ x, const float* __restrict__ wr, float s,
+                            const float* __restrict__ out_in, float a, float* __restrict__ out) {
+    const int64_t n = (int64_t)nz * nx * nx;
+    const int64_t plane = (int64_t)nx * nx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % nx);
+        const int iy = (int)((i / nx) % nx);
+        const int iz = (int)(i / plane);
+        const float c = x[i];
+        float r = 0.0f;
+        if (iy >= 1 && iy <= nx - 2) {  // uxx = Ux[y] - Ux[y-1]
+            const float ux_c = wr[i] * (x[i + nx] - c);
+            const float ux_m = wr[i - nx] * (c - x[i - nx]);
+            r -= ux_c - ux_m;
+        }
+        if (ix >= 1 && ix <= nx - 2) {
+            const float uy_c = wr[i] * (x[i + 1] - c);
+            const float uy_m = wr[i - 1] * (c - x[i - 1]);
+            r -= uy_c - uy_m;
+        }
+        if (nz > 2 && iz >= 1 && iz <= nz - 2) {
+            const float uz_c = wr[i] * (x[i + plane] - c);
+            const float uz_m = wr[i - plane] * (c - x[i - plane]);
+            r -= uz_c - uz_m;
+        }
+        float v = s * r;
+        if (a != 0.0f) v += a * out_in[i];
+        out[i] = v;
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double red[RED_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    v = (threadIdx.x < RED_THREADS / 32) ? red[threadIdx.x] : 0.0;
+    if (w == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+dot_partial_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t n, double* __restrict__ partials) {
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS)
+        s += (double)a[i] * (double)b[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+tv_partial_kernel(int nx, int nz, float beta, const float* __restrict__ x, double* __restrict__ partials) {
+    const int64_t n = (int64_t)nz * nx * nx;
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS) {
+        const int ix = (int)(i % nx);
+        const int iy = (int)((i / nx) % nx);
+        const int iz = (int)(i / ((int64_t)nx * nx));
+        Grad g = grad_at(x, nx, nz, iz, iy, ix);
+        s += sqrt((double)g.gy * g.gy + (double)g.gx * g.gx + (double)g.gz * g.gz + (double)beta);
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+finish_sum_kernel(const double* __restrict__ partials, int n, double* __restrict__ result) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += RED_THREADS) s += partials[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) *result = s;
+}
+
+// x += alpha d; r -= alpha q; partial sums of r^2 (alpha = rr/dq read on device)
+__global__ void __launch_bounds__(RED_THREADS)
+cgls_update_kernel(int64_t n, const double* __restrict__ rr, const double* __restrict__ dq, float* __restrict__ x,
+                   float* __restrict__ r, const float* __restrict__ d, const float* __restrict__ q,
+                   double* __restrict__ partials) {
+    const float alpha = (float)(*rr / *dq);
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS) {
+        const float di = d[i];
+        x[i] = x[i] + alpha * di;
+        const float ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        s += (double)ri * (double)ri;
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void cgls_direction_kernel(int64_t n, const double* __restrict__ rr, const double* __restrict__ rr_new,
+                                      const float* __restrict__ r, float* __restrict__ d) {
+    const float beta = (float)(*rr_new / *rr);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = r[i] + beta * d[i];
+}
+
+inline int ew_grid(int64_t n) {
+    int64_t b = (n + 255) / 256;
+    return (int)(b < 152 * 32 ? (b < 1 ? 1 : b) : 152 * 32);
+}
+
+}  // namespace
+}  // namespace mct
+
+using namespace mct;
+
+extern "C" {
+
+int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sgm, float* vol, void* stream) {
+    MCT_TRY(check_geom(g, "mct_bp_ref_unmatched"));
+    MCT_REQUIRE(t && t->angles && sgm && vol, "mct_bp_ref_unmatched: NULL buffer");
+    MCT_REQUIRE(!(g->flags & MCT_PMATRIX), "mct_bp_ref_unmatched: projection-matrix geometry is not supported");
+    const bool cone = (g->flags & MCT_CONE) != 0;
+    MCT_REQUIRE(!cone || g->nv >= 2, "mct_bp_ref_unmatched: cone beam needs at least 2 rows");
+    MCT_REQUIRE(cone || g->nz <= g->nv, "mct_bp_ref_unmatched: fan beam needs nz <= detector rows");
+    MCT_REQUIRE(g->u_step != 0.0f, "mct_bp_ref_unmatched: zero detector spacing");
+    UbParams p{};
+    p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views;
+    p.cone = cone; p.curved = (g->flags & MCT_CURVED) != 0;
+    p.sid = g->sid; p.sdd = g->sdd; p.img_rot = g->img_rot; p.px = g->px;
+    p.u0 = g->u0; p.inv_ustep = (float)(1.0 / (double)g->u_step);
+    p.v0 = g->v0;
+    if (cone) {
+        MCT_REQUIRE(g->v_step != 0.0f && g->dv != 0.0f, "mct_bp_ref_unmatched: zero row spacing");
+        p.kv = (float)((g->v_step > 0 ? 1.0 : -1.0) / (double)g->dv);
+    }
+    // voxel coordinates, run_mgfbp_iterative_recon_IRN_CGLS.py:386-401 (z without the
+    // per-view centre, which is added per view)
+    const double nx = g->nx, nz = g->nz, px = g->px, pz = g->pz;
+    const double cr = std::cos((double)g->img_rot), sr = std::sin((double)g->img_rot);
+    double ax[3] = {0, 0, 0}, ay[3] = {0, 0, 0}, az[3] = {0, 0, 0}, a0[3] = {0, 0, 0};
+    if (g->view_mode == 1) {
+        ax[0] = px; a0[0] = -px * (nx - 1) / 2.0 + g->cx;
+        ay[1] = -px; a0[1] = px * (nx - 1) / 2.0 + g->cy;
+        az[2] = pz; a0[2] = -(nz - 1) / 2.0 * pz;
+    } else if (g->view_mode == 2) {
+        ax[0] = px; a0[0] = -px * (nx - 1) / 2.0 + g->cx;
+        ay[2] = -px; a0[2] = px * (nx - 1) / 2.0;
+        az[1] = -pz; a0[1] = (nz - 1) / 2.0 * pz + g->cy;
+    } else {
+        ay[2] = -px; a0[2] = px * (nx - 1) / 2.0;
+        ax[1] = -px; a0[1] = px * (nx - 1) / 2.0 + g->cy;
+        az[0] = pz; a0[0] = -(nz - 1) / 2.0 * pz + g->cx;
+    }
+    auto rx = [&](const double* a) { return (float)(a[0] * cr + a[1] * sr); };
+    auto ry = [&](const double* a) { return (float)(-a[0] * sr + a[1] * cr); };
+    p.ex_x = rx(ax); p.ex_y = ry(ax); p.ey_x = rx(ay); p.ey_y = ry(ay); p.ez_x = rx(az); p.ez_y = ry(az);
+    p.o_x = rx(a0); p.o_y = ry(a0);
+    p.zx = (float)ax[2]; p.zy = (float)ay[2]; p.zz = (float)az[2]; p.z0 = (float)a0[2];
+    dim3 block(UB_TX, UB_TY);
+    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
+    bp_unmatched_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz, sgm, vol);
+    return launched("bp_unmatched_kernel");
+}
+
+int mct_tv_weights(const mct_geom* g, const float* x, float beta, float* wr, void* stream) {
+    MCT_REQUIRE(g && x && wr && x != wr && g->nx >= 1 && g->nz >= 1, "mct_tv_weights: bad arguments");
+    tv_weights_kernel<<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, beta, x, wr);
+    return launched("tv_weights_kernel");
+}
+
+int mct_dtwd(const mct_geom* g, const float* x, const float* wr, float s, const float* out_in, float a, float* out,
+             void* stream) {
+    MCT_REQUIRE(g && x && wr && out && out != x && out != wr && g->nx >= 1 && g->nz >= 1, "mct_dtwd: bad arguments");
+    MCT_REQUIRE(a == 0.0f || out_in, "mct_dtwd: out_in is NULL");
+    dtwd_kernel<<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, x, wr, s, out_in, a, out);
+    return launched("dtwd_kernel");
+}
+
+size_t mct_reduce_scratch_size(void) { return (size_t)RED_BLOCKS * sizeof(double); }
+
+int mct_tv_penalty(const mct_geom* g, const float* x, float beta, double* partials, double* result, void* stream) {
+    MCT_REQUIRE(g && x && partials && result, "mct_tv_penalty: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    tv_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(g->nx, g->nz, beta, x, partials);
+    MCT_TRY(launched("tv_partial_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, s>>>(partials, RED_BLOCKS, result);
+    return launched("finish_sum_kernel");
+}
+
+int mct_dot_f64(const float* a, const float* b, int64_t n, double* partials, double* result, void* stream) {
+    MCT_REQUIRE(a && b && partials && result && n >= 0, "mct_dot_f64: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n, partials);
+    MCT_TRY(launched("dot_partial_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, s>>>(partials, RED_BLOCKS, result);
+    return launched("finish_sum_kernel");
+}
+
+int mct_cgls_update(int64_t n, const double* rr, const double* dq, float* x, float* r, const float* d, const float* q,
+                    double* partials, double* rr_new, void* stream) {
+    MCT_REQUIRE(rr && dq && x && r && d && q && partials && rr_new && n >= 0, "mct_cgls_update: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    cgls_update_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, rr, dq, x, r, d, q, partials);
+    MCT_TRY(launched("cgls_update_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, s>>>(partials, RED_BLOCKS, rr_new);
+    return launched("finish_sum_kernel");
+}
+
+int mct_cgls_direction(int64_t n, const double* rr, const double* rr_new, const float* r, float* d, void* stream) {
+    MCT_REQUIRE(rr && rr_new && r && d && n >= 0, "mct_cgls_direction: bad arguments");
+    cgls_direction_kernel<<<ew_grid(n), 256, 0, as_stream(stream)>>>(n, rr, rr_new, r, d);
+    return launched("cgls_direction_kernel");
+}
+
+}  // extern "C"

@@ -1,0 +1,176 @@
+"""FBP / FDK drop-in: run_mgfbp(config_path) and class Mgfbp, mirroring
+run_mgfbp.py:18-85 (entry point and MainFunction) on the GB300 kernels.
+
+Every reconstruction runs as: weighting (+BH) -> [vertical Gaussian] -> Toeplitz row
+filter -> packing -> backprojection, all on one CUDA stream with the sinogram,
+filtered sinogram and volume resident in HBM.
+"""
+import gc
+import os
+import re
+import time
+
+import numpy as np
+import torch
+
+from . import ops
+from ._lib import MCT_BF16, MCT_F32
+from .config import ConfigError, ReadConfigFile, parse_fbp
+from .geometry import fbp_geometry, gaussian_taps, recon_taps
+from .io import imwriteRaw, imwriteTiff, read_sinogram_file, read_sinogram_raw_layout
+
+STORAGE = {"f32": MCT_F32, "float32": MCT_F32, "bf16": MCT_BF16, "bfloat16": MCT_BF16}
+
+
+def _device(device=None):
+    if not torch.cuda.is_available():
+        raise RuntimeError("a CUDA device is required (this package has no CPU fallback)")
+    return torch.device(device or "cuda")
+
+
+class FdkPipeline:
+    """Weight -> filter -> pack -> backproject for one FBP geometry, with reusable
+    device buffers.  `storage` selects the backprojection operand precision:
+    'f32' (plain) or 'bf16' (mixed precision storage)."""
+
+    def __init__(self, obj, device=None, storage="f32"):
+        dev = _device(device)
+        self.obj = obj
+        self.dg = fbp_geometry(obj, dev)
+        self.device = dev
+        self.dtype = STORAGE[storage]
+        self.kernel_none = obj.kernel_name == "None"
+        f32 = dict(dtype=torch.float32, device=dev)
+        self.taps = None if self.kernel_none else torch.tensor(recon_taps(obj), **f32)
+        self.gauss_v = None
+        if obj.apply_gauss_vertical:
+            self.gauss_v = torch.tensor(gaussian_taps(obj.det_elem_count_vertical_actual, obj.det_elem_height,
+                                                      obj.det_elem_vertical_gauss_filter_size), **f32)
+        self.bh = torch.tensor(obj.array_bh_coefficients, **f32) if obj.bool_bh_correction else None
+        g = self.dg.geom
+        self.weighted = torch.empty(self.dg.sgm_shape, **f32)
+        self.smoothed = torch.empty(self.dg.sgm_shape, **f32) if self.gauss_v is not None else None
+        self.filtered = torch.empty((g.views, g.nv, g.nu), **f32)
+        self.packed = torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16), dtype=torch.uint8, device=dev)
+        self.vol = torch.empty(self.dg.vol_shape, **f32)
+
+    def filter(self, sgm, row_stride=None, view_stride=None):
+        """Weighted and filtered view-major sinogram [views, rows, cols]."""
+        g = self.dg.geom
+        if row_stride is None:
+            row_stride, view_stride = g.views * g.nu, g.nu
+        w = ops.weight(self.dg, sgm, row_stride, view_stride, self.bh, out=self.weighted)
+        if self.gauss_v is not None:
+            w = ops.vgauss(self.dg, w, self.gauss_v, out=self.smoothed)
+        if self.kernel_none:
+            self.filtered.copy_(w.permute(1, 0, 2))
+            return self.filtered
+        return ops.filter_rows(self.dg, w, self.taps, out=self.filtered)
+
+    def backproject(self, filtered, out=None):
+        packed = ops.pack(self.dg, filtered, self.dtype, out=self.packed)
+        return ops.fdk_bp(self.dg, packed, self.dtype, out=self.vol if out is None else out)
+
+    def run(self, sgm, row_stride=None, view_stride=None, out=None):
+        """Full FBP of a device sinogram (default layout [rows, views, cols])."""
+        return self.backproject(self.filter(sgm, row_stride, view_stride), out)
+
+
+class Mgfbp:
+    """Drop-in for the reference class Mgfbp (run_mgfbp.py:50-1310)."""
+
+    def __init__(self, config_dict, device=None, storage="f32", verbose=True):
+        self.verbose = verbose
+        parse_fbp(self, config_dict)
+        self.img_recon = np.zeros((self.img_dim_z, self.img_dim, self.img_dim), dtype=np.float32)
+        self.device = device
+        self.storage = storage
+        self.file_processed_count = 0
+        self._pipe = None
+
+    def _log(self, msg):
+        if self.verbose:
+            print(msg)
+
+    @property
+    def pipeline(self):
+        if self._pipe is None:
+            self._pipe = FdkPipeline(self, self.device, self.storage)
+        return self._pipe
+
+    def MainFunction(self):  # noqa: N802 - reference name
+        """Reconstruct every matching input file (run_mgfbp.py:52-85)."""
+        if self.kernel_name is None:
+            raise ConfigError("ERROR: no reconstruction kernel (HammingFilter, GaussianApodizedRamp or None) "
+                              "in the config!")
+        pipe = self.pipeline
+        self.file_processed_count = 0
+        for file in os.listdir(self.input_dir):
+            if re.match(self.input_files_pattern, file):
+                if self.ReadSinogram(file):
+                    self.file_processed_count += 1
+                    self._log("Reconstructing %s ..." % self.input_path)
+                    dev = torch.from_numpy(self._raw).to(pipe.device, non_blocking=False)
+                    filtered = pipe.filter(dev, self._row_stride, self._view_stride)
+                    if self.save_filtered_sinogram:
+                        imwriteTiff(filtered.cpu().numpy(), self.output_dir + "/sgm_filtered_" + self.output_file)
+                    vol = pipe.backproject(filtered)
+                    self.img_recon = vol.cpu().numpy()
+                    self._log("Saving to %s !" % self.output_path)
+                    self.SaveReconImg()
+        return self.img_recon
+
+    def output_name(self, file):
+        """Output file name from OutputFileReplace pairs (run_mgfbp.py:1190-1203)."""
+        out = file
+        for i in range(int(len(self.output_file_replace) / 2)):
+            out = re.sub(self.output_file_replace[2 * i], self.output_file_replace[2 * i + 1], out)
+        if out == file:
+            raise ConfigError(f"ERROR: did not file string to replace in '{out}'")
+        if self.output_file_format in ("tif", "tiff"):
+            out = re.sub(".raw", ".tif", out)
+        return out
+
+    def ReadSinogram(self, file):  # noqa: N802 - reference name
+        """Read one input file (run_mgfbp.py:1189-1228); keeps the file layout and
+        lets the device weighting kernel read it with strides."""
+        self.input_path = os.path.join(self.input_dir, file)
+        self.output_file = self.output_name(file)
+        self.output_path = os.path.join(self.output_dir, self.output_file_prefix + self.output_file)
+        self._raw, self._row_stride, self._view_stride = read_sinogram_raw_layout(self, self.input_path)
+        return True
+
+    def read_sinogram_array(self, file):
+        """[rows, views, cols] float32 of one file, as the reference's img_sgm."""
+        return read_sinogram_file(self, os.path.join(self.input_dir, file))
+
+    def SaveReconImg(self):  # noqa: N802 - reference name
+        """HU conversion and file output (run_mgfbp.py:1302-1310)."""
+        if self.convert_to_HU:
+            self.img_recon = (self.img_recon / self.water_mu - 1) * 1000
+        if self.output_file_format == "raw":
+            imwriteRaw(self.img_recon, self.output_path, dtype=np.float32)
+        else:
+            imwriteTiff(self.img_recon, self.output_path, dtype=np.float32)
+
+
+def run_mgfbp(file_path, device=None, storage="f32", verbose=True):
+    """Drop-in for run_mgfbp.run_mgfbp (run_mgfbp.py:18-47): FBP of every file that
+    matches the config, returning the last reconstruction [z, y, x] (HU if WaterMu)."""
+    if verbose:
+        print("Performing FBP from MandoCT-GB300 ...")
+    start = time.time()
+    if not os.path.exists(file_path):
+        raise ConfigError(f"ERROR: Config File {file_path} does not exist!")
+    fbp = Mgfbp(ReadConfigFile(file_path), device=device, storage=storage, verbose=verbose)
+    img = fbp.MainFunction()
+    if verbose:
+        if fbp.file_processed_count > 0:
+            print(f"\nA total of {fbp.file_processed_count:d} file(s) are reconstructed!")
+            print(f"Time cost is {time.time() - start:.3} sec\n")
+        else:
+            print(f"\nWarning: Did not find files like {fbp.input_files_pattern:s} in {fbp.input_dir:s}.")
+            print("No images are reconstructed!\n")
+    del fbp
+    gc.collect()
+    return img

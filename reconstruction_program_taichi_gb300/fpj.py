@@ -1,0 +1,133 @@
+"""Forward-projection drop-in: run_mgfpj_v3(config_path) and class Mgfpj_v3,
+mirroring run_mgfpj_v3.py:45-127 on the GB300 kernels.  All views of a volume are
+projected in one launch; binning and noise follow in one more.
+"""
+import gc
+import os
+import re
+import time
+
+import numpy as np
+import torch
+
+from . import ops
+from .config import ConfigError, ReadConfigFile, parse_fbp, parse_fpj, parse_fpj_v3
+from .geometry import fpj_geometry
+from .io import imwriteRaw
+
+
+class FpPipeline:
+    """Forward projection + binning/noise for one Mgfpj_v3 geometry."""
+
+    def __init__(self, obj, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("a CUDA device is required (this package has no CPU fallback)")
+        self.obj = obj
+        self.dg = fpj_geometry(obj, device)
+        g = self.dg.geom
+        self.full_rows = obj.det_elem_count_vertical
+        self.begin = obj.det_elem_vertical_recon_range_begin
+        self.os = obj.oversample_size
+        # geometry of the binning step: all detector rows, binned columns
+        self.bin_dg = ops.DeviceGeometry(g.copy(nv=self.full_rows, nu=obj.det_elem_count_horizontal),
+                                         self.dg.host["angles"], device=self.dg.device)
+        self.rows_buf = torch.zeros((g.nv, g.views, g.nu), dtype=torch.float32, device=self.dg.device)
+        self.full_buf = None
+        if g.nv != self.full_rows:
+            self.full_buf = torch.zeros((self.full_rows, g.views, g.nu), dtype=torch.float32, device=self.dg.device)
+
+    def project(self, vol, seed=0):
+        """[rows, views, cols] sinogram of a device volume, binned (and noisy if
+        PhotonNumber is set), before the output-form flip."""
+        obj = self.obj
+        rows = ops.fp(self.dg, vol, out=self.rows_buf)
+        if self.full_buf is not None:
+            self.full_buf[self.begin:self.begin + rows.shape[0]] = rows
+            rows = self.full_buf
+        photons = float(obj.photon_number) if obj.add_possion_noise else 0.0
+        if self.os == 1 and photons == 0.0:
+            return rows
+        return ops.bin_noise(self.bin_dg, rows, self.os, photons, seed)
+
+
+class Mgfpj_v3:  # noqa: N801 - reference name
+    """Drop-in for the reference class Mgfpj_v3 (run_mgfpj_v3.py:80-391)."""
+
+    def __init__(self, config_dict, device=None, verbose=True, noise_seed=0):
+        self.verbose = verbose
+        parse_fbp(self, config_dict)
+        parse_fpj(self, config_dict)
+        parse_fpj_v3(self, config_dict)
+        self.img_sgm = np.zeros((self.det_elem_count_vertical, self.view_num, self.det_elem_count_horizontal),
+                                dtype=np.float32)
+        self.device = device
+        self.noise_seed = noise_seed
+        self.file_processed_count = 0
+        self._pipe = None
+
+    @property
+    def pipeline(self):
+        if self._pipe is None:
+            self._pipe = FpPipeline(self, self.device)
+        return self._pipe
+
+    def ReadImage(self, file):  # noqa: N802 - reference name
+        """Read one volume (run_mgfpj_v2.py:423-441)."""
+        self.input_path = os.path.join(self.input_dir, file)
+        self.output_file = re.sub(self.output_file_replace[0], self.output_file_replace[1], file)
+        if self.output_file == file:
+            raise ConfigError(f"ERROR: did not find string '{self.output_file_replace[0]}' to replace in "
+                              f"'{self.output_file}'")
+        self.output_path = os.path.join(self.output_dir, self.output_file_prefix + self.output_file)
+        img = np.fromfile(self.input_path, dtype=np.float32).reshape(self.img_dim_z, self.img_dim, self.img_dim)
+        if self.convert_to_HU:
+            img = ((img + 1000.0) / 1000.0 * self.water_mu).astype(np.float32)
+        self.img_image = img
+        return True
+
+    def MainFunction(self):  # noqa: N802 - reference name
+        """Forward project every matching volume (run_mgfpj_v3.py:82-127)."""
+        pipe = self.pipeline
+        self.file_processed_count = 0
+        for file in os.listdir(self.input_dir):
+            if re.match(self.input_files_pattern, file):
+                if self.ReadImage(file):
+                    if self.verbose:
+                        print("\nForward projecting %s ..." % self.input_path)
+                    self.file_processed_count += 1
+                    vol = torch.from_numpy(self.img_image).to(pipe.dg.device)
+                    sgm = pipe.project(vol, seed=self.noise_seed + self.file_processed_count)
+                    self.img_sgm = sgm.cpu().numpy()
+                    if self.verbose:
+                        print("\nSaving to %s !" % self.output_path)
+                    self.SaveSinogram()
+        return self.img_sgm
+
+    def SaveSinogram(self):  # noqa: N802 - reference name
+        """Output-form conventions of run_mgfpj_v2.py:458-470."""
+        if self.cone_beam:
+            if self.output_file_form == "sinogram":
+                self.img_sgm = np.ascontiguousarray(np.flip(self.img_sgm, axis=0))
+                imwriteRaw(self.img_sgm, self.output_path, dtype=np.float32)
+            else:
+                imwriteRaw(self.img_sgm.transpose(1, 0, 2), self.output_path, dtype=np.float32)
+        else:
+            imwriteRaw(self.img_sgm, self.output_path, dtype=np.float32)
+
+
+def run_mgfpj_v3(file_path, device=None, verbose=True, noise_seed=0):
+    """Drop-in for run_mgfpj_v3.run_mgfpj_v3 (run_mgfpj_v3.py:45-77): returns the
+    last sinogram [rows, views, cols] in the output-form convention."""
+    start = time.time()
+    if not os.path.exists(file_path):
+        raise ConfigError(f"ERROR: Config File {file_path} does not exist!")
+    fpj = Mgfpj_v3(ReadConfigFile(file_path), device=device, verbose=verbose, noise_seed=noise_seed)
+    sgm = fpj.MainFunction()
+    if verbose:
+        if fpj.file_processed_count > 0:
+            print(f"\nA total of {fpj.file_processed_count:d} files are forward projected!")
+            print(f"Time cost is {time.time() - start:.3} sec\n")
+        else:
+            print(f"\nWarning: Did not find files like {fpj.input_files_pattern:s} in {fpj.input_dir:s}.")
+    gc.collect()
+    return sgm

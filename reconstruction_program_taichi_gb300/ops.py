@@ -1,0 +1,269 @@
+"""Device operators over torch CUDA tensors, each a thin call into the C ABI
+(include/mandoct_gb300.h) on the current CUDA stream.
+
+Tensors are float32 and C-contiguous.  Sinograms are [rows, views, cols] and volumes
+[z, y, x], the reference's layouts; the filtered sinogram handed from the filter to
+the backprojector is view-major [views, rows, cols] and is then packed into the
+backprojector's gather layout.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import MCT_BF16, MCT_F32, Geom, Tables
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _check(t, name, shape=None, dtype=torch.float32):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+
+
+class DeviceGeometry:
+    """An mct_geom plus its device tables (angles, u, v, per-view z centre, matrices)."""
+
+    def __init__(self, geom, angles, u=None, v=None, cz=None, pmatrix=None, pmat_a=None, pmat_xs=None,
+                 device=None):
+        self.geom = geom
+        dev = torch.device(device or "cuda")
+        self._keep = {}
+
+        def up(name, arr):
+            if arr is None:
+                return None
+            t = torch.as_tensor(np.ascontiguousarray(np.asarray(arr, dtype=np.float64)).astype(np.float32),
+                                device=dev).contiguous()
+            self._keep[name] = t
+            return t.data_ptr()
+
+        self.tables = Tables(angles=up("angles", angles), u=up("u", u), v=up("v", v), cz=up("cz", cz),
+                             pmatrix=up("pmatrix", pmatrix), pmat_a=up("pmat_a", pmat_a),
+                             pmat_xs=up("pmat_xs", pmat_xs))
+        self.device = dev
+
+    @property
+    def sgm_shape(self):
+        g = self.geom
+        return (g.nv, g.views, g.nu)
+
+    @property
+    def vol_shape(self):
+        g = self.geom
+        return (g.nz, g.nx, g.nx)
+
+    def g(self):
+        return ctypes.byref(self.geom)
+
+    def t(self):
+        return ctypes.byref(self.tables)
+
+
+# ---------------------------------------------------------------- FBP / FDK
+
+def weight(dg, sgm, row_stride, view_stride, bh=None, out=None):
+    """BH polynomial + cosine (+ Parker) weighting into [nv, views, nu]."""
+    _check(sgm, "sgm")
+    if out is None:
+        out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=sgm.device)
+    _check(out, "out", dg.sgm_shape)
+    n_bh = 0
+    if bh is not None:
+        _check(bh, "bh")
+        n_bh = bh.numel()
+    _lib.call("mct_weight", dg.g(), dg.t(), _ptr(sgm), row_stride, view_stride, _ptr(bh), n_bh, _ptr(out), _stream())
+    return out
+
+
+def vgauss(dg, weighted, taps, out=None):
+    _check(weighted, "weighted", dg.sgm_shape)
+    _check(taps, "taps", (2 * dg.geom.nv - 1,))
+    if out is None:
+        out = torch.empty_like(weighted)
+    _lib.call("mct_vgauss", dg.g(), _ptr(weighted), _ptr(taps), _ptr(out), _stream())
+    return out
+
+
+def filter_rows(dg, weighted, taps, out=None):
+    """Toeplitz row filter; returns the view-major filtered sinogram [views, nv, nu]."""
+    g = dg.geom
+    _check(weighted, "weighted", dg.sgm_shape)
+    _check(taps, "taps", (2 * g.nu - 1,))
+    if out is None:
+        out = torch.empty((g.views, g.nv, g.nu), dtype=torch.float32, device=weighted.device)
+    _check(out, "out", (g.views, g.nv, g.nu))
+    _lib.call("mct_filter", dg.g(), _ptr(weighted), _ptr(taps), _ptr(out), _stream())
+    return out
+
+
+def packed_bytes(dg, dtype=MCT_F32):
+    return int(_lib.load().mct_packed_size(dg.g(), dtype))
+
+
+def pack(dg, filtered, dtype=MCT_F32, out=None):
+    g = dg.geom
+    _check(filtered, "filtered", (g.views, g.nv, g.nu))
+    nbytes = packed_bytes(dg, dtype)
+    if out is None:
+        out = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=filtered.device)
+    if out.numel() < nbytes:
+        raise ValueError("packed buffer too small")
+    _lib.call("mct_pack", dg.g(), _ptr(filtered), _ptr(out), dtype, _stream())
+    return out
+
+
+def fdk_bp(dg, packed, dtype=MCT_F32, out=None):
+    if out is None:
+        out = torch.empty(dg.vol_shape, dtype=torch.float32, device=packed.device)
+    _check(out, "out", dg.vol_shape)
+    _lib.call("mct_fdk_bp", dg.g(), dg.t(), _ptr(packed), dtype, _ptr(out), _stream())
+    return out
+
+
+# ---------------------------------------------------------------- forward projection
+
+def fp(dg, vol, mask=None, out=None):
+    _check(vol, "vol", dg.vol_shape)
+    if mask is not None:
+        _check(mask, "mask", dg.sgm_shape)
+    if out is None:
+        out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=vol.device)
+    _check(out, "out", dg.sgm_shape)
+    _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _stream())
+    return out
+
+
+def fp_adjoint(dg, sgm, mask=None, out=None, accumulate=False):
+    _check(sgm, "sgm", dg.sgm_shape)
+    if mask is not None:
+        _check(mask, "mask", dg.sgm_shape)
+    if out is None:
+        out = torch.zeros(dg.vol_shape, dtype=torch.float32, device=sgm.device)
+    elif not accumulate:
+        out.zero_()
+    _check(out, "out", dg.vol_shape)
+    _lib.call("mct_fp_adjoint", dg.g(), dg.t(), _ptr(sgm), _ptr(mask), _ptr(out), _stream())
+    return out
+
+
+def fp_count_samples(dg, mask=None):
+    """Number of in-volume trilinear samples of fp() (int)."""
+    out = torch.zeros(1, dtype=torch.int64, device=dg.device)
+    _lib.call("mct_fp_count_samples", dg.g(), dg.t(), _ptr(mask), _ptr(out), _stream())
+    return int(out.item())
+
+
+def effective_map(dg, out=None):
+    if out is None:
+        out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=dg.device)
+    _check(out, "out", dg.sgm_shape)
+    _lib.call("mct_effective_map", dg.g(), dg.t(), _ptr(out), _stream())
+    return out
+
+
+def bin_noise(dg, sgm_large, bin_size, photons=0.0, seed=0, out=None):
+    """[nv, views, nu*bin] -> [nv, views, nu] with optional photon noise."""
+    g = dg.geom
+    _check(sgm_large, "sgm_large", (g.nv, g.views, g.nu * bin_size))
+    if out is None:
+        out = torch.empty((g.nv, g.views, g.nu), dtype=torch.float32, device=sgm_large.device)
+    _check(out, "out", (g.nv, g.views, g.nu))
+    _lib.call("mct_bin_noise", dg.g(), _ptr(sgm_large), bin_size, float(photons), int(seed) & (2 ** 64 - 1),
+              _ptr(out), _stream())
+    return out
+
+
+def project_ellipsoids(dg, ell, out=None):
+    """Analytic line integrals of ellipsoids ([n, 10] rows) along the projector's rays."""
+    ell = torch.as_tensor(np.asarray(ell, dtype=np.float32), device=dg.device).contiguous()
+    if out is None:
+        out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=dg.device)
+    _check(out, "out", dg.sgm_shape)
+    _lib.call("mct_project_ellipsoids", dg.g(), dg.t(), _ptr(ell), int(ell.shape[0]), _ptr(out), _stream())
+    return out
+
+
+# ---------------------------------------------------------------- iterative reconstruction
+
+def bp_unmatched(dg, sgm, out=None):
+    _check(sgm, "sgm", dg.sgm_shape)
+    if out is None:
+        out = torch.empty(dg.vol_shape, dtype=torch.float32, device=sgm.device)
+    _check(out, "out", dg.vol_shape)
+    _lib.call("mct_bp_ref_unmatched", dg.g(), dg.t(), _ptr(sgm), _ptr(out), _stream())
+    return out
+
+
+def tv_weights(dg, x, beta, out=None):
+    _check(x, "x", dg.vol_shape)
+    if out is None:
+        out = torch.empty_like(x)
+    _lib.call("mct_tv_weights", dg.g(), _ptr(x), float(beta), _ptr(out), _stream())
+    return out
+
+
+def dtwd(dg, x, wr, s=1.0, out_in=None, a=0.0, out=None):
+    """out = a*out_in + s * D^T W D x."""
+    _check(x, "x", dg.vol_shape)
+    _check(wr, "wr", dg.vol_shape)
+    if out is None:
+        out = torch.empty_like(x)
+    _lib.call("mct_dtwd", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(out_in), float(a), _ptr(out), _stream())
+    return out
+
+
+_scratch = {}
+
+
+def reduce_scratch(device):
+    key = (str(device), torch.cuda.current_stream(device).cuda_stream)
+    t = _scratch.get(key)
+    if t is None:
+        n = int(_lib.load().mct_reduce_scratch_size()) // 8
+        t = torch.empty(n, dtype=torch.float64, device=device)
+        _scratch[key] = t
+    return t
+
+
+def tv_penalty(dg, x, beta, out=None):
+    """sum sqrt(|D x|^2 + beta) as a float64 device scalar."""
+    _check(x, "x", dg.vol_shape)
+    if out is None:
+        out = torch.empty((), dtype=torch.float64, device=x.device)
+    _lib.call("mct_tv_penalty", dg.g(), _ptr(x), float(beta), _ptr(reduce_scratch(x.device)), _ptr(out), _stream())
+    return out
+
+
+def dot(a, b, out=None):
+    """float64 inner product of two float32 tensors, as a device scalar."""
+    _check(a, "a")
+    _check(b, "b", tuple(a.shape))
+    if out is None:
+        out = torch.empty((), dtype=torch.float64, device=a.device)
+    _lib.call("mct_dot_f64", _ptr(a), _ptr(b), a.numel(), _ptr(reduce_scratch(a.device)), _ptr(out), _stream())
+    return out
+
+
+def cgls_update(rr, dq, x, r, d, q, rr_new):
+    """alpha = rr/dq; x += alpha d; r -= alpha q; rr_new = |r|^2 (device scalars)."""
+    _lib.call("mct_cgls_update", x.numel(), _ptr(rr), _ptr(dq), _ptr(x), _ptr(r), _ptr(d), _ptr(q),
+              _ptr(reduce_scratch(x.device)), _ptr(rr_new), _stream())
+
+
+def cgls_direction(rr, rr_new, r, d):
+    """d = r + (rr_new/rr) d."""
+    _lib.call("mct_cgls_direction", d.numel(), _ptr(rr), _ptr(rr_new), _ptr(r), _ptr(d), _stream())

@@ -1,0 +1,235 @@
+"""GPU parity: the drop-in entry points against the reference's own outputs
+(golden fixtures), and each CUDA operator against the float64 oracle.
+
+Tolerance: the plain float32 GPU path must match within 1e-4 relative L2."""
+import copy
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, rel_l2
+from oracle import PI
+from oracle import fbp_ops as F
+from oracle import fpj_ops as P
+from oracle import ir_ops as I
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+def _write_case(z, tmp_path, kind):
+    cfg = copy.deepcopy(z["config"])
+    d = tmp_path / "in"
+    d.mkdir()
+    cfg["InputDir"] = str(d)
+    cfg["OutputDir"] = str(tmp_path / "out")
+    if kind == "fpj":
+        z["input_vol"].astype(np.float32).tofile(d / "img_a.raw")
+    else:
+        s = z["input_sgm"].astype(np.float32)
+        if cfg.get("InputFileForm") == "post_log_images":
+            s = s.transpose(1, 0, 2)
+        s.tofile(d / "sgm_a.raw")
+    if "prior" in z:
+        z["prior"].astype(np.float32).tofile(tmp_path / "prior.raw")
+        cfg["PriorImageFile"] = str(tmp_path / "prior.raw")
+    p = tmp_path / "config.jsonc"
+    p.write_text(json.dumps(cfg))
+    return str(p)
+
+
+@pytest.mark.parametrize("name", golden_names("fbp") + golden_names("fdk"))
+def test_run_mgfbp_matches_reference(name, tmp_path, cuda):
+    from reconstruction_program_taichi_gb300 import run_mgfbp
+    z = load_golden(name)
+    img = run_mgfbp(_write_case(z, tmp_path, "fbp"), verbose=False)
+    assert img.shape == z["recon"].shape
+    mismatched_zero = int(np.sum((img == 0) != (z["recon"] == 0)))
+    assert mismatched_zero == 0
+    assert rel_l2(img, z["recon"]) < TOL
+    out = [f for f in os.listdir(tmp_path / "out")]
+    assert len(out) == 1
+
+
+@pytest.mark.parametrize("name", golden_names("fpj"))
+def test_run_mgfpj_v3_matches_reference(name, tmp_path, cuda):
+    from reconstruction_program_taichi_gb300 import run_mgfpj_v3
+    z = load_golden(name)
+    sgm = run_mgfpj_v3(_write_case(z, tmp_path, "fpj"), verbose=False)
+    assert sgm.shape == z["sgm"].shape
+    assert rel_l2(sgm, z["sgm"]) < TOL
+
+
+@pytest.mark.parametrize("name", golden_names("ir"))
+def test_run_mgfbp_ir_matches_reference(name, tmp_path, cuda):
+    from reconstruction_program_taichi_gb300 import run_mgfbp_ir, run_mgfbp_ir_piccs
+    z = load_golden(name)
+    path = _write_case(z, tmp_path, "ir")
+    img = run_mgfbp_ir_piccs(path, verbose=False) if "prior" in z else run_mgfbp_ir(path, verbose=False)
+    assert rel_l2(img, z["recon"]) < TOL
+
+
+# ---------------------------------------------------------------- operator level, larger sizes
+
+def _cone_obj(n=48, nz=20, nu=96, nv=40, views=90, **kw):
+    from reconstruction_program_taichi_gb300 import config
+
+    class O:
+        verbose = False
+
+    cfg = {"InputDir": "/tmp", "OutputDir": "/tmp/mct_out", "InputFiles": "x", "OutputFilePrefix": "",
+           "OutputFileReplace": ["a", "b"], "DetectorElementCountHorizontal": nu, "DetectorElementWidth": 0.8,
+           "DetectorOffsetHorizontal": 0.37, "DetectorElementCountVertical": nv, "DetectorElementHeight": 0.8,
+           "DetectorOffsetVertical": -0.21, "Views": views, "TotalScanAngle": 360, "SourceIsocenterDistance": 300,
+           "SourceDetectorDistance": 550, "ImageDimension": n, "PixelSize": 0.5, "ImageDimensionZ": nz,
+           "VoxelHeight": 0.5, "ConeBeam": True, "HammingFilter": 1, "ImageRotation": 7,
+           "ForwardProjectionStepSize": 0.3, "ImageCenter": [0.3, -0.2]}
+    cfg.update(kw)
+    o = O()
+    config.parse_fbp(o, cfg)
+    config.parse_fpj(o, cfg)
+    config.parse_fpj_v3(o, cfg)
+    return o
+
+
+def _smooth(rng, nz, n):
+    z, y, x = np.meshgrid(np.linspace(-1, 1, nz), np.linspace(-1, 1, n), np.linspace(-1, 1, n), indexing="ij")
+    v = np.zeros((nz, n, n))
+    for _ in range(5):
+        c = rng.uniform(-0.4, 0.4, 3)
+        v += rng.uniform(0.5, 1.5) * np.exp(-((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) / 0.15)
+    return (0.02 * v).astype(np.float32)
+
+
+@pytest.mark.parametrize("kw", [{}, {"ReconViewMode": "coronal"}, {"CurvedDetector": True, "TotalScanAngle": 220},
+                                {"ImageDimension": 37, "ImageDimensionZ": 13, "DetectorElementCountHorizontal": 75}])
+def test_fdk_ops_vs_oracle(kw, cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import fbp, geometry
+    o = _cone_obj(**kw)
+    pipe = fbp.FdkPipeline(o, storage="f32")
+    rng = np.random.default_rng(5)
+    sgm = rng.uniform(0, 1, (o.det_elem_count_vertical_actual, o.view_num, o.det_elem_count_horizontal)).astype(np.float32)
+    vol = pipe.run(torch.from_numpy(sgm).cuda()).cpu().numpy()
+    u, v, ang = geometry.fbp_arrays(o)
+    w = F.weight_sgm(sgm, u, v, ang, o.source_det_dis, o.curved_dect, o.short_scan, o.total_scan_angle)
+    filt = F.filter_rows(w, geometry.recon_taps(o), o.det_elem_width)
+    ref = F.fdk_bp(filt, ang, u, v, nx=o.img_dim, nz=o.img_dim_z, px=o.img_pix_size, pz=o.img_voxel_height,
+                   cx=o.img_center_x, cy=o.img_center_y, cz=o.img_center_z, sid=o.source_isocenter_dis,
+                   sdd=o.source_det_dis, dv=o.det_elem_height, img_rot=o.img_rot,
+                   total_scan_angle=o.total_scan_angle, short_scan=o.short_scan, cone_beam=True,
+                   curved=o.curved_dect, view_mode=o.recon_view_mode)
+    zero_mismatch = np.sum((vol == 0) != (ref == 0))
+    assert zero_mismatch <= max(2, vol.size // 20000)
+    keep = (vol != 0) & (ref != 0)
+    assert rel_l2(vol[keep], ref[keep]) < TOL
+
+
+def test_fdk_bf16_storage_error_is_small(cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import fbp
+    o = _cone_obj()
+    rng = np.random.default_rng(6)
+    sgm = torch.from_numpy(rng.uniform(0, 1, (o.det_elem_count_vertical, o.view_num,
+                                              o.det_elem_count_horizontal)).astype(np.float32)).cuda()
+    a = fbp.FdkPipeline(o, storage="f32").run(sgm).cpu().numpy()
+    b = fbp.FdkPipeline(o, storage="bf16").run(sgm).cpu().numpy()
+    assert rel_l2(b, a) < 5e-3
+
+
+@pytest.mark.parametrize("kw", [{}, {"CurvedDetector": True}, {"HelicalPitch": 0.7, "TotalScanAngle": 720},
+                                {"ImageDimension": 41, "DetectorElementCountHorizontal": 77}])
+def test_fp_vs_oracle(kw, cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    o = _cone_obj(views=24, **kw)
+    dg = geometry.fpj_geometry(o)
+    rng = np.random.default_rng(7)
+    vol = _smooth(rng, o.img_dim_z, o.img_dim)
+    got = ops.fp(dg, torch.from_numpy(vol).cuda()).cpu().numpy()
+    u, v, ang = dg.host["u"], dg.host["v"], dg.host["angles"]
+    ref = np.zeros_like(got, dtype=np.float64)
+    for j in range(o.view_num):
+        ref[:, j, :] = P.march(vol, j, ang, u, v, nx=o.img_dim, nz=o.img_dim_z, px=o.img_pix_size,
+                               pz=o.img_voxel_height, cx=o.img_center_x, cy=o.img_center_y,
+                               cz_view=o.array_img_center_z[j], sid=o.source_isocenter_dis, sdd=o.source_det_dis,
+                               step=o.fpj_step_size, cone_beam=True, curved=o.curved_dect,
+                               zpv=dg.geom.fp_z_per_view, rows=o.det_elem_count_vertical, K=dg.geom.fp_steps)
+    assert rel_l2(got, ref) < TOL
+
+
+def test_fp_adjoint_dot_product(cuda):
+    """<A x, y> = <x, A^T y> to 1e-5 relative (float64 accumulation of the sums)."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    o = _cone_obj(n=32, nz=16, nu=64, nv=24, views=30)
+    dg = geometry.fpj_geometry(o)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.rand(dg.vol_shape, device="cuda", generator=g)
+    y = torch.rand(dg.sgm_shape, device="cuda", generator=g)
+    mask = (torch.rand(dg.sgm_shape, device="cuda", generator=g) > 0.2).float()
+    ax = ops.fp(dg, x, mask=mask)
+    aty = ops.fp_adjoint(dg, y, mask=mask)
+    lhs = float((ax.double() * y.double()).sum())
+    rhs = float((x.double() * aty.double()).sum())
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+def test_ir_operators_vs_oracle(cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import config, geometry, ops
+    o = _cone_obj(n=40, nz=12, nu=64, nv=20, views=36, DetectorElementHeight=1.2)
+    config.parse_ir(o, {"Lambda": 1e-3})
+    dg = geometry.ir_geometry(o)
+    u, v, ang = dg.host["u"], dg.host["v"], dg.host["angles"]
+    g = dict(rows=o.det_elem_count_vertical, views=o.view_num, nu=o.det_elem_count_horizontal, nx=o.img_dim,
+             nz=o.img_dim_z, px=o.img_pix_size, pz=o.img_voxel_height, cx=o.img_center_x, cy=o.img_center_y,
+             cz=o.array_img_center_z, sid=o.source_isocenter_dis, sdd=o.source_det_dis, step=o.fpj_step_size,
+             cone=True, curved=False, zpv=0.0, K=dg.geom.fp_steps, angles=ang, u=u, v=v, dv=o.det_elem_height,
+             img_rot=o.img_rot)
+    ref_ops = I.IrOperators(g)
+    em = ops.effective_map(dg).cpu().numpy()
+    em_ref = ref_ops.emap()
+    assert np.mean(em != em_ref) < 1e-3 and 0 < em.mean() < 1
+    rng = np.random.default_rng(9)
+    sgm = rng.uniform(0, 1, dg.sgm_shape).astype(np.float32) * em_ref.astype(np.float32)
+    bp = ops.bp_unmatched(dg, torch.from_numpy(sgm).cuda()).cpu().numpy()
+    bp_ref = ref_ops.bp(sgm)
+    keep = (bp != 0) & (bp_ref != 0)
+    assert np.mean((bp == 0) != (bp_ref == 0)) < 1e-3
+    assert rel_l2(bp[keep], bp_ref[keep]) < TOL
+    x = _smooth(rng, o.img_dim_z, o.img_dim)
+    xd = torch.from_numpy(x).cuda()
+    wr = ops.tv_weights(dg, xd, 1e-6)
+    wr_ref = I.generate_wr(x, 1e-6)
+    assert rel_l2(wr.cpu().numpy(), wr_ref) < 1e-5
+    out = ops.dtwd(dg, xd, torch.from_numpy(wr_ref.astype(np.float32)).cuda())
+    assert rel_l2(out.cpu().numpy(), I.dtwd(x, wr_ref)) < 1e-5
+    tv = float(ops.tv_penalty(dg, xd, 1e-6))
+    assert math.isclose(tv, I.tv_penalty(x, 1e-6), rel_tol=1e-6)
+
+
+def test_cgls_fused_update_matches_numpy(cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import ops
+    rng = np.random.default_rng(11)
+    n = 100_003
+    x, r, d, q = (rng.standard_normal(n).astype(np.float32) for _ in range(4))
+    t = [torch.from_numpy(a.copy()).cuda() for a in (x, r, d, q)]
+    rr = ops.dot(t[1], t[1])
+    dq = ops.dot(t[2], t[3])
+    assert math.isclose(float(rr), float(np.dot(r.astype(np.float64), r)), rel_tol=1e-12)
+    rr_new = torch.empty((), dtype=torch.float64, device="cuda")
+    ops.cgls_update(rr, dq, t[0], t[1], t[2], t[3], rr_new)
+    ops.cgls_direction(rr, rr_new, t[1], t[2])
+    alpha = np.float32(np.dot(r.astype(np.float64), r) / np.dot(d.astype(np.float64), q))
+    x2 = x + alpha * d
+    r2 = r - alpha * q
+    beta = np.float32(np.dot(r2.astype(np.float64), r2) / np.dot(r.astype(np.float64), r))
+    d2 = r2 + beta * d
+    np.testing.assert_allclose(t[0].cpu().numpy(), x2, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(t[1].cpu().numpy(), r2, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(t[2].cpu().numpy(), d2, rtol=1e-5, atol=1e-5)
