@@ -27,6 +27,9 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(nu=1024, nv=256, views=1080, nx=512, nz=256, du=0.8, dv=0.8, px=0.4, pz=0.4, sid=600.0,
                 sdd=1100.0, step=0.2, n_ell=20, photons=1e5, seed=2024)
 SMALL = dict(WORKLOAD, nu=256, nv=64, views=270, nx=128, nz=64, du=3.2, dv=3.2, px=1.6, pz=1.6)
+# profiling case for ncu: the full detector and a volume larger than L2 (168 MB), 36 views
+PROF = dict(WORKLOAD, views=36, nz=160)
+WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF}
 
 
 def make_config(w):
@@ -406,12 +409,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16"])
-    ap.add_argument("--small", action="store_true", help="4x smaller workload (profiling / quick checks)")
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
+                    help="c2: the benchmark; small: quick checks; prof: short launches for ncu captures")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     args = ap.parse_args()
-    w = SMALL if args.small else WORKLOAD
+    w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w)
     else:

@@ -129,13 +129,19 @@ int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* packed, int32
 
 /* ---------------------------------------------------------------- forward projection */
 
+/* Bytes of the optional forward-projection workspace (an x/y-transposed copy of
+ * the volume). */
+size_t mct_fp_workspace_size(const mct_geom* g);
+
 /* Ray-driven trilinear forward projection of vol [nz][nx][nx] for all views into
  * sgm [nv][views][nu] (overwritten).  Rays with mask != 1 (mask [nv][views][nu], or
- * NULL for none) give 0.  Replaces Mgfpj_v3.ForwardProjectionBilinear
- * run_mgfpj_v3.py:184-366 and Mgfbp_ir.ForwardProjectionBilinear
- * run_mgfbp_iterative_recon_IRN_CGLS.py:494-676. */
+ * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes, or NULL) receives
+ * a transposed copy of vol that views whose detector columns run along y read
+ * instead, for coalesced gathers; results are identical either way.  Replaces
+ * Mgfpj_v3.ForwardProjectionBilinear run_mgfpj_v3.py:184-366 and
+ * Mgfbp_ir.ForwardProjectionBilinear run_mgfbp_iterative_recon_IRN_CGLS.py:494-676. */
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
-           void* stream);
+           void* workspace, void* stream);
 
 /* Exact transpose of mct_fp: vol += P^T sgm (vol is accumulated, not cleared).
  * No counterpart in the reference (its CGLS pairs mct_fp with the unmatched

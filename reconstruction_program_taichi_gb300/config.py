@@ -480,3 +480,118 @@ def parse_piccs(self, cfg):
     if "PriorImageFile" not in cfg:
         _err("Can not find PriorImageFile in the config file!")
     self.prior_image_file = cfg["PriorImageFile"]
+
+
+def parse_fpj_v1(self, cfg):
+    """Stand-alone parameter handling of the original projector Mgfpj
+    (run_mgfpj.py:98-450): its own aliases (DetectorElementCount,
+    DetectorZElementCount, DetectorZOffcenter, SliceCount for the image depth) and
+    StartAngle / ImageRotation in degrees."""
+    self.config_dict = cfg
+    for key, attr in (("InputDir", "input_dir"), ("OutputDir", "output_dir"), ("InputFiles", "input_files_pattern")):
+        if key not in cfg:
+            _err(f"Can not find {key}!")
+        if not isinstance(cfg[key], str):
+            _err(f"{key} must be a string!")
+        setattr(self, attr, cfg[key])
+    self.output_file_prefix = cfg.get("OutputFilePrefix", "")
+    if not isinstance(self.output_file_prefix, str):
+        _err("OutputFilePrefix must be a string!")
+    if "OutputFileReplace" not in cfg:
+        _err("Can not find OutputFileReplace in the config file!")
+    self.output_file_replace = cfg["OutputFileReplace"]
+    os.makedirs(self.output_dir, exist_ok=True)
+    self.output_file_form = cfg.get("OutputFileForm", "sinogram")
+    if self.output_file_form not in ("sinogram", "post_log_images"):
+        _err("OutputFileForm can only be sinogram or post_log_images!")
+    if "ImageDimension" not in cfg:
+        _err("can not find ImageDimension!")
+    self.img_dim = cfg["ImageDimension"]
+    if not isinstance(self.img_dim, int) or self.img_dim < 0:
+        _err("ImageDimension must be a positive integer!")
+    if "PixelSize" not in cfg:
+        _err("can not find PixelSize!")
+    self.img_pix_size = cfg["PixelSize"]
+    if "SliceCount" in cfg:
+        self.img_dim_z = cfg["SliceCount"]
+    elif "ImageDimensionZ" in cfg:
+        self.img_dim_z = cfg["ImageDimensionZ"]
+    else:
+        _err("Can not find image dimension along Z direction (ImageDimensionZ or SliceCount)!")
+    if not isinstance(self.img_dim_z, int) or self.img_dim_z <= 0:
+        _err("ImageDimensionZ (ImageSliceCount) must be a positive integer!")
+    self.img_center_x, self.img_center_y = cfg.get("ImageCenter", [0.0, 0.0])
+    self.img_center_z = cfg.get("ImageCenterZ", 0.0)
+    self.cone_beam = cfg.get("ConeBeam", False)
+    if not isinstance(self.cone_beam, bool):
+        _err("ConeBeam must be true or false!")
+    self.curved_dect = cfg.get("CurvedDetector", False)
+    if not isinstance(self.curved_dect, bool):
+        _err("CurvedDetector can only be true or false!")
+    for k in ("DetectorElementCountHorizontal", "SinogramWidth", "DetectorElementCount"):
+        if k in cfg:
+            self.det_elem_count_horizontal = cfg[k]
+            break
+    else:
+        _err("Can not find DetectorElementCountHorizontal (SinogramWidth or DetectorElementCount)!")
+    if self.det_elem_count_horizontal <= 0 or self.det_elem_count_horizontal % 1 != 0:
+        _err("DetectorElementCountHorizontal (SinogramWidth) should be a positive integer!")
+    self.det_elem_count_horizontal = int(self.det_elem_count_horizontal)
+    if "DetectorElementWidth" in cfg:
+        self.det_elem_width = cfg["DetectorElementWidth"]
+    elif "DetectorElementSize" in cfg:
+        self.det_elem_width = cfg["DetectorElementSize"]
+    else:
+        _err("Can not find DetectorElementWidth (DetectorElementSize)!")
+    self.det_offset_horizontal = cfg.get("DetectorOffcenter", cfg.get("DetectorOffsetHorizontal", 0.0))
+    for key, attr in (("SourceIsocenterDistance", "source_isocenter_dis"),
+                      ("SourceDetectorDistance", "source_det_dis")):
+        setattr(self, attr, cfg.get(key, self.det_elem_count_horizontal * self.det_elem_width * 1000.0))
+    if "StartAngle" in cfg:
+        self.start_angle = cfg["StartAngle"] / 180.0 * PI
+    elif "ImageRotation" in cfg:
+        self.start_angle = cfg["ImageRotation"] / 180.0 * PI
+    else:
+        self.start_angle = 0.0
+    self.scan_angle = cfg["TotalScanAngle"] / 180.0 * PI if "TotalScanAngle" in cfg else 2 * PI
+    if "Views" not in cfg:
+        _err("Can not find number of views!")
+    self.view_num = int(cfg["Views"])
+    self.oversample_size = int(cfg.get("OversampleSize", 1))
+    self.fpj_step_size = cfg.get("ForwardProjectionStepSize", 0.2)
+    if self.cone_beam:
+        self.img_voxel_height = cfg.get("VoxelHeight", cfg.get("ImageSliceThickness"))
+        if self.img_voxel_height is None:
+            _err("Can not find image voxel height for cone beam recon!")
+        nv = cfg.get("DetectorElementCountVertical", cfg.get("DetectorZElementCount"))
+        if nv is None:
+            _err("Can not find detector element count along vertical direction!")
+        self.det_elem_count_vertical = int(nv)
+        self.det_elem_height = cfg.get("SliceThickness", cfg.get("DetectorElementHeight"))
+        if self.det_elem_height is None:
+            _err("Can not find detector element height for cone beam recon! ")
+        self.det_offset_vertical = cfg.get("DetectorZOffcenter", cfg.get("DetectorOffsetVertical", 0.0))
+    else:
+        self.det_elem_count_vertical = self.img_dim_z
+        self.img_voxel_height = 0.0
+        self.det_elem_height = 0.0
+        self.det_offset_vertical = 0.0
+    if "WaterMu" in cfg:
+        self.water_mu = cfg["WaterMu"]
+        self.convert_to_HU = True
+    else:
+        self.convert_to_HU = False
+    self.helical_scan = "HelicalPitch" in cfg
+    self.helical_pitch = cfg.get("HelicalPitch", 0)
+    if self.helical_scan and "ImageCenterZ" not in cfg:
+        self.img_center_z = self.img_voxel_height * (self.img_dim_z - 1) / 2.0 * np.sign(self.helical_pitch)
+    self.add_possion_noise = "PhotonNumber" in cfg
+    self.photon_number = cfg.get("PhotonNumber", 0)
+    # fields shared with the Mgfbp-derived projectors
+    self.det_elem_count_vertical_actual = self.det_elem_count_vertical
+    self.det_elem_vertical_recon_range_begin = 0
+    self.img_rot = self.start_angle
+    self.total_scan_angle = self.scan_angle
+    self.recon_view_mode = 1
+    self.short_scan = 0
+    self.bool_apply_pmatrix = False

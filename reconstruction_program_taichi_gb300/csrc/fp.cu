@@ -107,11 +107,30 @@ __device__ __forceinline__ bool setup_ray(const FpParams& p, int iu, int iv, int
     return r.ks <= r.ke;
 }
 
+// Direction (in object x, y) along which neighbouring detector columns spread.
+__device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const float* __restrict__ angles,
+                                               const float* __restrict__ pa) {
+    if (p.pmat) {
+        float s0, c0;
+        sincosf(angles[0], &s0, &c0);
+        const float* A = pa + 9 * j;
+        const float ex = A[0] * c0 - A[3] * s0, ey = A[3] * c0 + A[0] * s0;
+        return fabsf(ey) > fabsf(ex);
+    }
+    float sb, cb;
+    sincosf(angles[j], &sb, &cb);
+    return fabsf(cb) > fabsf(sb);  // d(x, y)/du is (-sin b, cos b)
+}
+
+// One thread per ray (u, v) of view j = blockIdx.z.  vol is [z][y][x]; vol_t, when
+// given, is the same volume as [z][x][y]: views whose detector columns spread along
+// y read vol_t so that the 32 rays of a warp touch consecutive addresses.
+template <bool CONE>
 __global__ void __launch_bounds__(256)
 fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
           const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
-          const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ mask,
-          float* __restrict__ sgm) {
+          const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
+          const float* __restrict__ mask, float* __restrict__ sgm) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.y * blockDim.y + threadIdx.y;
     const int j = blockIdx.z;
@@ -121,46 +140,70 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         sgm[oidx] = 0.0f;
         return;
     }
+    const int nx = p.nx;
+    const bool tr = vol_t != nullptr && spread_along_y(p, j, angles, pa);
+    const float* __restrict__ V = tr ? vol_t : vol;
+    const int sx = tr ? nx : 1, sy = tr ? 1 : nx;
+    const int64_t plane = (int64_t)nx * nx;
     Ray r;
     float acc = 0.0f;
     if (setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) {
-        const int nx = p.nx;
-        const int64_t plane = (int64_t)nx * nx;
+        const float xmax = (float)(nx - 1), zmax = (float)(p.nz - 1);
+#pragma unroll 4
         for (int k = r.ks; k <= r.ke; ++k) {
             const float fk = (float)k;
             const float fx = fmaf(fk, r.dfx, r.fx0);
             const float fy = fmaf(fk, r.dfy, r.fy0);
             const float xf = floorf(fx), yf = floorf(fy);
-            if (!(xf >= 0.0f && xf + 1.0f < (float)nx && yf >= 0.0f && yf + 1.0f < (float)nx)) continue;
+            bool ok = xf >= 0.0f && xf < xmax && yf >= 0.0f && yf < xmax;
+            const int xi = min(max((int)xf, 0), nx - 2);
+            const int yi = min(max((int)yf, 0), nx - 2);
             const float xw = fx - xf, yw = fy - yf;
             int zi;
             float zw = 0.0f;
-            if (p.cone) {
+            if (CONE) {
                 const float fz = fmaf(fk, r.dfz, r.fz0);
                 const float zf = floorf(fz);
-                if (!(zf >= 0.0f && zf + 1.0f < (float)p.nz)) continue;
-                zi = (int)zf;
+                ok = ok && zf >= 0.0f && zf < zmax;
+                zi = min(max((int)zf, 0), p.nz - 2);
                 zw = fz - zf;
             } else {
                 zi = iv;
             }
-            const float* b = vol + (int64_t)zi * plane + (int64_t)(int)yf * nx + (int)xf;
-            const float a00 = __ldg(b), a01 = __ldg(b + 1), a10 = __ldg(b + nx), a11 = __ldg(b + nx + 1);
+            const float* b = V + (int64_t)zi * plane + (int64_t)yi * sy + (int64_t)xi * sx;
+            const float a00 = __ldg(b), a01 = __ldg(b + sx), a10 = __ldg(b + sy), a11 = __ldg(b + sx + sy);
             const float l0 = fmaf(xw, a01 - a00, a00);
             const float l1 = fmaf(xw, a11 - a10, a10);
             float val = fmaf(yw, l1 - l0, l0);
-            if (p.cone) {
+            if (CONE) {
                 const float* c = b + plane;
-                const float c00 = __ldg(c), c01 = __ldg(c + 1), c10 = __ldg(c + nx), c11 = __ldg(c + nx + 1);
+                const float c00 = __ldg(c), c01 = __ldg(c + sx), c10 = __ldg(c + sy), c11 = __ldg(c + sx + sy);
                 const float m0 = fmaf(xw, c01 - c00, c00);
                 const float m1 = fmaf(xw, c11 - c10, c10);
                 const float hi = fmaf(yw, m1 - m0, m0);
                 val = fmaf(zw, hi - val, val);
             }
-            acc += val;
+            acc += ok ? val : 0.0f;
         }
     }
     sgm[oidx] = acc * p.stepvd;
+}
+
+// vt[z][x][y] = v[z][y][x], 32x32 tiles through shared memory.
+__global__ void transpose_xy_kernel(int nx, int nz, const float* __restrict__ v, float* __restrict__ vt) {
+    __shared__ float tile[32][33];
+    const int64_t plane = (int64_t)nx * nx;
+    const int z = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int y = y0 + i, x = x0 + threadIdx.x;
+        if (y < nx && x < nx) tile[i][threadIdx.x] = v[z * plane + (int64_t)y * nx + x];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int x = x0 + i, y = y0 + threadIdx.x;
+        if (y < nx && x < nx) vt[z * plane + (int64_t)x * nx + y] = tile[threadIdx.x][i];
+    }
 }
 
 // Exact transpose of fp_kernel: every in-volume sample scatters its trilinear weights
@@ -391,14 +434,30 @@ using namespace mct;
 
 extern "C" {
 
-int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* stream) {
+size_t mct_fp_workspace_size(const mct_geom* g) {
+    if (!g || g->nx < 1 || g->nz < 1) return 0;
+    return (size_t)g->nz * g->nx * g->nx * sizeof(float);
+}
+
+int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* workspace,
+           void* stream) {
     FpParams p;
     MCT_TRY(make_params(g, p, "mct_fp"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp: NULL buffer");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp: projection-matrix tables missing");
+    cudaStream_t s = as_stream(stream);
+    float* vt = static_cast<float*>(workspace);
+    if (vt) {
+        MCT_REQUIRE(vt != vol, "mct_fp: workspace aliases the volume");
+        dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
+        transpose_xy_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, vt);
+        MCT_TRY(launched("transpose_xy_kernel"));
+    }
     dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
-    fp_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
-                                                     mask, sgm);
+    if (p.cone)
+        fp_kernel<true><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol, vt, mask, sgm);
+    else
+        fp_kernel<false><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol, vt, mask, sgm);
     return launched("fp_kernel");
 }
 

@@ -11,19 +11,24 @@ import numpy as np
 import torch
 
 from . import ops
-from .config import ConfigError, ReadConfigFile, parse_fbp, parse_fpj, parse_fpj_v3
-from .geometry import fpj_geometry
+from .config import ConfigError, ReadConfigFile, parse_fbp, parse_fpj, parse_fpj_v1, parse_fpj_v3
+from .geometry import fpj_geometry, fpj_variant_geometry
 from .io import imwriteRaw
 
 
 class FpPipeline:
-    """Forward projection + binning/noise for one Mgfpj_v3 geometry."""
+    """Forward projection + binning/noise for one projector geometry.
 
-    def __init__(self, obj, device=None):
+    version 3 (Mgfpj_v3): noise on every detector row (run_mgfpj_v3.py:117-122);
+    version 2 (Mgfpj of run_mgfpj_v2.py): rows outside the recon range stay 0 and
+    get no noise (:84-106); version 1 (run_mgfpj.py): all rows."""
+
+    def __init__(self, obj, device=None, version=3):
         if not torch.cuda.is_available():
             raise RuntimeError("a CUDA device is required (this package has no CPU fallback)")
         self.obj = obj
-        self.dg = fpj_geometry(obj, device)
+        self.version = version
+        self.dg = fpj_geometry(obj, device) if version == 3 else fpj_variant_geometry(obj, version, device)
         g = self.dg.geom
         self.full_rows = obj.det_elem_count_vertical
         self.begin = obj.det_elem_vertical_recon_range_begin
@@ -41,10 +46,19 @@ class FpPipeline:
         PhotonNumber is set), before the output-form flip."""
         obj = self.obj
         rows = ops.fp(self.dg, vol, out=self.rows_buf)
+        photons = float(obj.photon_number) if obj.add_possion_noise else 0.0
+        if self.version == 2 and self.full_buf is not None:
+            g = self.dg.geom
+            part_dg = ops.DeviceGeometry(g.copy(nu=obj.det_elem_count_horizontal), self.dg.host["angles"],
+                                         device=self.dg.device)
+            binned = ops.bin_noise(part_dg, rows, self.os, photons, seed)
+            out = torch.zeros((self.full_rows, g.views, obj.det_elem_count_horizontal), dtype=torch.float32,
+                              device=self.dg.device)
+            out[self.begin:self.begin + rows.shape[0]] = binned
+            return out
         if self.full_buf is not None:
             self.full_buf[self.begin:self.begin + rows.shape[0]] = rows
             rows = self.full_buf
-        photons = float(obj.photon_number) if obj.add_possion_noise else 0.0
         if self.os == 1 and photons == 0.0:
             return rows
         return ops.bin_noise(self.bin_dg, rows, self.os, photons, seed)
@@ -53,11 +67,16 @@ class FpPipeline:
 class Mgfpj_v3:  # noqa: N801 - reference name
     """Drop-in for the reference class Mgfpj_v3 (run_mgfpj_v3.py:80-391)."""
 
-    def __init__(self, config_dict, device=None, verbose=True, noise_seed=0):
-        self.verbose = verbose
+    VERSION = 3
+
+    def _parse(self, config_dict):
         parse_fbp(self, config_dict)
         parse_fpj(self, config_dict)
         parse_fpj_v3(self, config_dict)
+
+    def __init__(self, config_dict, device=None, verbose=True, noise_seed=0):
+        self.verbose = verbose
+        self._parse(config_dict)
         self.img_sgm = np.zeros((self.det_elem_count_vertical, self.view_num, self.det_elem_count_horizontal),
                                 dtype=np.float32)
         self.device = device
@@ -68,7 +87,7 @@ class Mgfpj_v3:  # noqa: N801 - reference name
     @property
     def pipeline(self):
         if self._pipe is None:
-            self._pipe = FpPipeline(self, self.device)
+            self._pipe = FpPipeline(self, self.device, self.VERSION)
         return self._pipe
 
     def ReadImage(self, file):  # noqa: N802 - reference name
@@ -131,3 +150,49 @@ def run_mgfpj_v3(file_path, device=None, verbose=True, noise_seed=0):
             print(f"\nWarning: Did not find files like {fpj.input_files_pattern:s} in {fpj.input_dir:s}.")
     gc.collect()
     return sgm
+
+
+class Mgfpj(Mgfpj_v3):
+    """Drop-in for Mgfpj of run_mgfpj_v2.py:69-470 (Mgfbp-derived, row by row)."""
+
+    VERSION = 2
+
+    def _parse(self, config_dict):
+        parse_fbp(self, config_dict)
+        parse_fpj(self, config_dict)
+
+
+class MgfpjOriginal(Mgfpj_v3):
+    """Drop-in for the stand-alone Mgfpj of run_mgfpj.py:56-669."""
+
+    VERSION = 1
+
+    def _parse(self, config_dict):
+        parse_fpj_v1(self, config_dict)
+
+    def ReadImage(self, file):  # noqa: N802 - reference name
+        """run_mgfpj.py:618-638 (only the first replacement pair is used)."""
+        return super().ReadImage(file)
+
+
+def _run(cls, file_path, device, verbose, noise_seed):
+    start = time.time()
+    if not os.path.exists(file_path):
+        raise ConfigError(f"ERROR: Config File {file_path} does not exist!")
+    fpj = cls(ReadConfigFile(file_path), device=device, verbose=verbose, noise_seed=noise_seed)
+    sgm = fpj.MainFunction()
+    if verbose and fpj.file_processed_count > 0:
+        print(f"\nA total of {fpj.file_processed_count:d} files are forward projected!")
+        print(f"Time cost is {time.time() - start:.3} sec\n")
+    gc.collect()
+    return sgm
+
+
+def run_mgfpj(file_path, device=None, verbose=True, noise_seed=0):
+    """Drop-in for run_mgfpj.run_mgfpj (run_mgfpj.py:24-53)."""
+    return _run(MgfpjOriginal, file_path, device, verbose, noise_seed)
+
+
+def run_mgfpj_v2(file_path, device=None, verbose=True, noise_seed=0):
+    """Drop-in for run_mgfpj_v2.run_mgfpj_v2 (run_mgfpj_v2.py:35-66)."""
+    return _run(Mgfpj, file_path, device, verbose, noise_seed)

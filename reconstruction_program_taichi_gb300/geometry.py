@@ -234,3 +234,45 @@ def ir_geometry(obj, device=None):
                         device=device)
     dg.host = dict(u=u, v=v, angles=angles)
     return dg
+
+
+def fpj_v2_arrays(obj):
+    """Mgfpj.MainFunction (run_mgfpj_v2.py:70-110) only runs Mgfbp.InitializeArrays:
+    the first nu entries of the (nu*oversample)-long u table hold the FBP u array,
+    the rest stay 0; v and the angles are the FBP arrays."""
+    u_fbp, v, angles = fbp_arrays(obj)
+    u = np.zeros(obj.det_elem_count_horizontal * obj.oversample_size)
+    u[:obj.det_elem_count_horizontal] = u_fbp
+    return u, v, angles
+
+
+def fpj_v1_arrays(obj):
+    """Mgfpj.MainFunction of run_mgfpj.py:57-66: FPJ-convention u and v (row 0 =
+    top) and angles from StartAngle."""
+    angles = angle_array(obj.view_num, obj.start_angle, obj.scan_angle)
+    v = det_positions_fpj(obj.det_elem_count_vertical, -obj.det_elem_height, obj.det_offset_vertical)
+    u = det_positions_fpj(obj.det_elem_count_horizontal * obj.oversample_size,
+                          -obj.det_elem_width / obj.oversample_size, -obj.det_offset_horizontal)
+    return u, v, angles
+
+
+def fpj_variant_geometry(obj, version, device=None):
+    """Forward-projector geometry of run_mgfpj.py (version 1) or run_mgfpj_v2.py
+    (version 2): step count (l_max - l_min)/(step*vd) and one image centre z."""
+    from .ops import DeviceGeometry
+    u, v, angles = fpj_v1_arrays(obj) if version == 1 else fpj_v2_arrays(obj)
+    g = _base_geom(obj)
+    g.nu = obj.det_elem_count_horizontal * obj.oversample_size
+    g.nv = obj.det_elem_count_vertical_actual
+    g.flags = _flags(obj, obj.bool_apply_pmatrix)
+    g.fp_steps = count_steps_ir(obj.img_dim, obj.img_dim_z, obj.img_pix_size, obj.img_voxel_height,
+                                obj.fpj_step_size, obj.source_isocenter_dis)
+    g.fp_step = obj.fpj_step_size
+    g.fp_z_per_view = helical_z_per_view(angles, v, obj.det_elem_count_vertical, obj.helical_pitch,
+                                         obj.source_isocenter_dis, obj.source_det_dis) if obj.helical_scan else 0.0
+    pa = pxs = None
+    if obj.bool_apply_pmatrix:
+        pa, pxs = obj.matrix_A_each_view, obj.x_s_each_view
+    dg = DeviceGeometry(g, angles, u=u, v=v[:g.nv], pmat_a=pa, pmat_xs=pxs, device=device)
+    dg.host = dict(u=u, v=v, angles=angles)
+    return dg

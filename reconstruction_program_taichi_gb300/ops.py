@@ -136,14 +136,27 @@ def fdk_bp(dg, packed, dtype=MCT_F32, out=None):
 
 # ---------------------------------------------------------------- forward projection
 
-def fp(dg, vol, mask=None, out=None):
+def fp_workspace(dg):
+    """Per-geometry workspace of fp() (the transposed volume copy), cached."""
+    ws = getattr(dg, "_fp_ws", None)
+    if ws is None:
+        n = int(_lib.load().mct_fp_workspace_size(dg.g()))
+        ws = torch.empty(max(n // 4, 1), dtype=torch.float32, device=dg.device)
+        dg._fp_ws = ws
+    return ws
+
+
+def fp(dg, vol, mask=None, out=None, workspace=True):
+    """P vol.  workspace=True uses the geometry's cached transposed-volume buffer
+    (coalesced gathers for every view); None runs without it."""
     _check(vol, "vol", dg.vol_shape)
     if mask is not None:
         _check(mask, "mask", dg.sgm_shape)
     if out is None:
         out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=vol.device)
     _check(out, "out", dg.sgm_shape)
-    _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _stream())
+    ws = fp_workspace(dg) if workspace is True else workspace
+    _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), _stream())
     return out
 
 

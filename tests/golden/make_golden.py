@@ -88,6 +88,18 @@ FPJ_CASES = {
     "fpj_helical": _upd(BASE_FPJ, HelicalPitch=0.5, TotalScanAngle=720, Views=16),
 }
 
+# the original stand-alone projector (run_mgfpj.py) and the Mgfbp-derived one
+# (run_mgfpj_v2.py)
+FPJ_V1_CASES = {
+    "fpjv1_cone": _upd(BASE_FPJ, StartAngle=20, ImageRotation=None, DetectorOffsetVertical=None,
+                       DetectorZOffcenter=0.4),
+    "fpjv1_fan_oversample2": _upd(BASE_FPJ, ConeBeam=False, OversampleSize=2, ImageDimensionZ=3,
+                                  ImageDimension=12, PhotonNumber=None),
+}
+FPJ_V2_CASES = {
+    "fpjv2_cone_rowrange": _upd(BASE_FPJ, DetectorElementVerticalReconRange=[2, 9]),
+}
+
 BASE_IR = {
     "InputFiles": "sgm_.*.raw", "OutputFilePrefix": "", "OutputFileReplace": ["sgm", "rec"],
     "InputFileForm": "post_log_images",
@@ -179,6 +191,26 @@ def run_fpj_case(name, cfg, R3, rng):
                     angles=_arr(fpj.array_angle_taichi), cz=_arr(fpj.array_img_center_z_taichi).ravel())
 
 
+def run_fpj_variant_case(name, cfg, module, rng):
+    """Mgfpj of run_mgfpj.py (v1) or run_mgfpj_v2.py (v2)."""
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("img")
+        os.makedirs("sgm")  # run_mgfpj.py does not create its output folder
+        cfg.update(InputDir=d + "/img", OutputDir=d + "/sgm")
+        nz = cfg.get("ImageDimensionZ") if cfg.get("ConeBeam") else cfg.get("ImageDimensionZ",
+                                                                             cfg["DetectorElementCountVertical"])
+        if not cfg.get("ConeBeam") and "DetectorElementVerticalReconRange" not in cfg and name.startswith("fpjv2"):
+            nz = cfg["DetectorElementCountVertical"]
+        vol = _smooth_volume(rng, nz, cfg["ImageDimension"])
+        vol.tofile("img/img_a.raw")
+        json.dump(cfg, open("config.jsonc", "w"))
+        fpj = module.Mgfpj(module.ReadConfigFile("config.jsonc"))
+        sgm = fpj.MainFunction()
+        return dict(config=json.dumps(cfg), input_vol=vol, sgm=np.asarray(sgm, np.float64),
+                    u=_arr(fpj.array_u_taichi), v=_arr(fpj.array_v_taichi), angles=_arr(fpj.array_angle_taichi))
+
+
 def run_ir_case(name, cfg, RI, RP, R, rng):
     cfg = _clean(cfg)
     with tempfile.TemporaryDirectory() as d, _chdir(d):
@@ -234,8 +266,11 @@ def main():
     import run_mgfpj_v3 as R3
     import run_mgfbp_iterative_recon_IRN_CGLS as RI
     import run_mgfbp_iterative_recon_IRN_CGLS_piccs as RP
+    import run_mgfpj as R1
+    import run_mgfpj_v2 as R2
     jobs = [(k, v, "fbp") for k, v in FBP_CASES.items()] + [(k, v, "fpj") for k, v in FPJ_CASES.items()] \
-        + [(k, v, "ir") for k, v in IR_CASES.items()]
+        + [(k, v, "ir") for k, v in IR_CASES.items()] + [(k, v, "v1") for k, v in FPJ_V1_CASES.items()] \
+        + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()]
     for i, (name, cfg, kind) in enumerate(jobs):
         if only and name not in only:
             continue
@@ -247,6 +282,8 @@ def main():
                 out = run_fbp_case(name, cfg, R, rng)
             elif kind == "fpj":
                 out = run_fpj_case(name, cfg, R3, rng)
+            elif kind in ("v1", "v2"):
+                out = run_fpj_variant_case(name, cfg, R1 if kind == "v1" else R2, rng)
             else:
                 out = run_ir_case(name, cfg, RI, RP, R, rng)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)

@@ -54,7 +54,7 @@ def test_run_mgfbp_matches_reference(name, tmp_path, cuda):
     assert len(out) == 1
 
 
-@pytest.mark.parametrize("name", golden_names("fpj"))
+@pytest.mark.parametrize("name", golden_names("fpj_"))
 def test_run_mgfpj_v3_matches_reference(name, tmp_path, cuda):
     from reconstruction_program_taichi_gb300 import run_mgfpj_v3
     z = load_golden(name)
@@ -233,3 +233,24 @@ def test_cgls_fused_update_matches_numpy(cuda):
     np.testing.assert_allclose(t[0].cpu().numpy(), x2, rtol=1e-5, atol=1e-6)
     np.testing.assert_allclose(t[1].cpu().numpy(), r2, rtol=1e-5, atol=1e-6)
     np.testing.assert_allclose(t[2].cpu().numpy(), d2, rtol=1e-5, atol=1e-5)
+
+
+def test_fp_transposed_copy_is_bit_identical(cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    o = _cone_obj(views=48)
+    dg = geometry.fpj_geometry(o)
+    vol = torch.from_numpy(_smooth(np.random.default_rng(8), o.img_dim_z, o.img_dim)).cuda()
+    a = ops.fp(dg, vol, workspace=None)
+    b = ops.fp(dg, vol, workspace=True)
+    assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("name", golden_names("fpjv"))
+def test_run_mgfpj_v1_v2_match_reference(name, tmp_path, cuda):
+    from reconstruction_program_taichi_gb300.fpj import run_mgfpj, run_mgfpj_v2
+    z = load_golden(name)
+    fn = run_mgfpj if name.startswith("fpjv1") else run_mgfpj_v2
+    sgm = fn(_write_case(z, tmp_path, "fpj"), verbose=False)
+    assert sgm.shape == z["sgm"].shape
+    assert rel_l2(sgm, z["sgm"]) < TOL

@@ -44,7 +44,7 @@ def test_fbp_arrays_and_taps(name, tmp_path):
         assert rel_l2(g, z["gauss_v"]) < 1e-12
 
 
-@pytest.mark.parametrize("name", golden_names("fpj"))
+@pytest.mark.parametrize("name", golden_names("fpj_"))
 def test_fpj_arrays(name, tmp_path):
     z = load_golden(name)
     o = _parse(z["config"], "fpj", tmp_path)
@@ -112,3 +112,21 @@ def test_jsonc_comment_stripping(tmp_path):
         config.load_jsonc(str(p))  # the reference's regex also strips '//' inside strings
     p.write_text('// header\n{ "a": 1, /* block\n comment */ "b": 2 // tail\n}\n')
     assert config.load_jsonc(str(p)) == {"a": 1, "b": 2}
+
+
+@pytest.mark.parametrize("name", golden_names("fpjv"))
+def test_fpj_variant_arrays(name, tmp_path):
+    z = load_golden(name)
+    cfg = copy.deepcopy(z["config"])
+    cfg["InputDir"], cfg["OutputDir"] = str(tmp_path), str(tmp_path / "out")
+    o = _Obj()
+    if name.startswith("fpjv1"):
+        config.parse_fpj_v1(o, cfg)
+        u, v, angles = geometry.fpj_v1_arrays(o)
+    else:
+        config.parse_fbp(o, cfg)
+        config.parse_fpj(o, cfg)
+        u, v, angles = geometry.fpj_v2_arrays(o)
+    np.testing.assert_allclose(u, z["u"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(v, z["v"][:len(v)], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(angles, z["angles"], rtol=0, atol=1e-12)
