@@ -205,6 +205,17 @@ size_t mct_reduce_scratch_size(void);
 int mct_dot_f64(const float* a, const float* b, int64_t n, double* partials, double* result,
                 void* stream);
 
+/* The same float64 inner product for callers that cannot allocate device memory
+ * (for example an application that manages all GPU memory itself and passes the
+ * library only its input and output buffers).  No counterpart in the reference.
+ * The per-block partial sums live in a fixed 512 KiB device array inside the
+ * library, held by every GPU that loads it until the process exits, so
+ * n <= 134,217,728; larger n returns MCT_E_INVALID.  The first call on a device
+ * looks up that array's address (make it before any stream capture).  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  No cudaMalloc/cudaFree is made. */
+int mct_dot_f64_noalloc(const float* a, const float* b, int64_t n, double* result, void* stream);
+
 /* One fused CGLS step on device scalars (no host round trip), following
  * TikhonovSol run_mgfbp_iterative_recon_IRN_CGLS.py:198-217:
  *   alpha = rr / dq;  x += alpha d;  r -= alpha q;  rr_new = sum r^2 (float64);

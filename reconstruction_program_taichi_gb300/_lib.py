@@ -80,6 +80,7 @@ SIGNATURES = {
     "mct_tv_penalty": (ctypes.c_int, [_G, _P, _f32, _P, _P, _P]),
     "mct_reduce_scratch_size": (ctypes.c_size_t, []),
     "mct_dot_f64": (ctypes.c_int, [_P, _P, _i64, _P, _P, _P]),
+    "mct_dot_f64_noalloc": (ctypes.c_int, [_P, _P, _i64, _P, _P]),
     "mct_cgls_update": (ctypes.c_int, [_i64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mct_cgls_direction": (ctypes.c_int, [_i64, _P, _P, _P, _P, _P]),
     "mct_project_ellipsoids": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
