@@ -144,11 +144,16 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
     const bool tr = vol_t != nullptr && spread_along_y(p, j, angles, pa);
     const float* __restrict__ V = tr ? vol_t : vol;
     const int sx = tr ? nx : 1, sy = tr ? 1 : nx;
-    const int64_t plane = (int64_t)nx * nx;
+    const int plane = nx * nx;  // volumes below 2^31 voxels (checked on the host)
     Ray r;
     float acc = 0.0f;
     if (setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) {
         const float xmax = (float)(nx - 1), zmax = (float)(p.nz - 1);
+        // Consecutive samples are 0.2 voxel diagonals apart, so most fall in the same
+        // 2x2x2 cell as the previous one: the 8 corners stay in registers and are
+        // reloaded only when the cell changes.
+        int cell = -1;
+        float a00 = 0.f, a01 = 0.f, a10 = 0.f, a11 = 0.f, c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
 #pragma unroll 4
         for (int k = r.ks; k <= r.ke; ++k) {
             const float fk = (float)k;
@@ -170,14 +175,20 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
             } else {
                 zi = iv;
             }
-            const float* b = V + (int64_t)zi * plane + (int64_t)yi * sy + (int64_t)xi * sx;
-            const float a00 = __ldg(b), a01 = __ldg(b + sx), a10 = __ldg(b + sy), a11 = __ldg(b + sx + sy);
+            const int off = zi * plane + yi * sy + xi * sx;
+            if (off != cell) {
+                cell = off;
+                const float* b = V + off;
+                a00 = __ldg(b); a01 = __ldg(b + sx); a10 = __ldg(b + sy); a11 = __ldg(b + sx + sy);
+                if (CONE) {
+                    const float* c = b + plane;
+                    c00 = __ldg(c); c01 = __ldg(c + sx); c10 = __ldg(c + sy); c11 = __ldg(c + sx + sy);
+                }
+            }
             const float l0 = fmaf(xw, a01 - a00, a00);
             const float l1 = fmaf(xw, a11 - a10, a10);
             float val = fmaf(yw, l1 - l0, l0);
             if (CONE) {
-                const float* c = b + plane;
-                const float c00 = __ldg(c), c01 = __ldg(c + sx), c10 = __ldg(c + sy), c11 = __ldg(c + sx + sy);
                 const float m0 = fmaf(xw, c01 - c00, c00);
                 const float m1 = fmaf(xw, c11 - c10, c10);
                 const float hi = fmaf(yw, m1 - m0, m0);
@@ -224,7 +235,27 @@ fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __r
     Ray r;
     if (!setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) return;
     const int nx = p.nx;
-    const int64_t plane = (int64_t)nx * nx;
+    const int plane = nx * nx;
+    // The 8 corner weights of consecutive samples in the same cell are summed in
+    // registers and scattered once when the ray leaves the cell.
+    int cell = -1;
+    float s00 = 0.f, s01 = 0.f, s10 = 0.f, s11 = 0.f, t00 = 0.f, t01 = 0.f, t10 = 0.f, t11 = 0.f;
+    auto flush = [&]() {
+        if (cell < 0) return;
+        float* b = vol + cell;
+        atomicAdd(b, s00);
+        atomicAdd(b + 1, s01);
+        atomicAdd(b + nx, s10);
+        atomicAdd(b + nx + 1, s11);
+        if (p.cone) {
+            float* c = b + plane;
+            atomicAdd(c, t00);
+            atomicAdd(c + 1, t01);
+            atomicAdd(c + nx, t10);
+            atomicAdd(c + nx + 1, t11);
+        }
+        s00 = s01 = s10 = s11 = t00 = t01 = t10 = t11 = 0.f;
+    };
     for (int k = r.ks; k <= r.ke; ++k) {
         const float fk = (float)k;
         const float fx = fmaf(fk, r.dfx, r.fx0);
@@ -243,23 +274,27 @@ fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __r
         } else {
             zi = iv;
         }
-        float* b = vol + (int64_t)zi * plane + (int64_t)(int)yf * nx + (int)xf;
+        const int off = zi * plane + (int)yf * nx + (int)xf;
+        if (off != cell) {
+            flush();
+            cell = off;
+        }
         const float wl = p.cone ? (1.0f - zw) * yv : yv;
         const float w00 = (1.0f - xw) * (1.0f - yw), w01 = xw * (1.0f - yw);
         const float w10 = (1.0f - xw) * yw, w11 = xw * yw;
-        atomicAdd(b, w00 * wl);
-        atomicAdd(b + 1, w01 * wl);
-        atomicAdd(b + nx, w10 * wl);
-        atomicAdd(b + nx + 1, w11 * wl);
+        s00 += w00 * wl;
+        s01 += w01 * wl;
+        s10 += w10 * wl;
+        s11 += w11 * wl;
         if (p.cone) {
             const float wh = zw * yv;
-            float* c = b + plane;
-            atomicAdd(c, w00 * wh);
-            atomicAdd(c + 1, w01 * wh);
-            atomicAdd(c + nx, w10 * wh);
-            atomicAdd(c + nx + 1, w11 * wh);
+            t00 += w00 * wh;
+            t01 += w01 * wh;
+            t10 += w10 * wh;
+            t11 += w11 * wh;
         }
     }
+    flush();
 }
 
 // Effective ray map, run_mgfbp_iterative_recon_IRN_CGLS.py:749-833.
@@ -411,6 +446,7 @@ int make_params(const mct_geom* g, FpParams& p, const char* who) {
     MCT_REQUIRE(p.cone || g->nz >= g->nv, "%s: fan beam needs one image slice per detector row", who);
     MCT_REQUIRE(!p.cone || g->pz > 0.0f, "%s: cone beam needs a positive voxel height", who);
     MCT_REQUIRE(g->px > 0.0f, "%s: pixel size must be positive", who);
+    MCT_REQUIRE((int64_t)g->nz * g->nx * g->nx < ((int64_t)1 << 31), "%s: volume must have fewer than 2^31 voxels", who);
     p.sid = g->sid; p.sdd = g->sdd; p.cx = g->cx; p.cy = g->cy; p.cz = g->cz;
     // run_mgfpj_v3.py:210-239 in double, then rounded
     const double px = g->px, pz = p.cone ? g->pz : 0.0;
