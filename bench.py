@@ -263,27 +263,39 @@ def run_gpu(args, w):
            "h2d_bytes_per_step": int(host_sgm.numel() * 4),
            "d2h_bytes_per_step": int(host_vol.numel() * 4 + host_fp.numel() * 4)}
 
-    # mixed-precision storage variant of the FDK (bf16 backprojection operand)
+    # mixed-precision FDK variants: tensor-core split-bf16 filter, with float32 or bf16
+    # backprojection operand
     mixed = None
     if args.storage == "f32" and not args.no_mixed:
-        pm = fbp.FdkPipeline(o, device=dev, storage="bf16")
-        pm.taps.copy_(pipe.taps)
         ref_vol = pipe.run(sgm).clone()
-        for _ in range(2):
-            mv = pm.run(sgm)
-        barrier()
-        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        m0.record(stream)
-        for _ in range(args.steps):
-            mv = pm.run(sgm)
-        m1.record(stream)
-        barrier()
-        mms = m0.elapsed_time(m1) / args.steps
-        rel = float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol))
-        mixed = {"fdk_ms": round(mms, 3), "fdk_plain_ms": round(float(st[0] + st[1] + st[2]), 3),
-                 "speedup_fdk": round(float(st[0] + st[1] + st[2]) / mms, 3), "rel_l2_vs_plain": rel,
-                 "storage": "bf16 packed backprojection operand"}
-        del pm
+        plain_ms = float(st[0] + st[1] + st[2])
+        mixed = {"fdk_plain_ms": round(plain_ms, 3)}
+        for name, storage in (("tc_filter", "f32"), ("tc_filter_bf16_bp", "bf16")):
+            pm = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl="tc")
+            pm.set_taps(pipe.taps.cpu().numpy())
+            for _ in range(2):
+                mv = pm.run(sgm)
+            barrier()
+            m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            m0.record(stream)
+            for _ in range(args.steps):
+                mv = pm.run(sgm)
+            m1.record(stream)
+            f0.record(stream)
+            pm.filter(sgm)
+            f1.record(stream)
+            barrier()
+            pm.tc.status()
+            mms = m0.elapsed_time(m1) / args.steps
+            rel = float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol))
+            mixed[name] = {"fdk_ms": round(mms, 3), "weight_filter_ms": round(f0.elapsed_time(f1), 3),
+                           "speedup_fdk": round(plain_ms / mms, 3), "rel_l2_vs_plain": rel}
+            del pm
+
+    cgls = None
+    if not args.no_cgls and w is WORKLOAD:
+        cgls = cgls_bench(dev, stream, barrier)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -308,12 +320,53 @@ def run_gpu(args, w):
             "fp_gups": round(nvox * w["views"] / (st[3] / 1e3) / 1e9, 2),
             "fp_samples_per_s": round(n_samples / (st[3] / 1e3), 1), "fp_in_volume_samples": n_samples,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clk.summary(), "mixed": mixed,
+            "clocks": clk.summary(), "mixed": mixed, "cgls_c3": cgls,
         }
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+C3 = dict(nu=1024, nv=64, views=360, nx=512, nz=64, du=0.8, dv=0.8, px=0.4, pz=0.4, sid=600.0, sdd=1100.0,
+          step=0.2, n_ell=20, photons=1e5, seed=2025)
+
+
+def cgls_bench(dev, stream, barrier, iters=5):
+    """Seconds per CGLS iteration (one P^T P + TV + fused updates) of the IRN-CGLS-TV
+    configuration: 512x512x64 volume, 360 views, 1024x64 detector, lambda 1e-3, with
+    the reference's operator pair (masked FP + voxel-driven backprojector)."""
+    import torch
+    from reconstruction_program_taichi_gb300 import config, ops
+    from reconstruction_program_taichi_gb300.ir import IrSystem
+    cfg = make_config(C3)
+    cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 20, "NumberOfIterations": 10})
+    o = Obj()
+    config.parse_fbp(o, cfg)
+    config.parse_fpj(o, cfg)
+    config.parse_fpj_v3(o, cfg)
+    config.parse_ir(o, cfg)
+    sy = IrSystem(o, device=dev)
+    sgm = ops.project_ellipsoids(sy.dg, ellipsoids(C3))
+    x0 = torch.zeros(sy.dg.vol_shape, dtype=torch.float32, device=dev)
+    sy.bpb = sy.bp_b(sgm)
+    wr = ops.tv_weights(sy.dg, x0 + 0.01, 1e-6)
+    lr = o.coef_lambda * o.pixel_count_ratio
+    sy.cgls(x0, [], [(lr, wr)], 1)  # warm-up
+    barrier()
+    calls0 = sy.ptp_calls
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    x = sy.cgls(x0, [], [(lr, wr)], iters)
+    e1.record(stream)
+    barrier()
+    n = sy.ptp_calls - calls0  # the reference's "iterations": P^T P applications
+    s = e0.elapsed_time(e1) / 1e3
+    total = 21 * 11  # 1 + 20 reweightings, each 1 + 10 P^T P (run_mgfbp_iterative_recon_IRN_CGLS.py:165-169)
+    return {"s_per_iter": round(s / n, 5), "ptp_per_solve": iters + 1, "timed_ptp": n,
+            "projected_20x10_s": round(s / n * total, 2), "operator": "reference pair (masked FP + per-view BP)",
+            "config": "512x512x64 @0.4mm, 360 views, 1024x64 det, lambda 1e-3",
+            "finite": bool(torch.isfinite(x).all())}
 
 
 # ---------------------------------------------------------------- CPU (reference) arm
@@ -413,6 +466,7 @@ def main():
                     help="c2: the benchmark; small: quick checks; prof: short launches for ncu captures")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-cgls", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]

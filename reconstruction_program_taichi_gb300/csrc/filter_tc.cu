@@ -1,0 +1,407 @@
+// Toeplitz row filter on the 5th-generation tensor cores (tcgen05), split BF16.
+//
+// Y[R][k] = du * sum_m X[R][m] h[k-m+nu-1] is a GEMM  D[M x N] = A[M x K] B[K x N]
+// with M = rows*views sinogram rows, N = K = nu.  Each float32 operand is split into
+// bf16 hi + lo parts and D = A_hi B_hi + A_hi B_lo + A_lo B_hi is accumulated in
+// float32 in tensor memory (the dropped A_lo B_lo term is ~2^-16 relative).
+// Replaces the row convolution of Mgfbp.ConvolveSgmAndKernel (run_mgfbp.py:1030-1046).
+//
+// Operand layout.  A and B^T are stored pre-tiled in global memory exactly as one
+// pipeline stage needs them in shared memory (tcgen05 canonical K-major layout, no
+// swizzle): a 128x64 (A) or 256x64 (B^T) bf16 tile is one contiguous block of 8x8
+// "core matrices" (8 rows x 16 bytes each); core (row group i, k group j) sits at
+// byte (i*8 + j)*128.  So the K-direction core stride (LBO) is 128 B and the
+// row-direction stride (SBO) is 1 KiB, and each stage is filled by plain bulk copies
+// (cp.async.bulk, the TMA engine) of contiguous tiles.
+//
+// Kernel structure: 128 threads.  Thread 0 issues the bulk copies of a 2-stage ring,
+// thread 32 issues tcgen05.mma (M=128, N=256, K=16; 3 products per K step) and
+// commits each stage back to the producer; after the last stage all four warps read
+// the 128x256 float32 accumulator from tensor memory (warp w owns lanes 32w..32w+31)
+// and store du*D to the view-major output.  Every mbarrier wait is bounded (about 2 s
+// of %globaltimer); a timeout sets an error flag, the kernel waits (bounded) for its
+// own copies and MMAs, frees its tensor memory and returns; the host reports
+// MCT_E_TIMEOUT on the next call that reads the flag.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace mct {
+namespace {
+
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 2;
+constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                    // 16 KiB
+constexpr int TC_B_TILE = TC_BN * TC_BK * 2;                    // 32 KiB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_TILE + 2 * TC_B_TILE;   // 96 KiB
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 2048;      // + 1 KiB alignment slack + barriers
+constexpr int TC_TMEM_COLS = 256;
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;        // 2 s
+
+struct TcDims {
+    int64_t rows;    // M (sinogram rows)
+    int nu;          // N = K
+    int mb, kb, nb;  // tile counts along M, K, N
+};
+
+inline TcDims tc_dims(int64_t rows, int nu) {
+    TcDims d;
+    d.rows = rows;
+    d.nu = nu;
+    d.mb = (int)((rows + TC_BM - 1) / TC_BM);
+    d.kb = (nu + TC_BK - 1) / TC_BK;
+    d.nb = (nu + TC_BN - 1) / TC_BN;
+    return d;
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(float x) { return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+
+// split x into bf16 hi + lo (bit patterns)
+__device__ __forceinline__ void split2(float x, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    hi = (uint32_t)__bfloat16_as_ushort(h);
+    lo = bf16_bits(x - __bfloat162float(h));
+}
+
+// Thread i writes one 16-byte core-matrix row (8 bf16 along K) of the hi and lo
+// A tiles.  i enumerates (tile = mb*KB + kb, row group mi, k group kj, row r8) in
+// storage order, so consecutive threads write consecutive 16-byte chunks.
+__global__ void split_a_kernel(const float* __restrict__ x, int64_t rows, int nu, int KB, int64_t n_chunks,
+                               uint4* __restrict__ a_hi, uint4* __restrict__ a_lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r8 = (int)(i & 7);
+        const int kj = (int)((i >> 3) & 7);
+        const int mi = (int)((i >> 6) & 15);
+        const int64_t tile = i >> 10;
+        const int kb = (int)(tile % KB);
+        const int64_t mb = tile / KB;
+        const int64_t R = mb * TC_BM + mi * 8 + r8;
+        const int m0 = kb * TC_BK + kj * 8;
+        uint32_t h[8], l[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int m = m0 + c;
+            const float v = (R < rows && m < nu) ? x[R * nu + m] : 0.0f;
+            split2(v, h[c], l[c]);
+        }
+        a_hi[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+        a_lo[i] = make_uint4(l[0] | (l[1] << 16), l[2] | (l[3] << 16), l[4] | (l[5] << 16), l[6] | (l[7] << 16));
+    }
+}
+
+// B^T element (n, k) = T[k][n] = h[n - k + nu - 1] (output column n, input column k),
+// tiled like A with 256-row tiles: chunk i enumerates (tile = nb*KB + kb, ni, kj, r8).
+__global__ void build_b_kernel(const float* __restrict__ taps, int nu, int KB, int64_t n_chunks,
+                               uint4* __restrict__ b_hi, uint4* __restrict__ b_lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r8 = (int)(i & 7);
+        const int kj = (int)((i >> 3) & 7);
+        const int ni = (int)((i >> 6) & 31);
+        const int64_t tile = i >> 11;
+        const int kb = (int)(tile % KB);
+        const int nb = (int)(tile / KB);
+        const int n = nb * TC_BN + ni * 8 + r8;
+        const int k0 = kb * TC_BK + kj * 8;
+        uint32_t h[8], l[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int k = k0 + c;
+            const float v = (n < nu && k < nu) ? taps[n - k + nu - 1] : 0.0f;
+            split2(v, h[c], l[c]);
+        }
+        b_hi[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+        b_lo[i] = make_uint4(l[0] | (l[1] << 16), l[2] | (l[3] << 16), l[4] | (l[5] << 16), l[6] | (l[7] << 16));
+    }
+}
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; returns false (and raises the error flag) after TC_WAIT_NS.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (global_ns() - t0 > TC_WAIT_NS) {
+            atomicExch(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    // start address >> 4 (bits 0-13), leading byte offset >> 4 (16-29), stride byte
+    // offset >> 4 (32-45), fixed 0b001 (46-48), no swizzle (61-63 = 0)
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(128, 1)
+tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict__ a_hi, const uint4* __restrict__ a_lo,
+                 const uint4* __restrict__ b_hi, const uint4* __restrict__ b_lo, float* __restrict__ F,
+                 int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1 KiB-aligned stage buffers
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* ctrl = smem + TC_STAGES * TC_STAGE_BYTES;  // barriers and the TMEM address
+    uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);
+    uint64_t* empty = full + TC_STAGES;
+    uint64_t* done = empty + TC_STAGES;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nbk = blockIdx.x;  // N tile
+    const int64_t mbk = blockIdx.y;  // M tile
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TC_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        // producer: bulk copies of A (hi, lo) and B (hi, lo) tiles for every K block
+        int issued = 0;
+        for (int kb = 0; kb < d.kb && ok; ++kb) {
+            const int s = kb % TC_STAGES;
+            if (kb >= TC_STAGES) ok = mbar_wait(smem_u32(&empty[s]), ((kb / TC_STAGES) - 1) & 1, err, 1);
+            if (!ok) break;
+            unsigned char* st = smem + s * TC_STAGE_BYTES;
+            const uint32_t bar = smem_u32(&full[s]);
+            mbar_expect_tx(bar, TC_STAGE_BYTES);
+            const int64_t at = mbk * d.kb + kb;
+            const int64_t bt = (int64_t)nbk * d.kb + kb;
+            bulk_g2s(smem_u32(st), a_hi + at * (TC_A_TILE / 16), TC_A_TILE, bar);
+            bulk_g2s(smem_u32(st + TC_A_TILE), a_lo + at * (TC_A_TILE / 16), TC_A_TILE, bar);
+            bulk_g2s(smem_u32(st + 2 * TC_A_TILE), b_hi + bt * (TC_B_TILE / 16), TC_B_TILE, bar);
+            bulk_g2s(smem_u32(st + 2 * TC_A_TILE + TC_B_TILE), b_lo + bt * (TC_B_TILE / 16), TC_B_TILE, bar);
+            issued = kb + 1;
+        }
+        // drain: the copies of the last issued block of every stage must have landed
+        // before this CTA's shared memory is released (immediate on the normal path)
+        for (int kb = (issued > TC_STAGES ? issued - TC_STAGES : 0); kb < issued; ++kb)
+            mbar_wait(smem_u32(&full[kb % TC_STAGES]), (kb / TC_STAGES) & 1, err, 4);
+    } else if (threadIdx.x == 32) {
+        // MMA issuer
+        const uint32_t idesc = idesc_bf16(TC_BM, TC_BN);
+        for (int kb = 0; kb < d.kb && ok; ++kb) {
+            const int s = kb % TC_STAGES;
+            ok = mbar_wait(smem_u32(&full[s]), (kb / TC_STAGES) & 1, err, 2);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t st = smem_u32(smem + s * TC_STAGE_BYTES);
+            const uint32_t ahi = st, alo = st + TC_A_TILE, bhi = st + 2 * TC_A_TILE, blo = bhi + TC_B_TILE;
+#pragma unroll
+            for (int ks = 0; ks < TC_BK / 16; ++ks) {
+                const uint32_t off = ks * 256;  // two core matrices along K
+                const uint64_t dah = smem_desc(ahi + off, 128, 1024), dal = smem_desc(alo + off, 128, 1024);
+                const uint64_t dbh = smem_desc(bhi + off, 128, 1024), dbl = smem_desc(blo + off, 128, 1024);
+                mma_bf16(tmem, dah, dbh, idesc, (kb | ks) != 0);
+                mma_bf16(tmem, dah, dbl, idesc, 1);
+                mma_bf16(tmem, dal, dbh, idesc, 1);
+            }
+            mma_commit(smem_u32(&empty[s]));  // stage free once these MMAs complete
+        }
+        mma_commit(smem_u32(done));  // accumulator complete (or all issued MMAs drained)
+    }
+    __syncwarp();
+    // epilogue: every warp waits for the accumulator, then reads its 32 lanes
+    ok = mbar_wait(smem_u32(done), 0, err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // tcgen05.ld is warp-collective: decide per warp
+    const bool go = __all_sync(0xffffffffu, ok && *(volatile int*)err == 0);
+    if (go) {
+        const int64_t R = mbk * TC_BM + warp * 32 + lane;
+        const bool row_ok = R < d.rows;
+        float* dst = nullptr;
+        if (row_ok) {
+            const int r = (int)(R / views), j = (int)(R % views);
+            dst = F + ((int64_t)j * nv + r) * d.nu;
+        }
+        for (int c0 = 0; c0 < TC_BN; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (row_ok) {
+                const int n0 = nbk * TC_BN + c0;
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (n0 + i < d.nu) dst[n0 + i] = v[i] * du;
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+    }
+}
+
+}  // namespace
+}  // namespace mct
+
+using namespace mct;
+
+extern "C" {
+
+size_t mct_filter_tc_workspace_size(const mct_geom* g) {
+    if (!g || g->nu < 2 || g->nv < 1 || g->views < 1) return 0;
+    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
+    const size_t a = (size_t)d.mb * d.kb * TC_A_TILE;
+    const size_t b = (size_t)d.nb * d.kb * TC_B_TILE;
+    return 2 * a + 2 * b + 256;  // hi+lo tiles of A and B, error flag
+}
+
+// Workspace layout: [A_hi][A_lo][B_hi][B_lo][flag]
+static void tc_parts(const mct_geom* g, void* ws, uint4** ahi, uint4** alo, uint4** bhi, uint4** blo, int** flag) {
+    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
+    const size_t a = (size_t)d.mb * d.kb * TC_A_TILE;
+    const size_t b = (size_t)d.nb * d.kb * TC_B_TILE;
+    unsigned char* p = static_cast<unsigned char*>(ws);
+    *ahi = reinterpret_cast<uint4*>(p);
+    *alo = reinterpret_cast<uint4*>(p + a);
+    *bhi = reinterpret_cast<uint4*>(p + 2 * a);
+    *blo = reinterpret_cast<uint4*>(p + 2 * a + b);
+    *flag = reinterpret_cast<int*>(p + 2 * a + 2 * b);
+}
+
+int mct_filter_tc_prepare(const mct_geom* g, const float* taps, void* workspace, void* stream) {
+    MCT_TRY(check_geom(g, "mct_filter_tc_prepare"));
+    MCT_REQUIRE(taps && workspace, "mct_filter_tc_prepare: NULL buffer");
+    MCT_REQUIRE(((uintptr_t)workspace & 1023) == 0, "mct_filter_tc_prepare: workspace must be 1 KiB aligned");
+    uint4 *ahi, *alo, *bhi, *blo;
+    int* flag;
+    tc_parts(g, workspace, &ahi, &alo, &bhi, &blo, &flag);
+    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
+    cudaStream_t s = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    if (e != cudaSuccess) {
+        set_error("mct_filter_tc_prepare: %s", cudaGetErrorString(e));
+        return MCT_E_CUDA;
+    }
+    const int64_t chunks = (int64_t)d.nb * d.kb * (TC_B_TILE / 16);
+    const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
+    build_b_kernel<<<grid, 256, 0, s>>>(taps, g->nu, d.kb, chunks, bhi, blo);
+    return launched("build_b_kernel");
+}
+
+int mct_filter_tc(const mct_geom* g, const float* weighted, void* workspace, float* filtered, void* stream) {
+    MCT_TRY(check_geom(g, "mct_filter_tc"));
+    MCT_REQUIRE(weighted && workspace && filtered, "mct_filter_tc: NULL buffer");
+    MCT_REQUIRE(((uintptr_t)workspace & 1023) == 0, "mct_filter_tc: workspace must be 1 KiB aligned");
+    uint4 *ahi, *alo, *bhi, *blo;
+    int* flag;
+    tc_parts(g, workspace, &ahi, &alo, &bhi, &blo, &flag);
+    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
+    MCT_REQUIRE(d.mb < 65535 * 32, "mct_filter_tc: too many rows");
+    cudaStream_t s = as_stream(stream);
+    const int64_t chunks = (int64_t)d.mb * d.kb * (TC_A_TILE / 16);
+    const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
+    split_a_kernel<<<grid, 256, 0, s>>>(weighted, d.rows, g->nu, d.kb, chunks, ahi, alo);
+    MCT_TRY(launched("split_a_kernel"));
+    {
+        // opt in to the large dynamic shared memory (per device, idempotent)
+        cudaError_t e = cudaFuncSetAttribute(tc_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+        if (e != cudaSuccess) {
+            set_error("mct_filter_tc: cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+            return MCT_E_CUDA;
+        }
+    }
+    dim3 grid2(d.nb, d.mb);
+    tc_filter_kernel<<<grid2, 128, TC_SMEM, s>>>(d, g->nv, g->views, g->du, ahi, alo, bhi, blo, filtered, flag);
+    return launched("tc_filter_kernel");
+}
+
+// 0 if no tensor-core filter launch on this workspace has timed out, else MCT_E_TIMEOUT
+// (synchronises the stream).
+int mct_filter_tc_status(const mct_geom* g, void* workspace, void* stream) {
+    MCT_REQUIRE(g && workspace, "mct_filter_tc_status: NULL argument");
+    uint4 *ahi, *alo, *bhi, *blo;
+    int* flag;
+    tc_parts(g, workspace, &ahi, &alo, &bhi, &blo, &flag);
+    int h = 0;
+    cudaStream_t s = as_stream(stream);
+    cudaError_t e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_error("mct_filter_tc_status: %s", cudaGetErrorString(e));
+        return MCT_E_CUDA;
+    }
+    if (h != 0) {
+        set_error("mct_filter_tc: a pipeline wait timed out (stage %d)", h);
+        return MCT_E_TIMEOUT;
+    }
+    return MCT_OK;
+}
+
+}  // extern "C"

@@ -122,7 +122,12 @@ __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const f
     return fabsf(cb) > fabsf(sb);  // d(x, y)/du is (-sin b, cos b)
 }
 
-// One thread per ray (u, v) of view j = blockIdx.z.  vol is [z][y][x]; vol_t, when
+// Grid of every ray kernel: x = 32-column detector tiles, y = views, z = 8-row
+// detector tiles.  Blocks are scheduled x, then y, then z, so the blocks resident at
+// one time cover many views of the same detector rows; those rays cross only a thin
+// z-slab of the volume, which then stays in L2 across views.
+//
+// One thread per ray (u, v) of view j = blockIdx.y.  vol is [z][y][x]; vol_t, when
 // given, is the same volume as [z][x][y]: views whose detector columns spread along
 // y read vol_t so that the 32 rays of a warp touch consecutive addresses.
 template <bool CONE>
@@ -132,8 +137,8 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
           const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
           const float* __restrict__ mask, float* __restrict__ sgm) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int j = blockIdx.z;
+    const int iv = blockIdx.z * blockDim.y + threadIdx.y;
+    const int j = blockIdx.y;
     if (iu >= p.nu || iv >= p.nv) return;
     const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
     if (mask && mask[oidx] != 1.0f) {
@@ -225,8 +230,8 @@ fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __r
                   const float* __restrict__ pxs, const float* __restrict__ sgm, const float* __restrict__ mask,
                   float* __restrict__ vol) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int j = blockIdx.z;
+    const int iv = blockIdx.z * blockDim.y + threadIdx.y;
+    const int j = blockIdx.y;
     if (iu >= p.nu || iv >= p.nv) return;
     const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
     if (mask && mask[oidx] != 1.0f) return;
@@ -303,8 +308,8 @@ emap_kernel(FpParams p, const float* __restrict__ angles, const float* __restric
             const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
             const float* __restrict__ pxs, float* __restrict__ mask) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int j = blockIdx.z;
+    const int iv = blockIdx.z * blockDim.y + threadIdx.y;
+    const int j = blockIdx.y;
     if (iu >= p.nu || iv >= p.nv) return;
     const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
     float m = 1.0f;
@@ -334,8 +339,8 @@ fp_count_kernel(FpParams p, const float* __restrict__ angles, const float* __res
                 const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
                 const float* __restrict__ pxs, const float* __restrict__ mask, unsigned long long* __restrict__ count) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int j = blockIdx.z;
+    const int iv = blockIdx.z * blockDim.y + threadIdx.y;
+    const int j = blockIdx.y;
     unsigned long long c = 0;
     Ray r;
     if (iu < p.nu && iv < p.nv && !(mask && mask[((int64_t)iv * p.views + j) * p.nu + iu] != 1.0f) &&
@@ -395,8 +400,8 @@ ellipsoid_kernel(FpParams p, const float* __restrict__ angles, const float* __re
                  const float* __restrict__ v_arr, const float* __restrict__ ell, int n_ell,
                  float* __restrict__ sgm) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int j = blockIdx.z;
+    const int iv = blockIdx.z * blockDim.y + threadIdx.y;
+    const int j = blockIdx.y;
     if (iu >= p.nu || iv >= p.nv) return;
     float sb, cb;
     sincosf(angles[j], &sb, &cb);
@@ -489,7 +494,7 @@ int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float
         transpose_xy_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, vt);
         MCT_TRY(launched("transpose_xy_kernel"));
     }
-    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
     if (p.cone)
         fp_kernel<true><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol, vt, mask, sgm);
     else
@@ -503,7 +508,7 @@ int mct_fp_adjoint(const mct_geom* g, const mct_tables* t, const float* sgm, con
     MCT_TRY(make_params(g, p, "mct_fp_adjoint"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp_adjoint: NULL buffer");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp_adjoint: projection-matrix tables missing");
-    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
     fp_adjoint_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
                                                              sgm, mask, vol);
     return launched("fp_adjoint_kernel");
@@ -519,7 +524,7 @@ int mct_fp_count_samples(const mct_geom* g, const mct_tables* t, const float* ma
         set_error("mct_fp_count_samples: %s", cudaGetErrorString(e));
         return MCT_E_CUDA;
     }
-    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
     fp_count_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, mask,
                                                            (unsigned long long*)count);
     return launched("fp_count_kernel");
@@ -530,7 +535,7 @@ int mct_effective_map(const mct_geom* g, const mct_tables* t, float* mask, void*
     MCT_TRY(make_params(g, p, "mct_effective_map"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && mask, "mct_effective_map: NULL buffer");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_effective_map: projection-matrix tables missing");
-    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
     emap_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, mask);
     return launched("emap_kernel");
 }
@@ -552,7 +557,7 @@ int mct_project_ellipsoids(const mct_geom* g, const mct_tables* t, const float* 
     FpParams p;
     MCT_TRY(make_params(g, p, "mct_project_ellipsoids"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && ell && sgm && n_ell >= 0, "mct_project_ellipsoids: bad arguments");
-    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->nv + 7) / 8, g->views);
+    dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
     ellipsoid_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, ell, n_ell, sgm);
     return launched("ellipsoid_kernel");
 }

@@ -25,7 +25,10 @@ STORAGE = {"f32": MCT_F32, "float32": MCT_F32, "bf16": MCT_BF16, "bfloat16": MCT
 def _device(device=None):
     if not torch.cuda.is_available():
         raise RuntimeError("a CUDA device is required (this package has no CPU fallback)")
-    return torch.device(device or "cuda")
+    dev = torch.device(device or "cuda")
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    return dev
 
 
 class FdkPipeline:
@@ -33,7 +36,7 @@ class FdkPipeline:
     device buffers.  `storage` selects the backprojection operand precision:
     'f32' (plain) or 'bf16' (mixed precision storage)."""
 
-    def __init__(self, obj, device=None, storage="f32"):
+    def __init__(self, obj, device=None, storage="f32", filter_impl="simt"):
         dev = _device(device)
         self.obj = obj
         self.dg = fbp_geometry(obj, dev)
@@ -42,6 +45,12 @@ class FdkPipeline:
         self.kernel_none = obj.kernel_name == "None"
         f32 = dict(dtype=torch.float32, device=dev)
         self.taps = None if self.kernel_none else torch.tensor(recon_taps(obj), **f32)
+        if filter_impl not in ("simt", "tc"):
+            raise ValueError("filter_impl must be 'simt' (float32 FMA) or 'tc' (tensor-core split bf16)")
+        self.filter_impl = filter_impl
+        self.tc = None
+        if filter_impl == "tc" and not self.kernel_none:
+            self.tc = ops.TcFilter(self.dg, self.taps)
         self.gauss_v = None
         if obj.apply_gauss_vertical:
             self.gauss_v = torch.tensor(gaussian_taps(obj.det_elem_count_vertical_actual, obj.det_elem_height,
@@ -65,7 +74,15 @@ class FdkPipeline:
         if self.kernel_none:
             self.filtered.copy_(w.permute(1, 0, 2))
             return self.filtered
+        if self.tc is not None:
+            return self.tc(w, out=self.filtered)
         return ops.filter_rows(self.dg, w, self.taps, out=self.filtered)
+
+    def set_taps(self, taps):
+        """Replace the filter taps (float64/float32 array of 2*nu-1 values)."""
+        self.taps.copy_(torch.as_tensor(taps, dtype=torch.float32))
+        if self.tc is not None:
+            self.tc = ops.TcFilter(self.dg, self.taps)
 
     def backproject(self, filtered, out=None):
         packed = ops.pack(self.dg, filtered, self.dtype, out=self.packed)

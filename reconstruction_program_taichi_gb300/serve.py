@@ -1,0 +1,281 @@
+"""Reconstruction serving loop on one GPU: continuous admission, same-geometry
+batching, captured CUDA graphs, p50/p99 latency.
+
+No counterpart in the reference (it reconstructs one config at a time).
+
+Model
+  * A request is an FBP/FDK reconstruction or an N-iteration CGLS solve of one
+    sinogram for one geometry (a parsed config).
+  * Requests of the same geometry and kind share a *slot class*.  A slot owns
+    device buffers for up to `batch` requests, a CUDA stream, and a CUDA graph of
+    the whole batch captured once (weight -> filter -> pack -> backproject for each
+    sinogram, or the full CGLS loop), so a batch executes as one graph launch.
+  * Admission is continuous: a scheduler thread takes pending requests in arrival
+    order, groups those whose slot class matches (up to `batch`), and starts them on
+    a free slot; new slots are created while the HBM budget allows, and a slot is
+    reused as soon as its previous batch finishes.  Batches on different slots run
+    concurrently on their own streams.
+  * Results do not depend on the mix: every kernel is deterministic and a slot's
+    graph always runs the same kernels on the same buffer layout.
+"""
+import queue
+import threading
+import time
+from concurrent.futures import Future
+
+import numpy as np
+import torch
+
+from . import ops
+from .fbp import FdkPipeline
+
+_SENTINEL = object()
+
+
+def _geom_key(obj, kind, extra=()):
+    g = (obj.det_elem_count_horizontal, obj.det_elem_count_vertical_actual, obj.view_num, obj.img_dim,
+         obj.img_dim_z, float(obj.det_elem_width), float(obj.det_elem_height), float(obj.img_pix_size),
+         float(obj.img_voxel_height), float(obj.source_isocenter_dis), float(obj.source_det_dis),
+         float(obj.total_scan_angle), float(obj.img_rot), bool(obj.cone_beam), bool(obj.curved_dect),
+         str(obj.kernel_name), float(obj.kernel_param), float(obj.det_offset_horizontal),
+         float(getattr(obj, "det_offset_vertical", 0.0)), float(obj.img_center_x), float(obj.img_center_y),
+         float(obj.img_center_z), int(obj.recon_view_mode))
+    return (kind,) + g + tuple(extra)
+
+
+class _Request:
+    __slots__ = ("kind", "obj", "sgm", "x0", "n_iter", "storage", "key", "future", "t_arrive", "t_start",
+                 "t_done", "units")
+
+    def __init__(self, kind, obj, sgm, x0=None, n_iter=0, storage="f32"):
+        self.kind, self.obj, self.sgm, self.x0, self.n_iter, self.storage = kind, obj, sgm, x0, n_iter, storage
+        extra = (storage, n_iter) if kind == "cgls" else (storage,)
+        self.key = _geom_key(obj, kind, extra)
+        self.future = Future()
+        self.t_arrive = time.perf_counter()
+        self.t_start = self.t_done = None
+        nvox = obj.img_dim * obj.img_dim * obj.img_dim_z
+        self.units = nvox * obj.view_num * (1 if kind == "fbp" else 2 * (n_iter + 1))
+
+
+class _FbpSlot:
+    """Static buffers and one captured graph for `batch` FBP reconstructions."""
+
+    def __init__(self, obj, batch, storage, device, use_graph):
+        self.device = device
+        self.stream = torch.cuda.Stream(device=device)
+        self.batch = batch
+        with torch.cuda.stream(self.stream):
+            self.pipes = [FdkPipeline(obj, device=device, storage=storage) for _ in range(batch)]
+            shape = self.pipes[0].dg.sgm_shape
+            self.inp = [torch.zeros(shape, dtype=torch.float32, device=device) for _ in range(batch)]
+            self.out = [torch.zeros(self.pipes[0].dg.vol_shape, dtype=torch.float32, device=device)
+                        for _ in range(batch)]
+        self.host_out = [torch.empty(self.pipes[0].dg.vol_shape, dtype=torch.float32, pin_memory=True)
+                         for _ in range(batch)]
+        self.graph = None
+        self.nbytes = sum(p.weighted.numel() * 4 + p.filtered.numel() * 4 + p.packed.numel() + p.vol.numel() * 4
+                          for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
+        if use_graph:
+            self._capture()
+
+    def _body(self):
+        for p, i, o in zip(self.pipes, self.inp, self.out):
+            p.run(i, out=o)
+
+    def _capture(self):
+        with torch.cuda.stream(self.stream):
+            self._body()  # warm (first-call set-up outside the capture)
+        self.stream.synchronize()
+        g = torch.cuda.CUDAGraph()
+        # thread-local capture: other slots keep running on their own threads/streams
+        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+            self._body()
+        self.graph = g
+
+    def run(self, reqs):
+        with torch.cuda.stream(self.stream):
+            for i, r in enumerate(reqs):
+                self.inp[i].copy_(torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)), non_blocking=False)
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._body()
+            for i in range(len(reqs)):
+                self.host_out[i].copy_(self.out[i], non_blocking=True)
+        self.stream.synchronize()
+        return [self.host_out[i].numpy().copy() for i in range(len(reqs))]
+
+
+class _CglsSlot:
+    """CGLS (reference operator pair, lambda*D^T D with unit weights) for one request."""
+
+    def __init__(self, obj, n_iter, device):
+        from .ir import IrSystem
+        self.stream = torch.cuda.Stream(device=device)
+        self.batch = 1
+        with torch.cuda.stream(self.stream):
+            self.sys = IrSystem(obj, device)
+        self.obj = obj
+        self.n_iter = n_iter
+        nvol = obj.img_dim * obj.img_dim * obj.img_dim_z
+        self.nbytes = 8 * nvol * 4 + 3 * self.sys.fp_buf.numel() * 4
+
+    def run(self, reqs):
+        r = reqs[0]
+        obj = self.obj
+        with torch.cuda.stream(self.stream):
+            sgm = torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)).to(self.sys.device)
+            x0 = torch.from_numpy(np.ascontiguousarray(r.x0, dtype=np.float32)).to(self.sys.device)
+            self.sys.bpb = self.sys.bp_b(sgm)
+            wr = torch.ones_like(x0)
+            lr = obj.coef_lambda * obj.pixel_count_ratio
+            x = self.sys.cgls(x0, [], [(lr, wr)], self.n_iter)
+            out = x.cpu().numpy()
+        return [out]
+
+
+class ReconServer:
+    """Continuous-batching reconstruction server on one GPU (see module docstring)."""
+
+    def __init__(self, device=None, hbm_budget_gb=150.0, batch=4, max_slots_per_class=4, use_graphs=True):
+        if not torch.cuda.is_available():
+            raise RuntimeError("a CUDA device is required")
+        self.device = torch.device(device or "cuda")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        self.budget = int(hbm_budget_gb * 1e9)
+        self.used = 0
+        self.batch = batch
+        self.max_slots = max_slots_per_class
+        self.use_graphs = use_graphs
+        self.pending = []
+        self.cv = threading.Condition()
+        self.free_slots = {}    # key -> [slot]
+        self.all_slots = {}     # key -> count
+        self.busy = 0
+        self.done = []
+        self.closed = False
+        self.errors = []
+        self._workers = []
+        self._thread = threading.Thread(target=self._schedule, daemon=True)
+        self._thread.start()
+
+    # ------------------------------------------------------------ API
+    def submit_fbp(self, obj, sgm, storage="f32"):
+        """FBP/FDK of a host sinogram [rows, views, cols] for the parsed config obj."""
+        return self._submit(_Request("fbp", obj, sgm, storage=storage))
+
+    def submit_cgls(self, obj, sgm, x0, n_iter):
+        """n_iter CGLS iterations (Tikhonov-TV with unit weights) from x0."""
+        return self._submit(_Request("cgls", obj, sgm, x0=x0, n_iter=n_iter))
+
+    def close(self, wait=True):
+        with self.cv:
+            self.closed = True
+            self.cv.notify_all()
+        if wait:
+            self._thread.join()
+            for t in self._workers:
+                t.join()
+
+    def stats(self):
+        lat = np.array([(r.t_done - r.t_arrive) * 1e3 for r in self.done]) if self.done else np.zeros(1)
+        t0 = min(r.t_arrive for r in self.done) if self.done else 0.0
+        t1 = max(r.t_done for r in self.done) if self.done else 1.0
+        units = sum(r.units for r in self.done)
+        return {"requests": len(self.done), "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "gups": units / max(t1 - t0, 1e-9) / 1e9, "slots": dict((str(k[0]), v) for k, v in
+                                                                      self.all_slots.items()),
+                "hbm_used_gb": self.used / 1e9}
+
+    # ------------------------------------------------------------ internals
+    def _submit(self, req):
+        with self.cv:
+            if self.closed:
+                raise RuntimeError("server is closed")
+            self.pending.append(req)
+            self.cv.notify_all()
+        return req.future
+
+    def _make_slot(self, req):
+        torch.cuda.set_device(self.device)
+        if req.kind == "fbp":
+            return _FbpSlot(req.obj, self.batch, req.storage, self.device, self.use_graphs)
+        return _CglsSlot(req.obj, req.n_iter, self.device)
+
+    def _estimate(self, req):
+        o = req.obj
+        nvol = o.img_dim * o.img_dim * o.img_dim_z * 4
+        nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
+        if req.kind == "fbp":
+            return self.batch * (nsgm * 7 + 2 * nvol)
+        return 8 * nvol + 3 * nsgm
+
+    def _schedule(self):
+        while True:
+            with self.cv:
+                while not self.closed and not self.pending:
+                    self.cv.wait()
+                if self.closed and not self.pending:
+                    break
+                started = self._try_start()
+                if not started:
+                    self.cv.wait(timeout=0.05)
+
+    def _try_start(self):
+        """Start the oldest pending request's class if a slot is free or can be
+        created within the budget; returns True if something started."""
+        for i, head in enumerate(self.pending):
+            key = head.key
+            free = self.free_slots.setdefault(key, [])
+            slot = free.pop() if free else None
+            if slot is None:
+                if self.all_slots.get(key, 0) >= self.max_slots:
+                    continue
+                need = self._estimate(head)
+                if self.used + need > self.budget:
+                    if self.busy == 0 and not any(self.free_slots.values()):
+                        head.future.set_exception(MemoryError("request exceeds the HBM budget"))
+                        self.pending.pop(i)
+                        return True
+                    continue
+                try:
+                    slot = self._make_slot(head)
+                except Exception as e:  # allocation or build failure: fail this request only
+                    head.future.set_exception(e)
+                    self.pending.pop(i)
+                    return True
+                self.used += slot.nbytes
+                self.all_slots[key] = self.all_slots.get(key, 0) + 1
+            group = [r for r in self.pending if r.key == key][:slot.batch]
+            for r in group:
+                self.pending.remove(r)
+                r.t_start = time.perf_counter()
+            self.busy += 1
+            t = threading.Thread(target=self._run, args=(slot, key, group), daemon=True)
+            self._workers.append(t)
+            t.start()
+            return True
+        return False
+
+    def _run(self, slot, key, group):
+        try:
+            torch.cuda.set_device(self.device)
+            outs = slot.run(group)
+            now = time.perf_counter()
+            for r, o in zip(group, outs):
+                r.t_done = now
+                r.future.set_result(o)
+        except Exception as e:  # a failed batch fails its own requests only
+            self.errors.append(e)
+            for r in group:
+                if not r.future.done():
+                    r.future.set_exception(e)
+        finally:
+            with self.cv:
+                self.done.extend(r for r in group if r.t_done is not None)
+                self.busy -= 1
+                self.free_slots.setdefault(key, []).append(slot)
+                self.cv.notify_all()

@@ -1,0 +1,60 @@
+"""Serving loop: results are the same alone and in a concurrent mix; batching and
+graphs are used; requests beyond the HBM budget are refused."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import _cone_obj
+
+pytestmark = pytest.mark.gpu
+
+
+def _cgls_obj(**kw):
+    from reconstruction_program_taichi_gb300 import config
+    o = _cone_obj(**kw)
+    config.parse_ir(o, {"Lambda": 1e-3})
+    return o
+
+
+def test_same_result_alone_and_in_mix(cuda):
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(21)
+    objs = [_cone_obj(n=40, nz=16, nu=72, nv=24, views=60), _cone_obj(n=32, nz=8, nu=64, nv=16, views=45)]
+    cg = _cgls_obj(n=24, nz=8, nu=48, nv=12, views=30, DetectorElementHeight=1.0)
+    reqs = []
+    for i in range(10):
+        o = objs[i % 2]
+        reqs.append(("fbp", o, rng.uniform(0, 1, (o.det_elem_count_vertical, o.view_num,
+                                                 o.det_elem_count_horizontal)).astype(np.float32)))
+    sgm_cg = rng.uniform(0, 0.5, (12, 30, 48)).astype(np.float32)
+    x0 = np.zeros((8, 24, 24), np.float32)
+
+    alone = []
+    srv = ReconServer(batch=1, max_slots_per_class=1)
+    for kind, o, s in reqs:
+        alone.append(srv.submit_fbp(o, s).result(timeout=120))
+    cg_alone = srv.submit_cgls(cg, sgm_cg, x0, 3).result(timeout=120)
+    srv.close()
+
+    srv = ReconServer(batch=4, max_slots_per_class=2)
+    futs = [srv.submit_fbp(o, s) for kind, o, s in reqs[:5]]
+    fut_cg = srv.submit_cgls(cg, sgm_cg, x0, 3)
+    futs += [srv.submit_fbp(o, s) for kind, o, s in reqs[5:]]
+    mixed = [f.result(timeout=120) for f in futs]
+    cg_mixed = fut_cg.result(timeout=120)
+    st = srv.stats()
+    srv.close()
+    for a, b in zip(alone, mixed):
+        assert np.array_equal(a, b)
+    # CGLS uses float64 device reductions with a fixed order: identical too
+    assert np.allclose(cg_alone, cg_mixed, rtol=1e-6, atol=1e-7)
+    assert st["requests"] == 11 and st["p99_ms"] >= st["p50_ms"] > 0
+
+
+def test_request_beyond_budget_is_refused(cuda):
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    o = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60)
+    srv = ReconServer(hbm_budget_gb=0.001, batch=1)
+    f = srv.submit_fbp(o, np.zeros((24, 60, 72), np.float32))
+    with pytest.raises(MemoryError):
+        f.result(timeout=60)
+    srv.close()
