@@ -133,6 +133,12 @@ size_t mct_packed_size(const mct_geom* g, int32_t dtype);
  * the pair {F[r][c], F[r][c+1]}.  dtype MCT_F32 or MCT_BF16. */
 int mct_pack(const mct_geom* g, const float* filtered, void* packed, int32_t dtype, void* stream);
 
+/* mct_pack for a source with any (row, view) element strides: element (view j, row r,
+ * col c) is src[r*row_stride + j*view_stride + c] (a [nv][views][nu] sinogram has
+ * row_stride = views*nu, view_stride = nu).  The packed layout is the same. */
+int mct_pack_strided(const mct_geom* g, const float* src, int64_t row_stride, int64_t view_stride, void* packed,
+                     int32_t dtype, void* stream);
+
 /* Pixel-driven FDK / fan-beam backprojection of a packed filtered sinogram into
  * vol [nz][nx][nx] (overwritten).  Replaces Mgfbp.BackProjectionPixelDriven
  * run_mgfbp.py:1062-1187, including its rule that a voxel projecting outside the
@@ -192,6 +198,11 @@ int mct_bin_noise(const mct_geom* g, const float* in, int32_t bin, float photons
  * SetTruncatedRegionToZero :477-481. */
 int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sgm, float* vol,
                          void* stream);
+
+/* The same operator reading the sinogram as packed stencils (mct_pack_strided of the
+ * [nv][views][nu] sinogram, dtype MCT_F32 or MCT_BF16): one gather per voxel x view. */
+int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
+                                float* vol, void* stream);
 
 /* TV reweighting WR = 1/sqrt(|D x|^2 + beta) (forward differences, zero at the far
  * edge; z differences only when nz > 2).  Replaces Mgfbp_ir.GenerateWR

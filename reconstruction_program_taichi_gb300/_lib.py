@@ -71,6 +71,8 @@ SIGNATURES = {
     "mct_filter_tc_status": (ctypes.c_int, [_G, _P, _P]),
     "mct_packed_size": (ctypes.c_size_t, [_G, _i32]),
     "mct_pack": (ctypes.c_int, [_G, _P, _P, _i32, _P]),
+    "mct_pack_strided": (ctypes.c_int, [_G, _P, _i64, _i64, _P, _i32, _P]),
+    "mct_bp_ref_unmatched_packed": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
     "mct_fdk_bp": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
     "mct_fp_workspace_size": (ctypes.c_size_t, [_G]),
     "mct_fp": (ctypes.c_int, [_G, _T, _P, _P, _P, _P, _P]),

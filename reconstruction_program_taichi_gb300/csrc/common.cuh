@@ -59,4 +59,44 @@ __device__ __forceinline__ float bf16_to_f32(__nv_bfloat16 h) { return __bfloat1
 template <typename T>
 __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
 
+// Loaders of the packed backprojection operand (see mct_pack): a 2x2 bilinear
+// stencil {r c, r c+1, r+1 c, r+1 c+1} as float4 or 4 x bf16 (uint2), and a column
+// pair {c, c+1} as float2 or 2 x bf16 (uint32).
+template <typename QT>
+struct Quad;
+template <>
+struct Quad<float4> {
+    static __device__ __forceinline__ void load(const float4* p, float& a, float& b, float& c, float& d) {
+        float4 q = __ldg(p);
+        a = q.x; b = q.y; c = q.z; d = q.w;
+    }
+};
+template <>
+struct Quad<uint2> {
+    static __device__ __forceinline__ void load(const uint2* p, float& a, float& b, float& c, float& d) {
+        uint2 q = __ldg(p);
+        a = __uint_as_float(q.x << 16);
+        b = __uint_as_float(q.x & 0xffff0000u);
+        c = __uint_as_float(q.y << 16);
+        d = __uint_as_float(q.y & 0xffff0000u);
+    }
+};
+template <typename PT>
+struct Pair;
+template <>
+struct Pair<float2> {
+    static __device__ __forceinline__ void load(const float2* p, float& a, float& b) {
+        float2 q = __ldg(p);
+        a = q.x; b = q.y;
+    }
+};
+template <>
+struct Pair<uint32_t> {
+    static __device__ __forceinline__ void load(const uint32_t* p, float& a, float& b) {
+        uint32_t q = __ldg(p);
+        a = __uint_as_float(q << 16);
+        b = __uint_as_float(q & 0xffff0000u);
+    }
+};
+
 }  // namespace mct

@@ -33,43 +33,6 @@ struct BpParams {
     float o_x, o_y, o_z;     // P
 };
 
-template <typename QT>
-struct Quad;
-template <>
-struct Quad<float4> {
-    static __device__ __forceinline__ void load(const float4* p, float& a, float& b, float& c, float& d) {
-        float4 q = __ldg(p);
-        a = q.x; b = q.y; c = q.z; d = q.w;
-    }
-};
-template <>
-struct Quad<uint2> {
-    static __device__ __forceinline__ void load(const uint2* p, float& a, float& b, float& c, float& d) {
-        uint2 q = __ldg(p);
-        a = __uint_as_float(q.x << 16);
-        b = __uint_as_float(q.x & 0xffff0000u);
-        c = __uint_as_float(q.y << 16);
-        d = __uint_as_float(q.y & 0xffff0000u);
-    }
-};
-template <typename PT>
-struct Pair;
-template <>
-struct Pair<float2> {
-    static __device__ __forceinline__ void load(const float2* p, float& a, float& b) {
-        float2 q = __ldg(p);
-        a = q.x; b = q.y;
-    }
-};
-template <>
-struct Pair<uint32_t> {
-    static __device__ __forceinline__ void load(const uint32_t* p, float& a, float& b) {
-        uint32_t q = __ldg(p);
-        a = __uint_as_float(q << 16);
-        b = __uint_as_float(q & 0xffff0000u);
-    }
-};
-
 // MODE 0: axial, flat or curved detector, no projection matrix (u hoisted per column)
 // MODE 1: any view mode, no projection matrix (per-voxel u)
 // MODE 2: projection matrix geometry

@@ -191,9 +191,11 @@ __device__ __forceinline__ uint32_t make_pair<uint32_t>(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&p);
 }
 
-// cone: Q[j][r][c] = {F[j][r][c], F[j][r][c+1], F[j][r+1][c], F[j][r+1][c+1]}, r<nv-1, c<nu-1
+// Source element (view j, row r, column c) is F[r*rs + j*vs + c].
+// cone: Q[j][r][c] = {F(j,r,c), F(j,r,c+1), F(j,r+1,c), F(j,r+1,c+1)}, r<nv-1, c<nu-1
 template <typename QT>
-__global__ void pack_quad_kernel(int nu, int nv, int views, const float* __restrict__ F, QT* __restrict__ Q) {
+__global__ void pack_quad_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
+                                 QT* __restrict__ Q) {
     const int nq = nu - 1, rq = nv - 1;
     int64_t n = (int64_t)views * rq * nq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -201,20 +203,23 @@ __global__ void pack_quad_kernel(int nu, int nv, int views, const float* __restr
         int64_t jr = i / nq;
         int r = (int)(jr % rq);
         int j = (int)(jr / rq);
-        const float* f = F + ((int64_t)j * nv + r) * nu + c;
-        Q[i] = make_quad<QT>(f[0], f[1], f[nu], f[nu + 1]);
+        const float* f = F + r * rs + j * vs + c;
+        Q[i] = make_quad<QT>(f[0], f[1], f[rs], f[rs + 1]);
     }
 }
 
-// fan: P[j][r][c] = {F[j][r][c], F[j][r][c+1]}, c<nu-1
+// fan: P[j][r][c] = {F(j,r,c), F(j,r,c+1)}, c<nu-1
 template <typename PT>
-__global__ void pack_pair_kernel(int nu, int nv, int views, const float* __restrict__ F, PT* __restrict__ P) {
+__global__ void pack_pair_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
+                                 PT* __restrict__ P) {
     const int nq = nu - 1;
     int64_t n = (int64_t)views * nv * nq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int c = (int)(i % nq);
         int64_t jr = i / nq;
-        const float* f = F + jr * nu + c;
+        int r = (int)(jr % nv);
+        int j = (int)(jr / nv);
+        const float* f = F + r * rs + j * vs + c;
         P[i] = make_pair<PT>(f[0], f[1]);
     }
 }
@@ -284,26 +289,37 @@ size_t mct_packed_size(const mct_geom* g, int32_t dtype) {
     return (size_t)g->views * g->nv * (g->nu - 1) * esz;
 }
 
-int mct_pack(const mct_geom* g, const float* filtered, void* packed, int32_t dtype, void* stream) {
+int mct_pack_strided(const mct_geom* g, const float* src, int64_t row_stride, int64_t view_stride, void* packed,
+                     int32_t dtype, void* stream) {
     MCT_TRY(check_geom(g, "mct_pack"));
-    MCT_REQUIRE(filtered && packed, "mct_pack: NULL buffer");
+    MCT_REQUIRE(src && packed, "mct_pack: NULL buffer");
     MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_pack: dtype must be MCT_F32 or MCT_BF16");
     cudaStream_t s = as_stream(stream);
+    const int64_t rs = row_stride, vs = view_stride;
     if (g->flags & MCT_CONE) {
         MCT_REQUIRE(g->nv >= 2, "mct_pack: cone beam needs at least 2 detector rows");
         int64_t n = (int64_t)g->views * (g->nv - 1) * (g->nu - 1);
         if (dtype == MCT_F32)
-            pack_quad_kernel<float4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (float4*)packed);
+            pack_quad_kernel<float4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float4*)packed);
         else
-            pack_quad_kernel<uint2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (uint2*)packed);
+            pack_quad_kernel<uint2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (uint2*)packed);
     } else {
         int64_t n = (int64_t)g->views * g->nv * (g->nu - 1);
         if (dtype == MCT_F32)
-            pack_pair_kernel<float2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (float2*)packed);
+            pack_pair_kernel<float2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float2*)packed);
         else
-            pack_pair_kernel<uint32_t><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, filtered, (uint32_t*)packed);
+            pack_pair_kernel<uint32_t><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src,
+                                                                 (uint32_t*)packed);
     }
     return launched("pack_kernel");
+}
+
+int mct_pack(const mct_geom* g, const float* filtered, void* packed, int32_t dtype, void* stream) {
+    if (!g) {
+        set_error("mct_pack: geometry is NULL");
+        return MCT_E_INVALID;
+    }
+    return mct_pack_strided(g, filtered, g->nu, (int64_t)g->nv * g->nu, packed, dtype, stream);
 }
 
 }  // extern "C"

@@ -107,6 +107,41 @@ __device__ __forceinline__ bool setup_ray(const FpParams& p, int iu, int iv, int
     return r.ks <= r.ke;
 }
 
+// Steps [kis, kie] whose sample lies at least 1e-3 voxel inside the box on every
+// tested axis (and one more step in from both ends): for them the reference's inside
+// test certainly passes, far beyond float rounding, so it can be skipped.
+__device__ __forceinline__ void interior_range(const FpParams& p, const Ray& r, bool test_z, int& kis, int& kie) {
+    const float eps = 1e-3f;
+    float lo = -3.0e38f, hi = 3.0e38f;
+    bool empty = false;
+    auto axis = [&](float f0, float df, float n) {
+        const float a = eps, b = n - 1.0f - eps;
+        if (fabsf(df) < 1e-20f) {
+            if (!(f0 >= a && f0 <= b)) empty = true;
+            return;
+        }
+        const float t1 = (a - f0) / df, t2 = (b - f0) / df;
+        lo = fmaxf(lo, fminf(t1, t2));
+        hi = fminf(hi, fmaxf(t1, t2));
+    };
+    axis(r.fx0, r.dfx, (float)p.nx);
+    axis(r.fy0, r.dfy, (float)p.nx);
+    if (test_z) axis(r.fz0, r.dfz, (float)p.nz);
+    lo = fmaxf(lo, (float)r.ks - 2.0f);
+    hi = fminf(hi, (float)r.ke + 2.0f);
+    if (empty || !(lo <= hi)) {
+        kis = r.ke + 1;
+        kie = r.ke;
+        return;
+    }
+    kis = max(r.ks, (int)ceilf(lo) + 1);
+    kie = min(r.ke, (int)floorf(hi) - 1);
+    if (kis > kie) {
+        kis = r.ke + 1;
+        kie = r.ke;
+    }
+}
+
 // Direction (in object x, y) along which neighbouring detector columns spread.
 __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const float* __restrict__ angles,
                                                const float* __restrict__ pa) {
@@ -129,13 +164,19 @@ __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const f
 //
 // One thread per ray (u, v) of view j = blockIdx.y.  vol is [z][y][x]; vol_t, when
 // given, is the same volume as [z][x][y]: views whose detector columns spread along
-// y read vol_t so that the 32 rays of a warp touch consecutive addresses.
-template <bool CONE>
+// y read vol_t so that the 32 rays of a warp touch consecutive addresses.  With ZP
+// (cone beam, workspace given) the volume is read from z-paired copies zp_x
+// ([z][y][x]) and zp_y ([z][x][y]) whose element (z, y, x) is the float2
+// {V[z][y][x], V[z+1][y][x]}: a cell reload is four 8-byte gathers instead of eight
+// 4-byte ones, and each gather already holds the lower/upper-plane pair that the
+// packed f32x2 interpolation consumes.
+template <bool CONE, bool ZP>
 __global__ void __launch_bounds__(256)
 fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
           const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
           const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
-          const float* __restrict__ mask, float* __restrict__ sgm) {
+          const float2* __restrict__ zp_x, const float2* __restrict__ zp_y, const float* __restrict__ mask,
+          float* __restrict__ sgm) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.z * blockDim.y + threadIdx.y;
     const int j = blockIdx.y;
@@ -146,8 +187,9 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         return;
     }
     const int nx = p.nx;
-    const bool tr = vol_t != nullptr && spread_along_y(p, j, angles, pa);
+    const bool tr = (ZP || vol_t != nullptr) && spread_along_y(p, j, angles, pa);
     const float* __restrict__ V = tr ? vol_t : vol;
+    const float2* __restrict__ V2 = tr ? zp_y : zp_x;
     const int sx = tr ? nx : 1, sy = tr ? 1 : nx;
     const int plane = nx * nx;  // volumes below 2^31 voxels (checked on the host)
     Ray r;
@@ -155,27 +197,33 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
     if (setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) {
         const float xmax = (float)(nx - 1), zmax = (float)(p.nz - 1);
         // Consecutive samples are 0.2 voxel diagonals apart, so most fall in the same
-        // 2x2x2 cell as the previous one: the 8 corners stay in registers and are
-        // reloaded only when the cell changes.
+        // 2x2x2 cell as the previous one: the cell stays in registers (as corner values
+        // and x-differences, lower and upper z-plane packed side by side) and is
+        // reloaded only when the ray enters a new cell.
         int cell = -1;
-        float a00 = 0.f, a01 = 0.f, a10 = 0.f, a11 = 0.f, c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
-#pragma unroll 4
-        for (int k = r.ks; k <= r.ke; ++k) {
+        float2 e00 = make_float2(0.f, 0.f), e10 = e00, g00 = e00, g10 = e00;  // corners, x-differences
+        auto sample = [&](int k, bool check) {
             const float fk = (float)k;
             const float fx = fmaf(fk, r.dfx, r.fx0);
             const float fy = fmaf(fk, r.dfy, r.fy0);
             const float xf = floorf(fx), yf = floorf(fy);
-            bool ok = xf >= 0.0f && xf < xmax && yf >= 0.0f && yf < xmax;
-            const int xi = min(max((int)xf, 0), nx - 2);
-            const int yi = min(max((int)yf, 0), nx - 2);
+            bool ok = true;
+            int xi = (int)xf, yi = (int)yf, zi;
+            if (check) {
+                ok = xf >= 0.0f && xf < xmax && yf >= 0.0f && yf < xmax;
+                xi = min(max(xi, 0), nx - 2);
+                yi = min(max(yi, 0), nx - 2);
+            }
             const float xw = fx - xf, yw = fy - yf;
-            int zi;
             float zw = 0.0f;
             if (CONE) {
                 const float fz = fmaf(fk, r.dfz, r.fz0);
                 const float zf = floorf(fz);
-                ok = ok && zf >= 0.0f && zf < zmax;
-                zi = min(max((int)zf, 0), p.nz - 2);
+                zi = (int)zf;
+                if (check) {
+                    ok = ok && zf >= 0.0f && zf < zmax;
+                    zi = min(max(zi, 0), p.nz - 2);
+                }
                 zw = fz - zf;
             } else {
                 zi = iv;
@@ -183,26 +231,70 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
             const int off = zi * plane + yi * sy + xi * sx;
             if (off != cell) {
                 cell = off;
-                const float* b = V + off;
-                a00 = __ldg(b); a01 = __ldg(b + sx); a10 = __ldg(b + sy); a11 = __ldg(b + sx + sy);
-                if (CONE) {
-                    const float* c = b + plane;
-                    c00 = __ldg(c); c01 = __ldg(c + sx); c10 = __ldg(c + sy); c11 = __ldg(c + sx + sy);
+                if (ZP) {
+                    const float2* b2 = V2 + off;
+                    e00 = __ldg(b2);
+                    const float2 e01 = __ldg(b2 + sx);
+                    e10 = __ldg(b2 + sy);
+                    const float2 e11 = __ldg(b2 + sx + sy);
+                    g00 = __fadd2_rn(e01, make_float2(-e00.x, -e00.y));
+                    g10 = __fadd2_rn(e11, make_float2(-e10.x, -e10.y));
+                } else {
+                    const float* b = V + off;
+                    const float a00 = __ldg(b), a01 = __ldg(b + sx), a10 = __ldg(b + sy), a11 = __ldg(b + sx + sy);
+                    float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+                    if (CONE) {
+                        const float* c = b + plane;
+                        c00 = __ldg(c); c01 = __ldg(c + sx); c10 = __ldg(c + sy); c11 = __ldg(c + sx + sy);
+                    }
+                    e00 = make_float2(a00, c00);
+                    e10 = make_float2(a10, c10);
+                    g00 = __fadd2_rn(make_float2(a01, c01), make_float2(-a00, -c00));
+                    g10 = __fadd2_rn(make_float2(a11, c11), make_float2(-a10, -c10));
                 }
             }
-            const float l0 = fmaf(xw, a01 - a00, a00);
-            const float l1 = fmaf(xw, a11 - a10, a10);
-            float val = fmaf(yw, l1 - l0, l0);
-            if (CONE) {
-                const float m0 = fmaf(xw, c01 - c00, c00);
-                const float m1 = fmaf(xw, c11 - c10, c10);
-                const float hi = fmaf(yw, m1 - m0, m0);
-                val = fmaf(zw, hi - val, val);
-            }
-            acc += ok ? val : 0.0f;
-        }
+            // lower (.x) and upper (.y) z-plane bilinear values in packed f32x2 FMAs;
+            // per lane this is exactly fmaf(xw, a01 - a00, a00) etc.
+            const float2 xw2 = make_float2(xw, xw), yw2 = make_float2(yw, yw);
+            const float2 l0 = __ffma2_rn(xw2, g00, e00);
+            const float2 l1 = __ffma2_rn(xw2, g10, e10);
+            const float2 pl = __ffma2_rn(yw2, __fadd2_rn(l1, make_float2(-l0.x, -l0.y)), l0);
+            const float val = CONE ? fmaf(zw, pl.y - pl.x, pl.x) : pl.x;
+            if (check) acc += ok ? val : 0.0f;
+            else acc += val;
+        };
+        int kis, kie;
+        interior_range(p, r, CONE, kis, kie);
+        for (int k = r.ks; k < kis; ++k) sample(k, true);
+#pragma unroll 4
+        for (int k = kis; k <= kie; ++k) sample(k, false);
+        for (int k = max(kie + 1, kis); k <= r.ke; ++k) sample(k, true);
     }
     sgm[oidx] = acc * p.stepvd;
+}
+
+// Z-paired copies: zx[z][y][x] = zy[z][x][y] = {v[z][y][x], v[z+1][y][x]} (0 above
+// the top slice); 32x32 tiles, the transposed copy through shared memory.
+__global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, float2* __restrict__ zx,
+                             float2* __restrict__ zy) {
+    __shared__ float2 tile[32][33];
+    const int64_t plane = (int64_t)nx * nx;
+    const int z = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int y = y0 + i, x = x0 + threadIdx.x;
+        if (y < nx && x < nx) {
+            const int64_t o = z * plane + (int64_t)y * nx + x;
+            const float2 e = make_float2(v[o], z + 1 < nz ? v[o + plane] : 0.0f);
+            zx[o] = e;
+            tile[i][threadIdx.x] = e;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int x = x0 + i, y = y0 + threadIdx.x;
+        if (y < nx && x < nx) zy[z * plane + (int64_t)x * nx + y] = tile[threadIdx.x][i];
+    }
 }
 
 // vt[z][x][y] = v[z][y][x], 32x32 tiles through shared memory.
@@ -477,7 +569,9 @@ extern "C" {
 
 size_t mct_fp_workspace_size(const mct_geom* g) {
     if (!g || g->nx < 1 || g->nz < 1) return 0;
-    return (size_t)g->nz * g->nx * g->nx * sizeof(float);
+    const size_t n = (size_t)g->nz * g->nx * g->nx;
+    // cone beam: two z-paired copies (float2); fan beam: one transposed copy
+    return (g->flags & MCT_CONE) ? 2 * n * sizeof(float2) : n * sizeof(float);
 }
 
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* workspace,
@@ -486,19 +580,31 @@ int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float
     MCT_TRY(make_params(g, p, "mct_fp"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp: NULL buffer");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp: projection-matrix tables missing");
+    MCT_REQUIRE(workspace != (void*)vol, "mct_fp: workspace aliases the volume");
+    MCT_REQUIRE(((uintptr_t)workspace & 15) == 0, "mct_fp: workspace must be 16-byte aligned");
     cudaStream_t s = as_stream(stream);
-    float* vt = static_cast<float*>(workspace);
-    if (vt) {
-        MCT_REQUIRE(vt != vol, "mct_fp: workspace aliases the volume");
-        dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
-        transpose_xy_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, vt);
-        MCT_TRY(launched("transpose_xy_kernel"));
-    }
+    dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
     dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
-    if (p.cone)
-        fp_kernel<true><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol, vt, mask, sgm);
-    else
-        fp_kernel<false><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol, vt, mask, sgm);
+    if (p.cone && workspace) {
+        float2* zx = static_cast<float2*>(workspace);
+        float2* zy = zx + (size_t)g->nz * g->nx * g->nx;
+        zpair_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
+        MCT_TRY(launched("zpair_kernel"));
+        fp_kernel<true, true><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
+                                                     nullptr, zx, zy, mask, sgm);
+    } else {
+        float* vt = static_cast<float*>(workspace);
+        if (vt) {
+            transpose_xy_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, vt);
+            MCT_TRY(launched("transpose_xy_kernel"));
+        }
+        if (p.cone)
+            fp_kernel<true, false><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
+                                                          vt, nullptr, nullptr, mask, sgm);
+        else
+            fp_kernel<false, false><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
+                                                           vt, nullptr, nullptr, mask, sgm);
+    }
     return launched("fp_kernel");
 }
 

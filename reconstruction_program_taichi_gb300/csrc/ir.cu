@@ -25,9 +25,14 @@ struct UbParams {
 };
 
 // All views of the per-view backprojector, accumulated in registers in view order.
+// SRC 0 reads the plain sinogram [nv][views][nu] (4 gathers per update); SRC 1 / 2
+// read the packed stencils of mct_pack_strided (one 16-byte float32 or 8-byte bf16
+// gather per update).
+template <int SRC, typename QT, typename PT>
 __global__ void __launch_bounds__(UB_TX* UB_TY)
 bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
-                    const float* __restrict__ sgm, float* __restrict__ vol) {
+                    const float* __restrict__ sgm, const void* __restrict__ packed, float* __restrict__ vol) {
+    const int nq = p.nu - 1, rq = p.cone ? p.nv - 1 : p.nv;
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, unused}
     const int ix = blockIdx.x * UB_TX + threadIdx.x;
     const int iy = blockIdx.y * UB_TY + threadIdx.y;
@@ -85,14 +90,26 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
                     const float vf = floorf(vi);
                     if (!(vf >= 0.0f && vf + 1.0f <= (float)(p.nv - 1))) continue;
                     const float rv = vi - vf;
-                    const float* s0 = sgm + (int64_t)(int)vf * rowstride + (int64_t)j * p.nu + uc;
-                    const float a = __ldg(s0), b = __ldg(s0 + 1), c = __ldg(s0 + rowstride), d = __ldg(s0 + rowstride + 1);
+                    float a, b, c, d;
+                    if (SRC == 0) {
+                        const float* s0 = sgm + (int64_t)(int)vf * rowstride + (int64_t)j * p.nu + uc;
+                        a = __ldg(s0); b = __ldg(s0 + 1); c = __ldg(s0 + rowstride); d = __ldg(s0 + rowstride + 1);
+                    } else {
+                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * rq + (int)vf) * nq + uc, a, b,
+                                       c, d);
+                    }
                     const float p0 = a * (1 - ru) + b * ru;
                     const float p1 = c * (1 - ru) + d * ru;
                     acc[k] += ((1 - rv) * p0 + rv * p1) * w;
                 } else {
-                    const float* s0 = sgm + (int64_t)(zb + k) * rowstride + (int64_t)j * p.nu + uc;
-                    acc[k] += ((1 - ru) * __ldg(s0) + ru * __ldg(s0 + 1)) * w;
+                    float a, b;
+                    if (SRC == 0) {
+                        const float* s0 = sgm + (int64_t)(zb + k) * rowstride + (int64_t)j * p.nu + uc;
+                        a = __ldg(s0); b = __ldg(s0 + 1);
+                    } else {
+                        Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * rq + zb + k) * nq + uc, a, b);
+                    }
+                    acc[k] += ((1 - ru) * a + ru * b) * w;
                 }
             }
         }
@@ -247,15 +264,43 @@ using namespace mct;
 
 extern "C" {
 
+static int unmatched_params(const mct_geom* g, UbParams& p);
+
 int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sgm, float* vol, void* stream) {
-    MCT_TRY(check_geom(g, "mct_bp_ref_unmatched"));
+    UbParams p{};
+    MCT_TRY(unmatched_params(g, p));
     MCT_REQUIRE(t && t->angles && sgm && vol, "mct_bp_ref_unmatched: NULL buffer");
+    dim3 block(UB_TX, UB_TY);
+    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
+    bp_unmatched_kernel<0, float4, float2><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz, sgm,
+                                                                                  nullptr, vol);
+    return launched("bp_unmatched_kernel");
+}
+
+int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype, float* vol,
+                                void* stream) {
+    UbParams p{};
+    MCT_TRY(unmatched_params(g, p));
+    MCT_REQUIRE(t && t->angles && packed && vol, "mct_bp_ref_unmatched_packed: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_bp_ref_unmatched_packed: dtype must be MCT_F32 or MCT_BF16");
+    dim3 block(UB_TX, UB_TY);
+    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
+    if (dtype == MCT_F32)
+        bp_unmatched_kernel<1, float4, float2><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz,
+                                                                                      nullptr, packed, vol);
+    else
+        bp_unmatched_kernel<2, uint2, uint32_t><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz,
+                                                                                       nullptr, packed, vol);
+    return launched("bp_unmatched_kernel");
+}
+
+static int unmatched_params(const mct_geom* g, UbParams& p) {
+    MCT_TRY(check_geom(g, "mct_bp_ref_unmatched"));
     MCT_REQUIRE(!(g->flags & MCT_PMATRIX), "mct_bp_ref_unmatched: projection-matrix geometry is not supported");
     const bool cone = (g->flags & MCT_CONE) != 0;
     MCT_REQUIRE(!cone || g->nv >= 2, "mct_bp_ref_unmatched: cone beam needs at least 2 rows");
     MCT_REQUIRE(cone || g->nz <= g->nv, "mct_bp_ref_unmatched: fan beam needs nz <= detector rows");
     MCT_REQUIRE(g->u_step != 0.0f, "mct_bp_ref_unmatched: zero detector spacing");
-    UbParams p{};
     p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views;
     p.cone = cone; p.curved = (g->flags & MCT_CURVED) != 0;
     p.sid = g->sid; p.sdd = g->sdd; p.img_rot = g->img_rot; p.px = g->px;
@@ -288,10 +333,7 @@ int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sg
     p.ex_x = rx(ax); p.ex_y = ry(ax); p.ey_x = rx(ay); p.ey_y = ry(ay); p.ez_x = rx(az); p.ez_y = ry(az);
     p.o_x = rx(a0); p.o_y = ry(a0);
     p.zx = (float)ax[2]; p.zy = (float)ay[2]; p.zz = (float)az[2]; p.z0 = (float)a0[2];
-    dim3 block(UB_TX, UB_TY);
-    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
-    bp_unmatched_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz, sgm, vol);
-    return launched("bp_unmatched_kernel");
+    return MCT_OK;
 }
 
 int mct_tv_weights(const mct_geom* g, const float* x, float beta, float* wr, void* stream) {

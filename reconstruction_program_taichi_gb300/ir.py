@@ -53,7 +53,11 @@ class IrSystem:
     def bp(self, sgm, out=None):
         if self.matched:
             return ops.fp_adjoint(self.dg, sgm, mask=self.mask, out=out)
-        return ops.bp_unmatched(self.dg, sgm, out=out)
+        # pack the sinogram into one-gather stencils, then backproject
+        if getattr(self, "_packed", None) is None:
+            self._packed = torch.empty(max(ops.packed_bytes(self.dg), 16), dtype=torch.uint8, device=self.device)
+        ops.pack_sinogram(self.dg, sgm, out=self._packed)
+        return ops.bp_unmatched_packed(self.dg, self._packed, out=out)
 
     def ptp(self, x, out=None):
         """P^T P x (run_mgfbp_iterative_recon_IRN_CGLS.py:288-316)."""

@@ -154,6 +154,27 @@ def pack(dg, filtered, dtype=MCT_F32, out=None):
     return out
 
 
+def pack_sinogram(dg, sgm, dtype=MCT_F32, out=None):
+    """Pack a [nv, views, nu] sinogram into the one-gather stencil layout."""
+    g = dg.geom
+    _check(sgm, "sgm", dg.sgm_shape)
+    nbytes = packed_bytes(dg, dtype)
+    if out is None:
+        out = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=sgm.device)
+    if out.numel() < nbytes:
+        raise ValueError("packed buffer too small")
+    _lib.call("mct_pack_strided", dg.g(), _ptr(sgm), g.views * g.nu, g.nu, _ptr(out), dtype, _stream())
+    return out
+
+
+def bp_unmatched_packed(dg, packed, dtype=MCT_F32, out=None):
+    if out is None:
+        out = torch.empty(dg.vol_shape, dtype=torch.float32, device=packed.device)
+    _check(out, "out", dg.vol_shape)
+    _lib.call("mct_bp_ref_unmatched_packed", dg.g(), dg.t(), _ptr(packed), dtype, _ptr(out), _stream())
+    return out
+
+
 def fdk_bp(dg, packed, dtype=MCT_F32, out=None):
     if out is None:
         out = torch.empty(dg.vol_shape, dtype=torch.float32, device=packed.device)

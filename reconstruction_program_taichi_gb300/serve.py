@@ -261,21 +261,25 @@ class ReconServer:
         return False
 
     def _run(self, slot, key, group):
+        outs, err = None, None
         try:
             torch.cuda.set_device(self.device)
             outs = slot.run(group)
             now = time.perf_counter()
-            for r, o in zip(group, outs):
-                r.t_done = now
-                r.future.set_result(o)
-        except Exception as e:  # a failed batch fails its own requests only
-            self.errors.append(e)
             for r in group:
-                if not r.future.done():
-                    r.future.set_exception(e)
-        finally:
-            with self.cv:
-                self.done.extend(r for r in group if r.t_done is not None)
-                self.busy -= 1
-                self.free_slots.setdefault(key, []).append(slot)
-                self.cv.notify_all()
+                r.t_done = now
+        except Exception as e:  # a failed batch fails its own requests only
+            err = e
+            self.errors.append(e)
+        # record completion and free the slot before any caller can observe the result
+        with self.cv:
+            if outs is not None:
+                self.done.extend(group)
+            self.busy -= 1
+            self.free_slots.setdefault(key, []).append(slot)
+            self.cv.notify_all()
+        for i, r in enumerate(group):
+            if outs is not None:
+                r.future.set_result(outs[i])
+            elif not r.future.done():
+                r.future.set_exception(err)

@@ -295,3 +295,19 @@ def test_fdk_with_tc_filter_vs_oracle(cuda):
                    cone_beam=True)
     keep = (vol != 0) & (ref != 0)
     assert rel_l2(vol[keep], ref[keep]) < 1e-4
+
+
+@pytest.mark.parametrize("cone", [True, False])
+def test_packed_unmatched_bp_is_identical(cone, cuda):
+    """The packed-stencil backprojector reads the same values in the same order."""
+    import torch
+    from reconstruction_program_taichi_gb300 import config, geometry, ops
+    kw = {} if cone else {"ConeBeam": False, "DetectorElementCountVertical": 6, "ImageDimensionZ": 6}
+    o = _cone_obj(n=40, nz=12, nu=64, nv=20, views=36, DetectorElementHeight=1.2, **kw)
+    config.parse_ir(o, {"Lambda": 1e-3})
+    dg = geometry.ir_geometry(o)
+    g = torch.Generator(device="cuda").manual_seed(31)
+    sgm = torch.rand(dg.sgm_shape, device="cuda", generator=g)
+    a = ops.bp_unmatched(dg, sgm)
+    b = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm))
+    assert torch.equal(a, b)
