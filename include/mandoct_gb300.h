@@ -148,19 +148,28 @@ int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* packed, int32
 
 /* ---------------------------------------------------------------- forward projection */
 
-/* Bytes of the optional forward-projection workspace (an x/y-transposed copy of
- * the volume). */
+/* Bytes of the optional forward-projection workspace (gather copies of the volume:
+ * cone beam, two z-paired float32 copies; fan beam, one x/y-transposed copy). */
 size_t mct_fp_workspace_size(const mct_geom* g);
 
 /* Ray-driven trilinear forward projection of vol [nz][nx][nx] for all views into
  * sgm [nv][views][nu] (overwritten).  Rays with mask != 1 (mask [nv][views][nu], or
- * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes, or NULL) receives
- * a transposed copy of vol that views whose detector columns run along y read
- * instead, for coalesced gathers; results are identical either way.  Replaces
+ * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes, 16-byte aligned, or
+ * NULL) receives gather copies of vol: for cone beam {V[z], V[z+1]} pairs in [z][y][x]
+ * and [z][x][y] order, for fan beam an x/y-transposed copy; views whose detector
+ * columns run along y read the transposed order, so a warp's gathers are coalesced.
+ * Results are identical with and without the workspace.  Replaces
  * Mgfpj_v3.ForwardProjectionBilinear run_mgfpj_v3.py:184-366 and
  * Mgfbp_ir.ForwardProjectionBilinear run_mgfbp_iterative_recon_IRN_CGLS.py:494-676. */
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
            void* workspace, void* stream);
+
+/* mct_fp with the z-paired gather copies stored as dtype: MCT_F32 is mct_fp; MCT_BF16
+ * (cone beam, workspace required) rounds the volume to bf16 in the copies, halving
+ * the bytes each trilinear gather moves; interpolation and sums stay float32.
+ * No counterpart in the reference (its projector is float32 only). */
+int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
+                   void* workspace, int32_t dtype, void* stream);
 
 /* Exact transpose of mct_fp: vol += P^T sgm (vol is accumulated, not cleared).
  * No counterpart in the reference (its CGLS pairs mct_fp with the unmatched

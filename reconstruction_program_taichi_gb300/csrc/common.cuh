@@ -59,44 +59,45 @@ __device__ __forceinline__ float bf16_to_f32(__nv_bfloat16 h) { return __bfloat1
 template <typename T>
 __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
 
-// Loaders of the packed backprojection operand (see mct_pack): a 2x2 bilinear
-// stencil {r c, r c+1, r+1 c, r+1 c+1} as float4 or 4 x bf16 (uint2), and a column
-// pair {c, c+1} as float2 or 2 x bf16 (uint32).
+// Loaders of the packed backprojection operand (see mct_pack).
+//
+// Cone beam: detector cell (r, c) with corners A = F[r][c], B = F[r][c+1],
+// C = F[r+1][c], D = F[r+1][c+1] is stored in bilinear coefficient form
+// {A, C-A, B-A, (D-C)-(B-A)} as float4 or 4 x bf16 (uint2) and returned as
+// lo = {A, C-A}, hi = {B-A, (D-C)-(B-A)}.  The bilinear value at fractions (ru, rv) is
+//     s = lo + ru*hi (one packed f32x2 FMA);  value = s.x + rv*s.y.
+// Fan beam: the column pair {A, B-A} as float2 or 2 x bf16 (uint32); value = A + ru*(B-A).
+// A bf16 word holds its first element in the low 16 bits.
+__device__ __forceinline__ float2 bf16x2_to_float2(uint32_t w) {
+    return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+}
 template <typename QT>
 struct Quad;
 template <>
 struct Quad<float4> {
-    static __device__ __forceinline__ void load(const float4* p, float& a, float& b, float& c, float& d) {
-        float4 q = __ldg(p);
-        a = q.x; b = q.y; c = q.z; d = q.w;
+    static __device__ __forceinline__ void load(const float4* p, float2& lo, float2& hi) {
+        const float4 q = __ldg(p);
+        lo = make_float2(q.x, q.y);
+        hi = make_float2(q.z, q.w);
     }
 };
 template <>
 struct Quad<uint2> {
-    static __device__ __forceinline__ void load(const uint2* p, float& a, float& b, float& c, float& d) {
-        uint2 q = __ldg(p);
-        a = __uint_as_float(q.x << 16);
-        b = __uint_as_float(q.x & 0xffff0000u);
-        c = __uint_as_float(q.y << 16);
-        d = __uint_as_float(q.y & 0xffff0000u);
+    static __device__ __forceinline__ void load(const uint2* p, float2& lo, float2& hi) {
+        const uint2 q = __ldg(p);
+        lo = bf16x2_to_float2(q.x);
+        hi = bf16x2_to_float2(q.y);
     }
 };
 template <typename PT>
 struct Pair;
 template <>
 struct Pair<float2> {
-    static __device__ __forceinline__ void load(const float2* p, float& a, float& b) {
-        float2 q = __ldg(p);
-        a = q.x; b = q.y;
-    }
+    static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
 };
 template <>
 struct Pair<uint32_t> {
-    static __device__ __forceinline__ void load(const uint32_t* p, float& a, float& b) {
-        uint32_t q = __ldg(p);
-        a = __uint_as_float(q << 16);
-        b = __uint_as_float(q & 0xffff0000u);
-    }
+    static __device__ __forceinline__ float2 load(const uint32_t* p) { return bf16x2_to_float2(__ldg(p)); }
 };
 
 }  // namespace mct

@@ -10,7 +10,11 @@
 //     magnification are evaluated once per (column, view) and v is an affine
 //     function of the slice index.
 // Voxels that project outside the detector in any view are written as 0, as in the
-// reference (the view loop "breaks" with the voxel set to 0).
+// reference (the view loop "breaks" with the voxel set to 0).  In the axial cone-beam
+// path an off-detector row index is redirected to the packed operand's NaN row, so the
+// voxel's sum becomes NaN and is written as 0 without any per-slice bookkeeping (a
+// voxel whose sum is NaN because the sinogram itself holds NaN is written as 0 too,
+// where the reference would return NaN).
 #include <cmath>
 
 #include "common.cuh"
@@ -19,6 +23,15 @@ namespace mct {
 namespace {
 
 constexpr int BP_TX = 32, BP_TY = 8, BP_ZC = 16, BP_VCHUNK = 1024;
+// Minimum resident blocks per SM, i.e. a register budget of 65536 / (256 * minb) per
+// thread.  The axial kernel needs enough registers to issue all BP_ZC stencil gathers
+// of a view before their arithmetic (that hides the gather latency): measured at
+// 512x512x256 / 1080 views, float32 stencils run fastest with 128 registers (2
+// blocks), bf16 stencils with 80 (3 blocks).  The general modes use 2.
+template <int MODE, typename QT>
+constexpr int bp_min_blocks() {
+    return MODE == 0 && sizeof(QT) == 8 ? 3 : 2;
+}
 
 struct BpParams {
     int nx, nz, nu, nv, views, cone, curved;
@@ -37,7 +50,7 @@ struct BpParams {
 // MODE 1: any view mode, no projection matrix (per-voxel u)
 // MODE 2: projection matrix geometry
 template <int MODE, bool CONE, typename QT, typename PT>
-__global__ void __launch_bounds__(BP_TX* BP_TY)
+__global__ void __launch_bounds__(BP_TX* BP_TY, bp_min_blocks<MODE, QT>())
 fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
               const void* __restrict__ packed, float* __restrict__ vol) {
     __shared__ float4 tab[BP_VCHUNK];  // {cos b, sin b, dbeta*div, unused}
@@ -46,8 +59,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     const int zb = blockIdx.z * BP_ZC;
     const int tid = threadIdx.y * BP_TX + threadIdx.x;
     const bool active = ix < p.nx && iy < p.nx;
-    const int nq = p.nu - 1;                // packed columns
-    const int rq = CONE ? p.nv - 1 : p.nv;  // packed rows
+    const int nq = p.nu - 1;  // packed columns; packed rows per view: nv (cone: row nv-1 is NaN)
 
     // voxel centres of the ZC slices of this column: c_k = c0 + k * dc
     const float c0x = p.o_x + ix * p.px_x + iy * p.py_x + zb * p.pz_x;
@@ -96,29 +108,28 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                 if (CONE) {
                     const float vA = (mag * c0z - p.v0) * p.kv;
                     const float vB = (mag * p.pz_z) * p.kv;
-                    const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * rq * nq + uc;
+                    const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq + uc;
+                    const float2 ru2 = make_float2(ru, ru);
+                    const unsigned nan_row = (unsigned)(p.nv - 1);
 #pragma unroll
                     for (int k = 0; k < BP_ZC; ++k) {
                         const float vi = fmaf((float)k, vB, vA);
                         const float vf = floorf(vi);
-                        int vr = (int)vf;
-                        if (vr < 0 || vr > p.nv - 2) dead |= 1u << k;
-                        vr = min(max(vr, 0), p.nv - 2);
+                        // rows outside [0, nv-2] (negative ones wrap around) read the NaN row
+                        const unsigned vr = min((unsigned)(int)vf, nan_row);
                         const float rv = vi - vf;
-                        float a, b, c2, d;
-                        Quad<QT>::load(base + (int64_t)vr * nq, a, b, c2, d);
-                        const float top = fmaf(ru, b - a, a);
-                        const float bot = fmaf(ru, d - c2, c2);
-                        acc[k] = fmaf(w, fmaf(rv, bot - top, top), acc[k]);
+                        float2 lo, hi;
+                        Quad<QT>::load(base + vr * (unsigned)nq, lo, hi);
+                        const float2 s2 = __ffma2_rn(ru2, hi, lo);
+                        acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
                     }
                 } else {
-                    const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * rq + zb) * nq + uc;
+                    const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
 #pragma unroll
                     for (int k = 0; k < BP_ZC; ++k) {
                         if (zb + k < p.nz) {
-                            float a, b;
-                            Pair<PT>::load(base + (int64_t)k * nq, a, b);
-                            acc[k] = fmaf(w, fmaf(ru, b - a, a), acc[k]);
+                            const float2 pr = Pair<PT>::load(base + (int64_t)k * nq);
+                            acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
                         }
                     }
                 }
@@ -165,15 +176,13 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                             continue;
                         }
                         const float rv = vi - vf;
-                        float a, b, c2, d;
-                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * rq + vr) * nq + uc, a, b, c2, d);
-                        const float top = fmaf(ru, b - a, a);
-                        const float bot = fmaf(ru, d - c2, c2);
-                        acc[k] = fmaf(w, fmaf(rv, bot - top, top), acc[k]);
+                        float2 lo, hi;
+                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * p.nv + vr) * nq + uc, lo, hi);
+                        const float2 s2 = __ffma2_rn(make_float2(ru, ru), hi, lo);
+                        acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
                     } else {
-                        float a, b;
-                        Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * rq + zb + k) * nq + uc, a, b);
-                        acc[k] = fmaf(w, fmaf(ru, b - a, a), acc[k]);
+                        const float2 pr = Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb + k) * nq + uc);
+                        acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
                     }
                 }
             }
@@ -184,7 +193,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     float* out = vol + (int64_t)zb * plane + (int64_t)iy * p.nx + ix;
 #pragma unroll
     for (int k = 0; k < BP_ZC; ++k) {
-        if (zb + k < p.nz) out[(int64_t)k * plane] = ((dead >> k) & 1u) ? 0.0f : acc[k];
+        if (zb + k < p.nz) out[(int64_t)k * plane] = (((dead >> k) & 1u) || acc[k] != acc[k]) ? 0.0f : acc[k];
     }
 }
 
@@ -213,6 +222,7 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     MCT_REQUIRE(!cone || g->nv >= 2, "mct_fdk_bp: cone beam needs at least 2 detector rows");
     MCT_REQUIRE(cone || g->nz <= g->nv, "mct_fdk_bp: fan beam needs nz <= detector rows");
     MCT_REQUIRE(g->u_step != 0.0f, "mct_fdk_bp: zero detector spacing");
+    MCT_REQUIRE((int64_t)g->nv * (g->nu - 1) < ((int64_t)1 << 31), "mct_fdk_bp: detector too large");
     BpParams p{};
     p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views;
     p.cone = cone; p.curved = (g->flags & MCT_CURVED) != 0;

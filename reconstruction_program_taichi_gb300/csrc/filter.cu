@@ -191,24 +191,50 @@ __device__ __forceinline__ uint32_t make_pair<uint32_t>(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&p);
 }
 
+// The base value A as the packed type stores it (float32: A itself; bf16: A rounded).
+template <typename QT>
+__device__ __forceinline__ float stored_base(float a);
+template <>
+__device__ __forceinline__ float stored_base<float4>(float a) { return a; }
+template <>
+__device__ __forceinline__ float stored_base<uint2>(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
+template <>
+__device__ __forceinline__ float stored_base<float2>(float a) { return a; }
+template <>
+__device__ __forceinline__ float stored_base<uint32_t>(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
+
 // Source element (view j, row r, column c) is F[r*rs + j*vs + c].
-// cone: Q[j][r][c] = {F(j,r,c), F(j,r,c+1), F(j,r+1,c), F(j,r+1,c+1)}, r<nv-1, c<nu-1
+// cone: Q[j][r][c], r < nv, c < nu-1.  For r < nv-1 the bilinear coefficients of
+// detector cell (r, c) (A = F(j,r,c), B = F(j,r,c+1), C = F(j,r+1,c), D = F(j,r+1,c+1)):
+// {A', C-A', B-A', (D-C)-(B-A')} with A' = A as stored.  The differences are formed in
+// float32 against the stored A', so with bf16 storage the corners B, C, D are
+// reproduced to bf16 precision of the (small) differences and only A carries a full
+// bf16 rounding error, weighted by (1-ru)(1-rv) in the interpolated value.
+// Row nv-1 is all NaN: the backprojector sends every off-detector row there, so an
+// off-detector voxel ends up NaN and is written as 0.
 template <typename QT>
 __global__ void pack_quad_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
                                  QT* __restrict__ Q) {
-    const int nq = nu - 1, rq = nv - 1;
+    const int nq = nu - 1, rq = nv;
     int64_t n = (int64_t)views * rq * nq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int c = (int)(i % nq);
         int64_t jr = i / nq;
         int r = (int)(jr % rq);
         int j = (int)(jr / rq);
+        if (r == nv - 1) {
+            const float qn = __int_as_float(0x7fffffff);
+            Q[i] = make_quad<QT>(qn, qn, qn, qn);
+            continue;
+        }
         const float* f = F + r * rs + j * vs + c;
-        Q[i] = make_quad<QT>(f[0], f[1], f[rs], f[rs + 1]);
+        const float a = stored_base<QT>(f[0]), b = f[1], cc = f[rs], d = f[rs + 1];
+        const float bma = b - a, dmc = d - cc;
+        Q[i] = make_quad<QT>(a, cc - a, bma, dmc - bma);
     }
 }
 
-// fan: P[j][r][c] = {F(j,r,c), F(j,r,c+1)}, c<nu-1
+// fan: P[j][r][c] = {A', F(j,r,c+1) - A'} with A' = F(j,r,c) as stored, c < nu-1
 template <typename PT>
 __global__ void pack_pair_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
                                  PT* __restrict__ P) {
@@ -220,7 +246,8 @@ __global__ void pack_pair_kernel(int nu, int nv, int views, int64_t rs, int64_t 
         int r = (int)(jr % nv);
         int j = (int)(jr / nv);
         const float* f = F + r * rs + j * vs + c;
-        P[i] = make_pair<PT>(f[0], f[1]);
+        const float a = stored_base<PT>(f[0]);
+        P[i] = make_pair<PT>(a, f[1] - a);
     }
 }
 
@@ -279,13 +306,10 @@ int mct_filter(const mct_geom* g, const float* weighted, const float* taps, floa
 
 size_t mct_packed_size(const mct_geom* g, int32_t dtype) {
     if (!g || g->nu < 2 || g->nv < 1 || g->views < 1) return 0;
-    size_t esz;
-    if (g->flags & MCT_CONE) {
-        if (g->nv < 2) return 0;
-        esz = dtype == MCT_BF16 ? 8 : 16;
-        return (size_t)g->views * (g->nv - 1) * (g->nu - 1) * esz;
-    }
-    esz = dtype == MCT_BF16 ? 4 : 8;
+    // cone: 4 coefficients per (view, row incl. the NaN row nv-1, col < nu-1); fan: 2
+    const bool cone = (g->flags & MCT_CONE) != 0;
+    if (cone && g->nv < 2) return 0;
+    const size_t esz = (cone ? 2 : 1) * (dtype == MCT_BF16 ? 4 : 8);
     return (size_t)g->views * g->nv * (g->nu - 1) * esz;
 }
 
@@ -298,7 +322,7 @@ int mct_pack_strided(const mct_geom* g, const float* src, int64_t row_stride, in
     const int64_t rs = row_stride, vs = view_stride;
     if (g->flags & MCT_CONE) {
         MCT_REQUIRE(g->nv >= 2, "mct_pack: cone beam needs at least 2 detector rows");
-        int64_t n = (int64_t)g->views * (g->nv - 1) * (g->nu - 1);
+        int64_t n = (int64_t)g->views * g->nv * (g->nu - 1);
         if (dtype == MCT_F32)
             pack_quad_kernel<float4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float4*)packed);
         else

@@ -170,12 +170,28 @@ __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const f
 // {V[z][y][x], V[z+1][y][x]}: a cell reload is four 8-byte gathers instead of eight
 // 4-byte ones, and each gather already holds the lower/upper-plane pair that the
 // packed f32x2 interpolation consumes.
-template <bool CONE, bool ZP>
+template <typename ZT>
+struct ZPair;
+template <>
+struct ZPair<float2> {
+    static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
+    static __device__ __forceinline__ float2 make(float lo, float hi) { return make_float2(lo, hi); }
+};
+template <>
+struct ZPair<uint32_t> {  // bf16 pair, lower plane in the low 16 bits
+    static __device__ __forceinline__ float2 load(const uint32_t* p) { return bf16x2_to_float2(__ldg(p)); }
+    static __device__ __forceinline__ uint32_t make(float lo, float hi) {
+        __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+        return *reinterpret_cast<uint32_t*>(&b);
+    }
+};
+
+template <bool CONE, bool ZP, typename ZT>
 __global__ void __launch_bounds__(256)
 fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
           const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
           const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
-          const float2* __restrict__ zp_x, const float2* __restrict__ zp_y, const float* __restrict__ mask,
+          const ZT* __restrict__ zp_x, const ZT* __restrict__ zp_y, const float* __restrict__ mask,
           float* __restrict__ sgm) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.z * blockDim.y + threadIdx.y;
@@ -189,7 +205,7 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
     const int nx = p.nx;
     const bool tr = (ZP || vol_t != nullptr) && spread_along_y(p, j, angles, pa);
     const float* __restrict__ V = tr ? vol_t : vol;
-    const float2* __restrict__ V2 = tr ? zp_y : zp_x;
+    const ZT* __restrict__ V2 = tr ? zp_y : zp_x;
     const int sx = tr ? nx : 1, sy = tr ? 1 : nx;
     const int plane = nx * nx;  // volumes below 2^31 voxels (checked on the host)
     Ray r;
@@ -232,11 +248,11 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
             if (off != cell) {
                 cell = off;
                 if (ZP) {
-                    const float2* b2 = V2 + off;
-                    e00 = __ldg(b2);
-                    const float2 e01 = __ldg(b2 + sx);
-                    e10 = __ldg(b2 + sy);
-                    const float2 e11 = __ldg(b2 + sx + sy);
+                    const ZT* b2 = V2 + off;
+                    e00 = ZPair<ZT>::load(b2);
+                    const float2 e01 = ZPair<ZT>::load(b2 + sx);
+                    e10 = ZPair<ZT>::load(b2 + sy);
+                    const float2 e11 = ZPair<ZT>::load(b2 + sx + sy);
                     g00 = __fadd2_rn(e01, make_float2(-e00.x, -e00.y));
                     g10 = __fadd2_rn(e11, make_float2(-e10.x, -e10.y));
                 } else {
@@ -275,9 +291,9 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
 
 // Z-paired copies: zx[z][y][x] = zy[z][x][y] = {v[z][y][x], v[z+1][y][x]} (0 above
 // the top slice); 32x32 tiles, the transposed copy through shared memory.
-__global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, float2* __restrict__ zx,
-                             float2* __restrict__ zy) {
-    __shared__ float2 tile[32][33];
+template <typename ZT>
+__global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, ZT* __restrict__ zx, ZT* __restrict__ zy) {
+    __shared__ ZT tile[32][33];
     const int64_t plane = (int64_t)nx * nx;
     const int z = blockIdx.z;
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
@@ -285,7 +301,7 @@ __global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, float2
         const int y = y0 + i, x = x0 + threadIdx.x;
         if (y < nx && x < nx) {
             const int64_t o = z * plane + (int64_t)y * nx + x;
-            const float2 e = make_float2(v[o], z + 1 < nz ? v[o + plane] : 0.0f);
+            const ZT e = ZPair<ZT>::make(v[o], z + 1 < nz ? v[o + plane] : 0.0f);
             zx[o] = e;
             tile[i][threadIdx.x] = e;
         }
@@ -574,24 +590,34 @@ size_t mct_fp_workspace_size(const mct_geom* g) {
     return (g->flags & MCT_CONE) ? 2 * n * sizeof(float2) : n * sizeof(float);
 }
 
-int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* workspace,
-           void* stream) {
+int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
+                   void* workspace, int32_t dtype, void* stream) {
     FpParams p;
     MCT_TRY(make_params(g, p, "mct_fp"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp: NULL buffer");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp: projection-matrix tables missing");
     MCT_REQUIRE(workspace != (void*)vol, "mct_fp: workspace aliases the volume");
     MCT_REQUIRE(((uintptr_t)workspace & 15) == 0, "mct_fp: workspace must be 16-byte aligned");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_fp: dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(dtype == MCT_F32 || (p.cone && workspace), "mct_fp: bf16 storage needs cone beam and a workspace");
     cudaStream_t s = as_stream(stream);
     dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
     dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
-    if (p.cone && workspace) {
-        float2* zx = static_cast<float2*>(workspace);
-        float2* zy = zx + (size_t)g->nz * g->nx * g->nx;
-        zpair_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
+    const size_t n = (size_t)g->nz * g->nx * g->nx;
+    if (p.cone && workspace && dtype == MCT_BF16) {
+        uint32_t* zx = static_cast<uint32_t*>(workspace);
+        uint32_t* zy = zx + n;
+        zpair_kernel<uint32_t><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
         MCT_TRY(launched("zpair_kernel"));
-        fp_kernel<true, true><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
-                                                     nullptr, zx, zy, mask, sgm);
+        fp_kernel<true, true, uint32_t><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
+                                                               vol, nullptr, zx, zy, mask, sgm);
+    } else if (p.cone && workspace) {
+        float2* zx = static_cast<float2*>(workspace);
+        float2* zy = zx + n;
+        zpair_kernel<float2><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
+        MCT_TRY(launched("zpair_kernel"));
+        fp_kernel<true, true, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
+                                                             vol, nullptr, zx, zy, mask, sgm);
     } else {
         float* vt = static_cast<float*>(workspace);
         if (vt) {
@@ -599,13 +625,18 @@ int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float
             MCT_TRY(launched("transpose_xy_kernel"));
         }
         if (p.cone)
-            fp_kernel<true, false><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
-                                                          vt, nullptr, nullptr, mask, sgm);
+            fp_kernel<true, false, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a,
+                                                                  t->pmat_xs, vol, vt, nullptr, nullptr, mask, sgm);
         else
-            fp_kernel<false, false><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
-                                                           vt, nullptr, nullptr, mask, sgm);
+            fp_kernel<false, false, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a,
+                                                                   t->pmat_xs, vol, vt, nullptr, nullptr, mask, sgm);
     }
     return launched("fp_kernel");
+}
+
+int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* workspace,
+           void* stream) {
+    return mct_fp_storage(g, t, vol, mask, sgm, workspace, MCT_F32, stream);
 }
 
 int mct_fp_adjoint(const mct_geom* g, const mct_tables* t, const float* sgm, const float* mask, float* vol,

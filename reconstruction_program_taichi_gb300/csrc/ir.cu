@@ -26,13 +26,13 @@ struct UbParams {
 
 // All views of the per-view backprojector, accumulated in registers in view order.
 // SRC 0 reads the plain sinogram [nv][views][nu] (4 gathers per update); SRC 1 / 2
-// read the packed stencils of mct_pack_strided (one 16-byte float32 or 8-byte bf16
-// gather per update).
+// read the packed bilinear coefficients of mct_pack_strided (one 16-byte float32 or
+// 8-byte bf16 gather per update; the same bilinear value up to float32 rounding).
 template <int SRC, typename QT, typename PT>
 __global__ void __launch_bounds__(UB_TX* UB_TY)
 bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
                     const float* __restrict__ sgm, const void* __restrict__ packed, float* __restrict__ vol) {
-    const int nq = p.nu - 1, rq = p.cone ? p.nv - 1 : p.nv;
+    const int nq = p.nu - 1;  // packed: nv rows of nu-1 stencils per view
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, unused}
     const int ix = blockIdx.x * UB_TX + threadIdx.x;
     const int iy = blockIdx.y * UB_TY + threadIdx.y;
@@ -90,26 +90,30 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
                     const float vf = floorf(vi);
                     if (!(vf >= 0.0f && vf + 1.0f <= (float)(p.nv - 1))) continue;
                     const float rv = vi - vf;
-                    float a, b, c, d;
                     if (SRC == 0) {
                         const float* s0 = sgm + (int64_t)(int)vf * rowstride + (int64_t)j * p.nu + uc;
-                        a = __ldg(s0); b = __ldg(s0 + 1); c = __ldg(s0 + rowstride); d = __ldg(s0 + rowstride + 1);
+                        const float a = __ldg(s0), b = __ldg(s0 + 1), c = __ldg(s0 + rowstride),
+                                    d = __ldg(s0 + rowstride + 1);
+                        const float p0 = a * (1 - ru) + b * ru;
+                        const float p1 = c * (1 - ru) + d * ru;
+                        acc[k] += ((1 - rv) * p0 + rv * p1) * w;
                     } else {
-                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * rq + (int)vf) * nq + uc, a, b,
-                                       c, d);
+                        float2 lo, hi;
+                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * p.nv + (int)vf) * nq + uc, lo,
+                                       hi);
+                        const float2 s2 = __ffma2_rn(make_float2(ru, ru), hi, lo);
+                        acc[k] += fmaf(rv, s2.y, s2.x) * w;
                     }
-                    const float p0 = a * (1 - ru) + b * ru;
-                    const float p1 = c * (1 - ru) + d * ru;
-                    acc[k] += ((1 - rv) * p0 + rv * p1) * w;
                 } else {
-                    float a, b;
                     if (SRC == 0) {
                         const float* s0 = sgm + (int64_t)(zb + k) * rowstride + (int64_t)j * p.nu + uc;
-                        a = __ldg(s0); b = __ldg(s0 + 1);
+                        const float a = __ldg(s0), b = __ldg(s0 + 1);
+                        acc[k] += ((1 - ru) * a + ru * b) * w;
                     } else {
-                        Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * rq + zb + k) * nq + uc, a, b);
+                        const float2 pr =
+                            Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb + k) * nq + uc);
+                        acc[k] += fmaf(ru, pr.y, pr.x) * w;
                     }
-                    acc[k] += ((1 - ru) * a + ru * b) * w;
                 }
             }
         }
@@ -119,6 +123,106 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
 #pragma unroll
     for (int k = 0; k < UB_ZC; ++k)
         if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = ((trunc >> k) & 1u) ? 0.0f : acc[k];
+}
+
+// Axial view mode over packed coefficients.  For a voxel column (x, y) the rotation,
+// the magnification, u, the truncation test and the in-plane distance to the source
+// depend only on (x, y, view), so they are evaluated once per column and view; per
+// slice remain v, one gather and the distance factor
+//     sqrt(qx^2 + qy^2 + z^2) / max(|qx|, |qy|) * px
+// (run_mgfbp_iterative_recon_IRN_CGLS.py:417-421) with the square root as d2 * rsqrt(d2).
+// A column that leaves the detector in u in some view is all zero in the reference
+// (SetTruncatedRegionToZero), so its thread stops there.
+constexpr int UA_ZC = 16;
+template <bool CONE, typename QT, typename PT>
+__global__ void __launch_bounds__(UB_TX* UB_TY)
+bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
+                          const void* __restrict__ packed, float* __restrict__ vol) {
+    const int nq = p.nu - 1;  // packed: nv rows of nu-1 coefficient sets per view
+    __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, sid*cos b}
+    __shared__ float tab_s[UB_VCHUNK];  // sid*sin b
+    const int ix = blockIdx.x * UB_TX + threadIdx.x;
+    const int iy = blockIdx.y * UB_TY + threadIdx.y;
+    const int zb = blockIdx.z * UA_ZC;
+    const int tid = threadIdx.y * UB_TX + threadIdx.x;
+    const bool active = ix < p.nx && iy < p.nx;
+    // same expressions as the general kernel with the axial mode's zero z-terms
+    const float x = p.o_x + ix * p.ex_x + iy * p.ey_x + zb * p.ez_x;
+    const float y = p.o_y + ix * p.ex_y + iy * p.ey_y + zb * p.ez_y;
+    const float bz = p.z0 + ix * p.zx + iy * p.zy + zb * p.zz;
+    float acc[UA_ZC];
+#pragma unroll
+    for (int k = 0; k < UA_ZC; ++k) acc[k] = 0.0f;
+    bool trunc = false;
+
+    for (int jc = 0; jc < p.views; jc += UB_VCHUNK) {
+        const int nvc = min(UB_VCHUNK, p.views - jc);
+        __syncthreads();
+        for (int q = tid; q < nvc; q += UB_TX * UB_TY) {
+            float s, c;
+            sincosf(angles[jc + q] - p.img_rot, &s, &c);
+            tab[q] = make_float4(c, s, czv ? czv[jc + q] : cz_const, p.sid * c);
+            tab_s[q] = p.sid * s;
+        }
+        __syncthreads();
+        if (!active || trunc) continue;
+        for (int q = 0; q < nvc; ++q) {
+            const int j = jc + q;
+            const float4 tb = tab[q];
+            const float cb = tb.x, sb = tb.y;
+            const float L = p.sid - x * cb - y * sb;
+            const float qx = x - tb.w, qy = y - tab_s[q];
+            const float aqx = fabsf(qx), aqy = fabsf(qy);
+            const float mag = p.sdd / L;
+            const float t = -x * sb + y * cb;
+            const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
+            const float ui = (u - p.u0) * p.inv_ustep;
+            if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {
+                trunc = true;
+                break;
+            }
+            const float uf = floorf(ui);
+            const float ru = ui - uf;
+            const int uc = (int)uf;
+            const float r2 = qx * qx + qy * qy;
+            const float wpx = p.px / (aqx > aqy ? aqx : aqy);
+            if (CONE) {
+                const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq + uc;
+                const float2 ru2 = make_float2(ru, ru);
+#pragma unroll
+                for (int k = 0; k < UA_ZC; ++k) {
+                    const float z = fmaf((float)k, p.zz, bz) + tb.z;
+                    const float vi = (mag * z - p.v0) * p.kv;
+                    const float vf = floorf(vi);
+                    const bool in = vf >= 0.0f && vf + 1.0f <= (float)(p.nv - 1);  // else: no contribution
+                    const int vr = in ? (int)vf : 0;
+                    const float rv = vi - vf;
+                    float2 lo, hi;
+                    Quad<QT>::load(base + vr * nq, lo, hi);
+                    const float2 s2 = __ffma2_rn(ru2, hi, lo);
+                    const float d2 = fmaf(z, z, r2);
+                    const float w = d2 * rsqrtf(d2) * wpx;
+                    acc[k] += in ? fmaf(rv, s2.y, s2.x) * w : 0.0f;
+                }
+            } else {
+                const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
+#pragma unroll
+                for (int k = 0; k < UA_ZC; ++k) {
+                    if (zb + k < p.nz) {
+                        const float z = fmaf((float)k, p.zz, bz) + tb.z;
+                        const float2 pr = Pair<PT>::load(base + k * nq);
+                        const float d2 = fmaf(z, z, r2);
+                        acc[k] += fmaf(ru, pr.y, pr.x) * (d2 * rsqrtf(d2) * wpx);
+                    }
+                }
+            }
+        }
+    }
+    if (!active) return;
+    const int64_t plane = (int64_t)p.nx * p.nx;
+#pragma unroll
+    for (int k = 0; k < UA_ZC; ++k)
+        if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = trunc ? 0.0f : acc[k];
 }
 
 // Forward differences (y, x, z) with zero at the far edge; z only when nz > 2.
@@ -283,7 +387,24 @@ int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const vo
     MCT_TRY(unmatched_params(g, p));
     MCT_REQUIRE(t && t->angles && packed && vol, "mct_bp_ref_unmatched_packed: NULL buffer");
     MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_bp_ref_unmatched_packed: dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE((int64_t)g->nv * (g->nu - 1) < ((int64_t)1 << 31), "mct_bp_ref_unmatched_packed: detector too large");
     dim3 block(UB_TX, UB_TY);
+    cudaStream_t s = as_stream(stream);
+    if (g->view_mode == 1) {
+        dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UA_ZC - 1) / UA_ZC);
+        const bool bf = dtype == MCT_BF16;
+        if (p.cone && bf)
+            bp_unmatched_axial_kernel<true, uint2, uint32_t><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed, vol);
+        else if (p.cone)
+            bp_unmatched_axial_kernel<true, float4, float2><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed, vol);
+        else if (bf)
+            bp_unmatched_axial_kernel<false, uint2, uint32_t><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed,
+                                                                                    vol);
+        else
+            bp_unmatched_axial_kernel<false, float4, float2><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed,
+                                                                                   vol);
+        return launched("bp_unmatched_axial_kernel");
+    }
     dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
     if (dtype == MCT_F32)
         bp_unmatched_kernel<1, float4, float2><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz,

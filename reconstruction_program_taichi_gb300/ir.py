@@ -31,13 +31,20 @@ class IrSystem:
     """P (masked FP), P^T (reference backprojector or exact adjoint), the TV
     operators and CGLS for one iterative-reconstruction geometry."""
 
-    def __init__(self, obj, device=None):
+    def __init__(self, obj, device=None, storage=None):
         if not torch.cuda.is_available():
             raise RuntimeError("a CUDA device is required (this package has no CPU fallback)")
         self.obj = obj
         self.dg = ir_geometry(obj, device)
         self.device = self.dg.device
         self.matched = getattr(obj, "back_projector", "reference") == "adjoint"
+        storage = storage or getattr(obj, "storage_precision", "float32")
+        if storage not in ("float32", "bfloat16"):
+            raise ValueError("storage must be float32 or bfloat16")
+        # bf16 gathers: FP volume copies (cone beam) and the packed sinogram of the
+        # reference backprojector; the exact adjoint scatters float32 either way
+        self.dtype = ops.MCT_BF16 if storage == "bfloat16" else ops.MCT_F32
+        self.fp_dtype = self.dtype if self.dg.geom.flags & ops.MCT_CONE else ops.MCT_F32
         self.mask = ops.effective_map(self.dg)
         f32 = dict(dtype=torch.float32, device=self.device)
         self.fp_buf = torch.empty(self.dg.sgm_shape, **f32)
@@ -48,16 +55,17 @@ class IrSystem:
 
     # ------------------------------------------------------------ operators
     def fp(self, x, out=None):
-        return ops.fp(self.dg, x, mask=self.mask, out=out)
+        return ops.fp(self.dg, x, mask=self.mask, out=out, dtype=self.fp_dtype)
 
     def bp(self, sgm, out=None):
         if self.matched:
             return ops.fp_adjoint(self.dg, sgm, mask=self.mask, out=out)
-        # pack the sinogram into one-gather stencils, then backproject
+        # pack the sinogram into one-gather bilinear coefficients, then backproject
         if getattr(self, "_packed", None) is None:
-            self._packed = torch.empty(max(ops.packed_bytes(self.dg), 16), dtype=torch.uint8, device=self.device)
-        ops.pack_sinogram(self.dg, sgm, out=self._packed)
-        return ops.bp_unmatched_packed(self.dg, self._packed, out=out)
+            self._packed = torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16), dtype=torch.uint8,
+                                       device=self.device)
+        ops.pack_sinogram(self.dg, sgm, dtype=self.dtype, out=self._packed)
+        return ops.bp_unmatched_packed(self.dg, self._packed, dtype=self.dtype, out=out)
 
     def ptp(self, x, out=None):
         """P^T P x (run_mgfbp_iterative_recon_IRN_CGLS.py:288-316)."""

@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import MCT_BF16, MCT_F32, Geom, Tables
+from ._lib import MCT_BF16, MCT_CONE, MCT_F32, Geom, Tables
 
 
 def _ptr(t):
@@ -195,9 +195,10 @@ def fp_workspace(dg):
     return ws
 
 
-def fp(dg, vol, mask=None, out=None, workspace=True):
-    """P vol.  workspace=True uses the geometry's cached transposed-volume buffer
-    (coalesced gathers for every view); None runs without it."""
+def fp(dg, vol, mask=None, out=None, workspace=True, dtype=MCT_F32):
+    """P vol.  workspace=True uses the geometry's cached gather-copy buffer (coalesced
+    gathers for every view); None runs without it.  dtype=MCT_BF16 (cone beam) stores
+    the gather copies as bf16 (mct_fp_storage)."""
     _check(vol, "vol", dg.vol_shape)
     if mask is not None:
         _check(mask, "mask", dg.sgm_shape)
@@ -205,7 +206,10 @@ def fp(dg, vol, mask=None, out=None, workspace=True):
         out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=vol.device)
     _check(out, "out", dg.sgm_shape)
     ws = fp_workspace(dg) if workspace is True else workspace
-    _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), _stream())
+    if dtype == MCT_F32:
+        _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), _stream())
+    else:
+        _lib.call("mct_fp_storage", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), int(dtype), _stream())
     return out
 
 

@@ -298,8 +298,9 @@ def test_fdk_with_tc_filter_vs_oracle(cuda):
 
 
 @pytest.mark.parametrize("cone", [True, False])
-def test_packed_unmatched_bp_is_identical(cone, cuda):
-    """The packed-stencil backprojector reads the same values in the same order."""
+def test_packed_unmatched_bp_matches_plain(cone, cuda):
+    """The packed-coefficient backprojector gives the plain one's result up to float32
+    rounding of the bilinear form, with the same truncated voxels."""
     import torch
     from reconstruction_program_taichi_gb300 import config, geometry, ops
     kw = {} if cone else {"ConeBeam": False, "DetectorElementCountVertical": 6, "ImageDimensionZ": 6}
@@ -310,4 +311,41 @@ def test_packed_unmatched_bp_is_identical(cone, cuda):
     sgm = torch.rand(dg.sgm_shape, device="cuda", generator=g)
     a = ops.bp_unmatched(dg, sgm)
     b = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm))
-    assert torch.equal(a, b)
+    assert torch.equal(a == 0, b == 0)
+    assert float((a - b).norm() / a.norm()) < 1e-6
+    assert float((a - b).abs().max()) < 1e-5 * float(a.abs().max())
+
+
+def test_fp_bf16_storage_error_is_small(cuda):
+    """bf16 gather copies: only the stored voxel values are rounded (relative 2^-9 per
+    voxel); the projection error stays far below that, and masking is unchanged."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    from reconstruction_program_taichi_gb300._lib import MCT_BF16
+    o = _cone_obj(views=60)
+    dg = geometry.fpj_geometry(o)
+    vol = torch.from_numpy(_smooth(np.random.default_rng(9), o.img_dim_z, o.img_dim)).cuda()
+    a = ops.fp(dg, vol)
+    b = ops.fp(dg, vol, dtype=MCT_BF16)
+    assert torch.equal(a == 0, b == 0)
+    assert float((a - b).norm() / a.norm()) < 2e-3
+    # exact when the volume is representable in bf16
+    vb = vol.to(torch.bfloat16).float()
+    assert float((ops.fp(dg, vb) - ops.fp(dg, vb, dtype=MCT_BF16)).abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("cone", [True, False])
+def test_packed_unmatched_bp_bf16_error_is_small(cone, cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import config, geometry, ops
+    from reconstruction_program_taichi_gb300._lib import MCT_BF16
+    kw = {} if cone else {"ConeBeam": False, "DetectorElementCountVertical": 6, "ImageDimensionZ": 6}
+    o = _cone_obj(n=40, nz=12, nu=64, nv=20, views=36, DetectorElementHeight=1.2, **kw)
+    config.parse_ir(o, {"Lambda": 1e-3})
+    dg = geometry.ir_geometry(o)
+    g = torch.Generator(device="cuda").manual_seed(32)
+    sgm = torch.rand(dg.sgm_shape, device="cuda", generator=g)
+    a = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm))
+    b = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm, dtype=MCT_BF16), dtype=MCT_BF16)
+    assert torch.equal(a == 0, b == 0)
+    assert float((a - b).norm() / a.norm()) < 5e-3
