@@ -65,6 +65,37 @@ def ellipsoids(w):
     return np.asarray(out, dtype=np.float32)
 
 
+def phantom(w, dev):
+    """The ellipsoids of ellipsoids(w) sampled at the voxel centres of the
+    reconstruction grid ([z][y][x], row 0 = +y, slice 0 = -z), float32 on dev."""
+    import torch
+    nx, nz, px, pz = w["nx"], w["nz"], w["px"], w["pz"]
+    f64 = dict(device=dev, dtype=torch.float64)
+    x = ((torch.arange(nx, **f64) - (nx - 1) / 2) * px)[None, None, :]
+    y = (((nx - 1) / 2 - torch.arange(nx, **f64)) * px)[None, :, None]
+    z = ((torch.arange(nz, **f64) - (nz - 1) / 2) * pz)[:, None, None]
+    vol = torch.zeros(nz, nx, nx, device=dev, dtype=torch.float32)
+    for e in ellipsoids(w).astype(np.float64):
+        c, s_ = math.cos(e[6]), math.sin(e[6])
+        qx, qy = x - e[0], y - e[1]
+        r = ((qx * c + qy * s_) / e[3]) ** 2 + ((-qx * s_ + qy * c) / e[4]) ** 2 + ((z - e[2]) / e[5]) ** 2
+        vol += (r <= 1.0).float() * float(e[9])
+    return vol
+
+
+def rmse(a, b, mask):
+    import torch
+    return float(torch.sqrt(((a - b)[mask].double() ** 2).mean()))
+
+
+def noisy(line, photons, seed):
+    """Poisson counts at `photons` incident photons, back to line integrals."""
+    import torch
+    gen = torch.Generator(device=line.device).manual_seed(seed)
+    counts = torch.poisson(photons * torch.exp(-line.double()), generator=gen).clamp_(min=1.0)
+    return torch.log(photons / counts).float().contiguous()
+
+
 class Obj:
     verbose = False
 
@@ -160,12 +191,9 @@ def run_gpu(args, w):
     fpg = geometry.fpj_geometry(o, device=dev)
     # synthetic data (not timed)
     ell = ellipsoids(w)
-    line = ops.project_ellipsoids(pipe.dg, ell)
-    gen = torch.Generator(device=dev).manual_seed(w["seed"])
-    counts = torch.poisson(w["photons"] * torch.exp(-line.double()), generator=gen).clamp_(min=1.0)
-    sgm = torch.log(w["photons"] / counts).float().contiguous()
-    del line, counts
+    sgm = noisy(ops.project_ellipsoids(pipe.dg, ell), w["photons"], w["seed"])
     fp_out = torch.empty(fpg.sgm_shape, dtype=torch.float32, device=dev)
+    fp_dtype = ops.MCT_BF16 if args.storage == "bf16" else ops.MCT_F32
     stream = torch.cuda.current_stream(dev)
 
     def step(evs=None):
@@ -180,7 +208,7 @@ def run_gpu(args, w):
         vol = ops.fdk_bp(pipe.dg, packed, pipe.dtype, out=pipe.vol)
         if evs:
             evs[3].record(stream)
-        ops.fp(fpg, vol, out=fp_out)
+        ops.fp(fpg, vol, out=fp_out, dtype=fp_dtype)
         if evs:
             evs[4].record(stream)
         return vol
@@ -223,13 +251,13 @@ def run_gpu(args, w):
     hbm, _, peak_kind = peaks()
     n_samples = ops.fp_count_samples(fpg)
     bp_bytes = nvox * w["views"] * (8 if pipe.dtype == 1 else 16) + nvox * 4
-    fp_bytes = n_samples * 32 + fpg.geom.nv * fpg.geom.views * fpg.geom.nu * 4
+    fp_bytes = n_samples * (16 if fp_dtype == ops.MCT_BF16 else 32) + fpg.geom.nv * fpg.geom.views * fpg.geom.nu * 4
     dom = "fp_kernel" if st[3] >= st[2] else "fdk_bp_kernel"
     dom_ms, dom_bytes = (st[3], fp_bytes) if dom == "fp_kernel" else (st[2], bp_bytes)
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     traffic = None
     tj = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if os.path.exists(tj):
+    if os.path.exists(tj) and args.storage == "f32" and w is WORKLOAD:
         traffic = json.load(open(tj)).get(dom)
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": peak_kind,
@@ -245,7 +273,7 @@ def run_gpu(args, w):
     def e2e_step():
         dev_sgm.copy_(host_sgm, non_blocking=True)
         vol = pipe.run(dev_sgm)
-        ops.fp(fpg, vol, out=fp_out)
+        ops.fp(fpg, vol, out=fp_out, dtype=fp_dtype)
         host_vol.copy_(vol, non_blocking=True)
         host_fp.copy_(fp_out, non_blocking=True)
 
@@ -263,13 +291,46 @@ def run_gpu(args, w):
            "h2d_bytes_per_step": int(host_sgm.numel() * 4),
            "d2h_bytes_per_step": int(host_vol.numel() * 4 + host_fp.numel() * 4)}
 
-    # mixed-precision FDK variants: tensor-core split-bf16 filter, with float32 or bf16
-    # backprojection operand
+    # mixed precision: tensor-core split-bf16 filter, bf16 backprojection operand, bf16
+    # forward-projection cells; the whole step, then FDK-only variants
     mixed = None
     if args.storage == "f32" and not args.no_mixed:
         ref_vol = pipe.run(sgm).clone()
+        ref_fp = ops.fp(fpg, ref_vol).clone()
         plain_ms = float(st[0] + st[1] + st[2])
         mixed = {"fdk_plain_ms": round(plain_ms, 3)}
+        pm = fbp.FdkPipeline(o, device=dev, storage="bf16", filter_impl="tc")
+        pm.set_taps(pipe.taps.cpu().numpy())
+        fp_m = torch.empty_like(fp_out)
+
+        def mixed_step():
+            vol = pm.run(sgm)
+            ops.fp(fpg, vol, out=fp_m, dtype=ops.MCT_BF16)
+            return vol
+
+        for _ in range(args.warmup):
+            mixed_step()
+        barrier()
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for _ in range(args.steps):
+            mv = mixed_step()
+        m1.record(stream)
+        barrier()
+        pm.tc.status()
+        mms = m0.elapsed_time(m1) / args.steps
+        ph = phantom(w, dev)
+        live = ref_vol != 0
+        r_plain, r_mixed = rmse(ref_vol, ph, live), rmse(mv, ph, live)
+        mixed["step"] = {
+            "ms_per_step": round(mms, 3), "gups": round(units / (mms / 1e3) / 1e9, 3),
+            "speedup_vs_plain": round(ms / mms, 3),
+            "fdk_rmse_vs_phantom": {"plain": r_plain, "mixed": r_mixed, "ratio": round(r_mixed / r_plain, 5)},
+            "fdk_rel_l2_vs_plain": float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol)),
+            "fp_rel_l2_vs_plain": float(torch.linalg.vector_norm(fp_m - ref_fp) / torch.linalg.vector_norm(ref_fp)),
+            "storage": "sinogram filter split-bf16 on tcgen05; bf16 backprojection coefficients; bf16 FP cells",
+        }
+        del pm, ph, live, fp_m
         for name, storage in (("tc_filter", "f32"), ("tc_filter_bf16_bp", "bf16")):
             pm = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl="tc")
             pm.set_taps(pipe.taps.cpu().numpy())
@@ -295,7 +356,7 @@ def run_gpu(args, w):
 
     cgls = None
     if not args.no_cgls and w is WORKLOAD:
-        cgls = cgls_bench(dev, stream, barrier)
+        cgls = irn_bench(dev, stream, barrier)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -320,7 +381,7 @@ def run_gpu(args, w):
             "fp_gups": round(nvox * w["views"] / (st[3] / 1e3) / 1e9, 2),
             "fp_samples_per_s": round(n_samples / (st[3] / 1e3), 1), "fp_in_volume_samples": n_samples,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clk.summary(), "mixed": mixed, "cgls_c3": cgls,
+            "clocks": clk.summary(), "mixed": mixed, "irn_cgls_tv": cgls,
         }
         print(json.dumps(line))
     if world > 1:
@@ -332,41 +393,51 @@ C3 = dict(nu=1024, nv=64, views=360, nx=512, nz=64, du=0.8, dv=0.8, px=0.4, pz=0
           step=0.2, n_ell=20, photons=1e5, seed=2025)
 
 
-def cgls_bench(dev, stream, barrier, iters=5):
-    """Seconds per CGLS iteration (one P^T P + TV + fused updates) of the IRN-CGLS-TV
-    configuration: 512x512x64 volume, 360 views, 1024x64 detector, lambda 1e-3, with
-    the reference's operator pair (masked FP + voxel-driven backprojector)."""
+def irn_bench(dev, stream, barrier):
+    """IRN-CGLS-TV, 20 reweightings x 10 CG iterations (the reference driver's loop,
+    run_mgfbp_iterative_recon_IRN_CGLS.py:157-172) on 512x512x64 @0.4 mm, 360 views,
+    1024x64 detector, lambda 1e-3, beta_TV 1e-6, with the reference operator pair
+    (masked FP + voxel-driven backprojector), from a zero start, for float32 and bf16
+    gather storage: seconds per P^T P iteration and RMSE vs the phantom."""
     import torch
-    from reconstruction_program_taichi_gb300 import config, ops
-    from reconstruction_program_taichi_gb300.ir import IrSystem
-    cfg = make_config(C3)
-    cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 20, "NumberOfIterations": 10})
-    o = Obj()
-    config.parse_fbp(o, cfg)
-    config.parse_fpj(o, cfg)
-    config.parse_fpj_v3(o, cfg)
-    config.parse_ir(o, cfg)
-    sy = IrSystem(o, device=dev)
-    sgm = ops.project_ellipsoids(sy.dg, ellipsoids(C3))
-    x0 = torch.zeros(sy.dg.vol_shape, dtype=torch.float32, device=dev)
-    sy.bpb = sy.bp_b(sgm)
-    wr = ops.tv_weights(sy.dg, x0 + 0.01, 1e-6)
-    lr = o.coef_lambda * o.pixel_count_ratio
-    sy.cgls(x0, [], [(lr, wr)], 1)  # warm-up
-    barrier()
-    calls0 = sy.ptp_calls
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    x = sy.cgls(x0, [], [(lr, wr)], iters)
-    e1.record(stream)
-    barrier()
-    n = sy.ptp_calls - calls0  # the reference's "iterations": P^T P applications
-    s = e0.elapsed_time(e1) / 1e3
-    total = 21 * 11  # 1 + 20 reweightings, each 1 + 10 P^T P (run_mgfbp_iterative_recon_IRN_CGLS.py:165-169)
-    return {"s_per_iter": round(s / n, 5), "ptp_per_solve": iters + 1, "timed_ptp": n,
-            "projected_20x10_s": round(s / n * total, 2), "operator": "reference pair (masked FP + per-view BP)",
-            "config": "512x512x64 @0.4mm, 360 views, 1024x64 det, lambda 1e-3",
-            "finite": bool(torch.isfinite(x).all())}
+    from reconstruction_program_taichi_gb300 import ops
+    from reconstruction_program_taichi_gb300.ir import Mgfbp_ir
+    out = {"config": "512x512x64 @0.4mm, 360 views, 1024x64 det, lambda 1e-3, beta_TV 1e-6, 20 IRN x 10 CG "
+                     "(231 P^T P), zero start, Poisson 1e5",
+           "operator": "reference pair (masked FP + per-view BP)"}
+    ph = None
+    for storage in ("float32", "bfloat16"):
+        cfg = make_config(C3)
+        cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 20, "NumberOfIterations": 10,
+                    "StoragePrecision": storage})
+        ir = Mgfbp_ir(cfg, device=dev, verbose=False)
+        sy = ir.system
+        sgm = noisy(ops.project_ellipsoids(sy.dg, ellipsoids(C3)), C3["photons"], C3["seed"])
+        x0 = torch.zeros(sy.dg.vol_shape, dtype=torch.float32, device=dev)
+        sy.bpb = sy.bp_b(sgm)
+        sy.cgls(x0, [], [(1e-3, torch.ones_like(x0))], 2)  # warm-up
+        barrier()
+        calls0 = sy.ptp_calls
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        x = ir.solve_tv(sgm, x0)
+        e1.record(stream)
+        barrier()
+        n = sy.ptp_calls - calls0
+        sec = e0.elapsed_time(e1) / 1e3
+        if ph is None:
+            ph = phantom(C3, dev)
+            n_ = C3["nx"]
+            yy, xx = torch.meshgrid(torch.arange(n_, device=dev) - (n_ - 1) / 2,
+                                    torch.arange(n_, device=dev) - (n_ - 1) / 2, indexing="ij")
+            fov = (yy ** 2 + xx ** 2 <= (0.95 * n_ / 2) ** 2).expand_as(ph).contiguous()
+        out[storage] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
+                        "rmse_vs_phantom": rmse(x, ph, fov), "finite": bool(torch.isfinite(x).all())}
+        del ir, sy, sgm, x
+    f, b = out["float32"], out["bfloat16"]
+    out["speedup_mixed"] = round(f["s_total"] / b["s_total"], 3)
+    out["rmse_ratio_mixed"] = round(b["rmse_vs_phantom"] / f["rmse_vs_phantom"], 5)
+    return out
 
 
 # ---------------------------------------------------------------- CPU (reference) arm

@@ -164,10 +164,15 @@ size_t mct_fp_workspace_size(const mct_geom* g);
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
            void* workspace, void* stream);
 
-/* mct_fp with the z-paired gather copies stored as dtype: MCT_F32 is mct_fp; MCT_BF16
- * (cone beam, workspace required) rounds the volume to bf16 in the copies, halving
- * the bytes each trilinear gather moves; interpolation and sums stay float32.
- * No counterpart in the reference (its projector is float32 only). */
+/* Bytes of the mct_fp_storage workspace for dtype (MCT_F32: mct_fp_workspace_size;
+ * MCT_BF16: two bf16 cell copies, 32 bytes per voxel; 0 if unsupported). */
+size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype);
+
+/* mct_fp reading gather copies stored as dtype: MCT_F32 is mct_fp; MCT_BF16 (cone
+ * beam, workspace of mct_fp_storage_workspace_size bytes required) stores every
+ * voxel's whole 2x2x2 trilinear cell as 8 bf16 values, so a cell is one 16-byte
+ * gather; the volume values are rounded to bf16, interpolation and sums stay
+ * float32.  No counterpart in the reference (its projector is float32 only). */
 int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
                    void* workspace, int32_t dtype, void* stream);
 

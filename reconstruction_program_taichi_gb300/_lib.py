@@ -76,6 +76,7 @@ SIGNATURES = {
     "mct_fdk_bp": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
     "mct_fp_workspace_size": (ctypes.c_size_t, [_G]),
     "mct_fp": (ctypes.c_int, [_G, _T, _P, _P, _P, _P, _P]),
+    "mct_fp_storage_workspace_size": (ctypes.c_size_t, [_G, _i32]),
     "mct_fp_storage": (ctypes.c_int, [_G, _T, _P, _P, _P, _P, _i32, _P]),
     "mct_fp_adjoint": (ctypes.c_int, [_G, _T, _P, _P, _P, _P]),
     "mct_effective_map": (ctypes.c_int, [_G, _T, _P, _P]),

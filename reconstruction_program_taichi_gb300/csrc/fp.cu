@@ -12,6 +12,7 @@
 // applies the reference's per-sample inside test exactly; samples outside the box
 // contribute 0 in the reference too.
 #include <cmath>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -177,14 +178,17 @@ struct ZPair<float2> {
     static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
     static __device__ __forceinline__ float2 make(float lo, float hi) { return make_float2(lo, hi); }
 };
-template <>
-struct ZPair<uint32_t> {  // bf16 pair, lower plane in the low 16 bits
-    static __device__ __forceinline__ float2 load(const uint32_t* p) { return bf16x2_to_float2(__ldg(p)); }
-    static __device__ __forceinline__ uint32_t make(float lo, float hi) {
-        __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
-        return *reinterpret_cast<uint32_t*>(&b);
-    }
-};
+
+// bf16 cell copy: element (z, y, x) of either orientation holds the whole 2x2x2 cell
+// whose lowest corner is voxel (z, y, x), as four bf16 pairs {lower, upper z-plane}:
+//   .x = e00 = {V[z][y][x], V[z+1][y][x]}      .y = g00 = e01 - e00' (x+1 corner)
+//   .z = e10 = {V[z][y+1][x], V[z+1][y+1][x]}  .w = g10 = e11 - e10' (x+1, y+1)
+// (x, y as in the volume; e' is e rounded to bf16, so the x+1 corners are restored to
+// the bf16 precision of the differences).  A reload is one 16-byte gather.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&b);
+}
 
 template <bool CONE, bool ZP, typename ZT>
 __global__ void __launch_bounds__(256)
@@ -247,7 +251,13 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
             const int off = zi * plane + yi * sy + xi * sx;
             if (off != cell) {
                 cell = off;
-                if (ZP) {
+                if constexpr (ZP && std::is_same<ZT, uint4>::value) {
+                    const uint4 q = __ldg(V2 + off);
+                    e00 = bf16x2_to_float2(q.x);
+                    g00 = bf16x2_to_float2(q.y);
+                    e10 = bf16x2_to_float2(q.z);
+                    g10 = bf16x2_to_float2(q.w);
+                } else if constexpr (ZP) {
                     const ZT* b2 = V2 + off;
                     e00 = ZPair<ZT>::load(b2);
                     const float2 e01 = ZPair<ZT>::load(b2 + sx);
@@ -294,6 +304,7 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
 template <typename ZT>
 __global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, ZT* __restrict__ zx, ZT* __restrict__ zy) {
     __shared__ ZT tile[32][33];
+    static_assert(std::is_same<ZT, float2>::value, "z-pairs are float32");
     const int64_t plane = (int64_t)nx * nx;
     const int z = blockIdx.z;
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
@@ -310,6 +321,40 @@ __global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, ZT* __
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
         const int x = x0 + i, y = y0 + threadIdx.x;
         if (y < nx && x < nx) zy[z * plane + (int64_t)x * nx + y] = tile[threadIdx.x][i];
+    }
+}
+
+// bf16 cell copies (layout above): cx[z][y][x] and cy[z][x][y] both hold the cell at
+// voxel (z, y, x); corners outside the volume are 0 (no in-volume sample uses them).
+// 32x32 tiles, the transposed copy through shared memory.
+__global__ void cell_bf16_kernel(int nx, int nz, const float* __restrict__ v, uint4* __restrict__ cx,
+                                 uint4* __restrict__ cy) {
+    __shared__ uint4 tile[32][33];
+    const int64_t plane = (int64_t)nx * nx;
+    const int z = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    auto at = [&](int zz, int yy, int xx) -> float {
+        return (zz < nz && yy < nx && xx < nx) ? v[zz * plane + (int64_t)yy * nx + xx] : 0.0f;
+    };
+    auto rb = [](float a) { return __bfloat162float(__float2bfloat16_rn(a)); };
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int y = y0 + i, x = x0 + threadIdx.x;
+        if (y < nx && x < nx) {
+            const float a0 = rb(at(z, y, x)), a1 = rb(at(z + 1, y, x));
+            const float c0 = rb(at(z, y + 1, x)), c1 = rb(at(z + 1, y + 1, x));
+            uint4 q;
+            q.x = pack_bf16x2(a0, a1);
+            q.y = pack_bf16x2(at(z, y, x + 1) - a0, at(z + 1, y, x + 1) - a1);
+            q.z = pack_bf16x2(c0, c1);
+            q.w = pack_bf16x2(at(z, y + 1, x + 1) - c0, at(z + 1, y + 1, x + 1) - c1);
+            cx[z * plane + (int64_t)y * nx + x] = q;
+            tile[i][threadIdx.x] = q;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int x = x0 + i, y = y0 + threadIdx.x;
+        if (y < nx && x < nx) cy[z * plane + (int64_t)x * nx + y] = tile[threadIdx.x][i];
     }
 }
 
@@ -590,6 +635,13 @@ size_t mct_fp_workspace_size(const mct_geom* g) {
     return (g->flags & MCT_CONE) ? 2 * n * sizeof(float2) : n * sizeof(float);
 }
 
+size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype) {
+    if (!g || g->nx < 1 || g->nz < 1) return 0;
+    if (dtype != MCT_BF16) return mct_fp_workspace_size(g);
+    if (!(g->flags & MCT_CONE)) return 0;
+    return 2 * (size_t)g->nz * g->nx * g->nx * sizeof(uint4);  // two bf16 cell copies
+}
+
 int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
                    void* workspace, int32_t dtype, void* stream) {
     FpParams p;
@@ -605,12 +657,12 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
     dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
     const size_t n = (size_t)g->nz * g->nx * g->nx;
     if (p.cone && workspace && dtype == MCT_BF16) {
-        uint32_t* zx = static_cast<uint32_t*>(workspace);
-        uint32_t* zy = zx + n;
-        zpair_kernel<uint32_t><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
-        MCT_TRY(launched("zpair_kernel"));
-        fp_kernel<true, true, uint32_t><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
-                                                               vol, nullptr, zx, zy, mask, sgm);
+        uint4* cx = static_cast<uint4*>(workspace);
+        uint4* cy = cx + n;
+        cell_bf16_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy);
+        MCT_TRY(launched("cell_bf16_kernel"));
+        fp_kernel<true, true, uint4><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
+                                                            nullptr, cx, cy, mask, sgm);
     } else if (p.cone && workspace) {
         float2* zx = static_cast<float2*>(workspace);
         float2* zy = zx + n;

@@ -57,15 +57,17 @@ class IrSystem:
     def fp(self, x, out=None):
         return ops.fp(self.dg, x, mask=self.mask, out=out, dtype=self.fp_dtype)
 
-    def bp(self, sgm, out=None):
+    def bp(self, sgm, out=None, dtype=None):
         if self.matched:
             return ops.fp_adjoint(self.dg, sgm, mask=self.mask, out=out)
         # pack the sinogram into one-gather bilinear coefficients, then backproject
-        if getattr(self, "_packed", None) is None:
-            self._packed = torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16), dtype=torch.uint8,
-                                       device=self.device)
-        ops.pack_sinogram(self.dg, sgm, dtype=self.dtype, out=self._packed)
-        return ops.bp_unmatched_packed(self.dg, self._packed, dtype=self.dtype, out=out)
+        dtype = self.dtype if dtype is None else dtype
+        packed = self.__dict__.setdefault("_packed", {})
+        if dtype not in packed:
+            packed[dtype] = torch.empty(max(ops.packed_bytes(self.dg, dtype), 16), dtype=torch.uint8,
+                                        device=self.device)
+        ops.pack_sinogram(self.dg, sgm, dtype=dtype, out=packed[dtype])
+        return ops.bp_unmatched_packed(self.dg, packed[dtype], dtype=dtype, out=out)
 
     def ptp(self, x, out=None):
         """P^T P x (run_mgfbp_iterative_recon_IRN_CGLS.py:288-316)."""
@@ -73,8 +75,14 @@ class IrSystem:
         return self.bp(self.fp(x, out=self.fp_buf), out=out)
 
     def bp_b(self, sgm):
-        """P^T (b * mask) (run_mgfbp_iterative_recon_IRN_CGLS.py:319-336)."""
-        return self.bp(sgm * self.mask)
+        """P^T (b * mask) (run_mgfbp_iterative_recon_IRN_CGLS.py:319-336).  The measured
+        data is packed at float32 whatever the storage precision: rounding b to bf16
+        adds noise of the order of the photon noise, which the iterations would fit;
+        only the operator applications inside CG use the reduced storage."""
+        out = self.bp(sgm * self.mask, dtype=ops.MCT_F32)
+        if self.dtype != ops.MCT_F32:  # the float32 operand is needed once per solve
+            self._packed.pop(ops.MCT_F32, None)
+        return out
 
     def dtwd_acc(self, x, wr, s, acc):
         """acc += s * D^T W D x (in place)."""

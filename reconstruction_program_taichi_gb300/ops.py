@@ -185,13 +185,17 @@ def fdk_bp(dg, packed, dtype=MCT_F32, out=None):
 
 # ---------------------------------------------------------------- forward projection
 
-def fp_workspace(dg):
-    """Per-geometry workspace of fp() (the transposed volume copy), cached."""
-    ws = getattr(dg, "_fp_ws", None)
+def fp_workspace(dg, dtype=MCT_F32):
+    """Per-geometry workspace of fp() (the gather copies of the volume), cached per
+    storage type."""
+    cache = dg.__dict__.setdefault("_fp_ws", {})
+    ws = cache.get(int(dtype))
     if ws is None:
-        n = int(_lib.load().mct_fp_workspace_size(dg.g()))
+        n = int(_lib.load().mct_fp_storage_workspace_size(dg.g(), int(dtype)))
+        if n == 0:
+            raise ValueError("this storage type needs a cone-beam geometry")
         ws = torch.empty(max(n // 4, 1), dtype=torch.float32, device=dg.device)
-        dg._fp_ws = ws
+        cache[int(dtype)] = ws
     return ws
 
 
@@ -205,7 +209,7 @@ def fp(dg, vol, mask=None, out=None, workspace=True, dtype=MCT_F32):
     if out is None:
         out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=vol.device)
     _check(out, "out", dg.sgm_shape)
-    ws = fp_workspace(dg) if workspace is True else workspace
+    ws = fp_workspace(dg, dtype) if workspace is True else workspace
     if dtype == MCT_F32:
         _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), _stream())
     else:

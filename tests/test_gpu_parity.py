@@ -317,8 +317,9 @@ def test_packed_unmatched_bp_matches_plain(cone, cuda):
 
 
 def test_fp_bf16_storage_error_is_small(cuda):
-    """bf16 gather copies: only the stored voxel values are rounded (relative 2^-9 per
-    voxel); the projection error stays far below that, and masking is unchanged."""
+    """bf16 cell copies: only stored values are rounded (the base corner to 2^-9
+    relative, the other corners through rounded differences); the projection error
+    stays far below that, and which rays are zero is unchanged."""
     import torch
     from reconstruction_program_taichi_gb300 import geometry, ops
     from reconstruction_program_taichi_gb300._lib import MCT_BF16
@@ -329,9 +330,10 @@ def test_fp_bf16_storage_error_is_small(cuda):
     b = ops.fp(dg, vol, dtype=MCT_BF16)
     assert torch.equal(a == 0, b == 0)
     assert float((a - b).norm() / a.norm()) < 2e-3
-    # exact when the volume is representable in bf16
+    # with a bf16-representable volume only the rounded differences remain
     vb = vol.to(torch.bfloat16).float()
-    assert float((ops.fp(dg, vb) - ops.fp(dg, vb, dtype=MCT_BF16)).abs().max()) == 0.0
+    ab, bb = ops.fp(dg, vb), ops.fp(dg, vb, dtype=MCT_BF16)
+    assert float((ab - bb).norm() / ab.norm()) < 5e-4
 
 
 @pytest.mark.parametrize("cone", [True, False])
