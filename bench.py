@@ -39,7 +39,7 @@ def make_config(w):
             "DetectorElementCountVertical": w["nv"], "DetectorElementHeight": w["dv"],
             "DetectorOffsetVertical": 0.0, "Views": w["views"], "TotalScanAngle": 360,
             "SourceIsocenterDistance": w["sid"], "SourceDetectorDistance": w["sdd"], "ImageDimension": w["nx"],
-            "PixelSize": w["px"], "ImageDimensionZ": w["nz"], "VoxelHeight": w["pz"], "ConeBeam": True,
+            "PixelSize": w["px"], "ImageDimensionZ": w["nz"], "VoxelHeight": w["pz"], "ConeBeam": w.get("cone", True),
             "HammingFilter": 1, "ForwardProjectionStepSize": w["step"]}
 
 
@@ -52,6 +52,8 @@ def hann_from_ramp(ramp):
 
 
 def ellipsoids(w):
+    if not w.get("cone", True):
+        return ellipses(w)
     rng = np.random.default_rng(w["seed"])
     fov = w["nx"] * w["px"] / 2
     zext = w["nz"] * w["pz"] / 2
@@ -65,9 +67,26 @@ def ellipsoids(w):
     return np.asarray(out, dtype=np.float32)
 
 
+def ellipses(w):
+    """2D phantom as ellipsoids infinitely long in z: centres uniform in a 50 mm disc,
+    semi-axes U(5, 40) mm, angles U(0, pi), attenuation U(0.01, 0.05) /mm."""
+    rng = np.random.default_rng(w["seed"])
+    out = []
+    for _ in range(w["n_ell"]):
+        r, a = 50.0 * math.sqrt(rng.uniform()), rng.uniform(0, 2 * math.pi)
+        ax, ay = rng.uniform(5.0, 40.0, 2)
+        out.append([r * math.cos(a), r * math.sin(a), 0.0, ax, ay, 1e7, rng.uniform(0, math.pi), 0.0, 0.0,
+                    rng.uniform(0.01, 0.05)])
+    return np.asarray(out, dtype=np.float32)
+
+
 def phantom(w, dev):
     """The ellipsoids of ellipsoids(w) sampled at the voxel centres of the
     reconstruction grid ([z][y][x], row 0 = +y, slice 0 = -z), float32 on dev."""
+    return phantom_from(ellipsoids(w), w, dev)
+
+
+def phantom_from(ell, w, dev):
     import torch
     nx, nz, px, pz = w["nx"], w["nz"], w["px"], w["pz"]
     f64 = dict(device=dev, dtype=torch.float64)
@@ -75,7 +94,7 @@ def phantom(w, dev):
     y = (((nx - 1) / 2 - torch.arange(nx, **f64)) * px)[None, :, None]
     z = ((torch.arange(nz, **f64) - (nz - 1) / 2) * pz)[:, None, None]
     vol = torch.zeros(nz, nx, nx, device=dev, dtype=torch.float32)
-    for e in ellipsoids(w).astype(np.float64):
+    for e in np.asarray(ell, dtype=np.float64):
         c, s_ = math.cos(e[6]), math.sin(e[6])
         qx, qy = x - e[0], y - e[1]
         r = ((qx * c + qy * s_) / e[3]) ** 2 + ((-qx * s_ + qy * c) / e[4]) ** 2 + ((z - e[2]) / e[5]) ** 2
@@ -167,6 +186,18 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, device):
+    """The largest value over all ranks (the job's time is its slowest replica's);
+    the value itself when not distributed."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -235,11 +266,7 @@ def run_gpu(args, w):
         barrier()
     launches = _lib.launch_count() - launches0
     total_ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms = total_ms / args.steps
     stage = np.array([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(nstage - 1)] for k in range(args.steps)])
     st = stage.mean(axis=0)  # filter, pack, bp, fp
@@ -354,9 +381,16 @@ def run_gpu(args, w):
                            "speedup_fdk": round(plain_ms / mms, 3), "rel_l2_vs_plain": rel}
             del pm
 
-    cgls = None
+    cgls = piccs = c1 = served = None
+    if w is WORKLOAD and not args.no_mixed:
+        c1 = c1_bench(dev, stream, barrier)
     if not args.no_cgls and w is WORKLOAD:
         cgls = irn_bench(dev, stream, barrier)
+        piccs = piccs_bench(dev, stream, barrier)
+    if not args.no_serve and w is WORKLOAD and world == 1:
+        del pipe, fpg, sgm, fp_out, dev_sgm, host_sgm, host_vol, host_fp
+        torch.cuda.empty_cache()
+        served = serve_bench(dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -381,7 +415,8 @@ def run_gpu(args, w):
             "fp_gups": round(nvox * w["views"] / (st[3] / 1e3) / 1e9, 2),
             "fp_samples_per_s": round(n_samples / (st[3] / 1e3), 1), "fp_in_volume_samples": n_samples,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clk.summary(), "mixed": mixed, "irn_cgls_tv": cgls,
+            "clocks": clk.summary(), "mixed": mixed, "irn_cgls_tv": cgls, "irn_cgls_piccs": piccs,
+            "fbp_2d_fan": c1, "serving": served,
         }
         print(json.dumps(line))
     if world > 1:
@@ -391,6 +426,46 @@ def run_gpu(args, w):
 
 C3 = dict(nu=1024, nv=64, views=360, nx=512, nz=64, du=0.8, dv=0.8, px=0.4, pz=0.4, sid=600.0, sdd=1100.0,
           step=0.2, n_ell=20, photons=1e5, seed=2025)
+# 2D fan-beam FBP: 256x256 at 0.5 mm, 720 views, 512 bins at 0.8 mm, SID 500 / SDD 1000, 10 ellipses
+C1 = dict(cone=False, nu=512, nv=1, views=720, nx=256, nz=1, du=0.8, dv=0.8, px=0.5, pz=0.5, sid=500.0,
+          sdd=1000.0, step=0.2, n_ell=10, photons=1e5, seed=2023)
+# IRN-CGLS-PICCS: 512x512x128 at 0.4 mm, 1024x128 detector; prior from 1440 views, target 90 views
+C4 = dict(nu=1024, nv=128, views=90, nx=512, nz=128, du=0.8, dv=0.8, px=0.4, pz=0.4, sid=600.0, sdd=1100.0,
+          step=0.2, n_ell=20, photons=1e5, seed=2026)
+
+
+def c1_bench(dev, stream, barrier, reps=50):
+    """2D fan-beam FBP, plain and mixed: GUPS, error vs plain and RMSE vs the phantom."""
+    import torch
+    from reconstruction_program_taichi_gb300 import fbp, geometry, ops
+    o = parse(C1)
+    out = {"config": "2D fan FBP 256x256 @0.5mm, 720 views, 512 bins @0.8mm, SID 500 SDD 1000, ramp x Hann, "
+                     "10 ellipses, Poisson 1e5"}
+    ph = phantom(C1, dev)
+    ref = None
+    for name, storage, impl in (("plain", "f32", "simt"), ("mixed", "bf16", "tc")):
+        pipe = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl=impl)
+        pipe.set_taps(hann_from_ramp(geometry.recon_taps(o)))
+        sgm = noisy(ops.project_ellipsoids(pipe.dg, ellipsoids(C1)), C1["photons"], C1["seed"])
+        for _ in range(5):
+            vol = pipe.run(sgm)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            vol = pipe.run(sgm)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / reps
+        live = vol != 0
+        r = {"ms": round(ms, 4), "gups": round(C1["nx"] ** 2 * C1["views"] / (ms / 1e3) / 1e9, 2),
+             "rmse_vs_phantom": rmse(vol, ph, live)}
+        if ref is None:
+            ref = vol.clone()
+        else:
+            r["rel_l2_vs_plain"] = float(torch.linalg.vector_norm(vol - ref) / torch.linalg.vector_norm(ref))
+        out[name] = r
+    return out
 
 
 def irn_bench(dev, stream, barrier):
@@ -438,6 +513,137 @@ def irn_bench(dev, stream, barrier):
     out["speedup_mixed"] = round(f["s_total"] / b["s_total"], 3)
     out["rmse_ratio_mixed"] = round(b["rmse_vs_phantom"] / f["rmse_vs_phantom"], 5)
     return out
+
+
+def piccs_bench(dev, stream, barrier):
+    """IRN-CGLS-PICCS (alpha 0.5, lambda 1e-3, 30 reweightings x 8 CG iterations) on
+    512x512x128 @0.4 mm with a 1024x128 detector: prior = FDK of 1440 views of phantom
+    A, target = 90 views of A plus 3 extra seeded ellipsoids; float32 and bf16 gather
+    storage; seconds and RMSE vs the target phantom."""
+    import torch
+    from reconstruction_program_taichi_gb300 import fbp, geometry, io, ops
+    from reconstruction_program_taichi_gb300.ir import Mgfbp_ir_piccs
+    w_prior = dict(C4, views=1440)
+    o = parse(w_prior)
+    pipe = fbp.FdkPipeline(o, device=dev)
+    pipe.set_taps(hann_from_ramp(geometry.recon_taps(o)))
+    ell_a = ellipsoids(C4)
+    prior = pipe.run(noisy(ops.project_ellipsoids(pipe.dg, ell_a), C4["photons"], C4["seed"])).clone()
+    del pipe
+    prior_file = os.path.join("/tmp", f"mandoct_bench_prior_{os.getpid()}.raw")
+    io.imwriteRaw(prior.cpu().numpy(), prior_file)
+    ell_t = np.concatenate([ell_a, ellipsoids(dict(C4, n_ell=3, seed=C4["seed"] + 1))])
+    truth = phantom(dict(C4), dev)
+    truth += phantom_from(ell_t[len(ell_a):], C4, dev)
+    out = {"config": "512x512x128 @0.4mm, 1024x128 det, target 90 views, prior FDK of 1440 views, alpha 0.5, "
+                     "lambda 1e-3, 30 IRN x 8 CG, Poisson 1e5",
+           "prior_rmse_vs_target": None}
+    n_ = C4["nx"]
+    yy, xx = torch.meshgrid(torch.arange(n_, device=dev) - (n_ - 1) / 2, torch.arange(n_, device=dev) - (n_ - 1) / 2,
+                            indexing="ij")
+    fov = (yy ** 2 + xx ** 2 <= (0.95 * n_ / 2) ** 2).expand_as(truth).contiguous()
+    out["prior_rmse_vs_target"] = rmse(prior, truth, fov)
+    try:
+        for storage in ("float32", "bfloat16"):
+            cfg = make_config(C4)
+            cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 30, "NumberOfIterations": 8,
+                        "Alpha": 0.5, "PriorImageFile": prior_file, "StoragePrecision": storage})
+            ir = Mgfbp_ir_piccs(cfg, device=dev, verbose=False)
+            sy = ir.system
+            sgm = noisy(ops.project_ellipsoids(sy.dg, ell_t), C4["photons"], C4["seed"] + 7)
+            pr = torch.from_numpy(ir.img_prior).to(dev)
+            sy.bpb = sy.bp_b(sgm)
+            sy.cgls(pr, [], [(1e-3, torch.ones_like(pr))], 2)  # warm-up
+            barrier()
+            calls0 = sy.ptp_calls
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            x = ir.solve_piccs(sgm, pr)
+            e1.record(stream)
+            barrier()
+            n = sy.ptp_calls - calls0
+            sec = e0.elapsed_time(e1) / 1e3
+            out[storage] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
+                            "rmse_vs_phantom": rmse(x, truth, fov), "finite": bool(torch.isfinite(x).all())}
+            del ir, sy, sgm, x, pr
+    finally:
+        os.remove(prior_file)
+    f, b = out["float32"], out["bfloat16"]
+    out["speedup_mixed"] = round(f["s_total"] / b["s_total"], 3)
+    out["rmse_ratio_mixed"] = round(b["rmse_vs_phantom"] / f["rmse_vs_phantom"], 5)
+    return out
+
+
+def serve_bench(dev, n_req=256, seed=7, mean_gap_ms=80.0):
+    """Serving stream: n_req requests with Poisson arrivals (seeded), mixing 2D fan FBP
+    (256^2-1024^2, 360-1440 views), cone-beam FDK (256^3-512^3, 360-1080 views) and
+    10-iteration CGLS at 256^3, under a 150 GB HBM budget; sinograms resident on the
+    device (as written by an acquisition pipeline), results returned as device tensors;
+    p50/p99 latency and GUPS."""
+    import torch
+    from reconstruction_program_taichi_gb300 import config, geometry, ops
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(seed)
+    classes = []
+    for n in (256, 512, 1024):
+        for v in (360, 720, 1440):
+            classes.append(("fbp", dict(C1, nx=n, px=128.0 / n, nu=2 * n, du=0.8 * 256 / n, views=v, seed=seed + n + v)))
+    for n, v in ((256, 360), (256, 1080), (512, 360), (512, 1080)):
+        classes.append(("fbp", dict(WORKLOAD, nx=n, nz=n, px=204.8 / n, pz=204.8 / n, nu=2 * n, nv=n,
+                                    du=0.8 * 512 / n, dv=0.8 * 512 / n, views=v, seed=seed + n + v)))
+    classes.append(("cgls", dict(WORKLOAD, nx=256, nz=256, px=0.8, pz=0.8, nu=512, nv=256, du=1.6, dv=1.6,
+                                 views=360, seed=seed + 1)))
+    weights = np.array([0.4 / 9] * 9 + [0.4 / 4] * 4 + [0.2])
+    # one noisy sinogram per class, made on the device and kept on the host
+    objs, sgms = [], []
+    for kind, w in classes:
+        o = parse(w)
+        if kind == "cgls":
+            config.parse_ir(o, {"Lambda": 1e-3})
+            dg = geometry.ir_geometry(o, dev)
+        else:
+            dg = geometry.fbp_geometry(o, dev)
+        sgms.append(noisy(ops.project_ellipsoids(dg, ellipsoids(w)), w["photons"], w["seed"]))
+        objs.append(o)
+        del dg
+    torch.cuda.empty_cache()
+    kinds = rng.choice(len(classes), size=n_req, p=weights / weights.sum())
+    gaps = rng.exponential(mean_gap_ms / 1e3, size=n_req)
+    x0 = {}
+    srv = ReconServer(device=dev, hbm_budget_gb=150.0, batch=4, max_slots_per_class=2)
+    t0 = time.perf_counter()
+    futs = []
+    for i, c in enumerate(kinds):
+        target = t0 + gaps[: i + 1].sum()
+        now = time.perf_counter()
+        if target > now:
+            time.sleep(target - now)
+        kind, w = classes[c]
+        if kind == "cgls":
+            if c not in x0:
+                x0[c] = torch.zeros((w["nz"], w["nx"], w["nx"]), dtype=torch.float32, device=dev)
+            futs.append(srv.submit_cgls(objs[c], sgms[c], x0[c], 10))
+        else:
+            futs.append(srv.submit_fbp(objs[c], sgms[c]))
+    ok = 0
+    for i, f in enumerate(futs):
+        f.result(timeout=600)
+        futs[i] = None  # drop the device result
+        ok += 1
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    counts = {"fbp_2d": int(sum(1 for c in kinds if c < 9)), "fdk": int(sum(1 for c in kinds if 9 <= c < 13)),
+              "cgls10": int(sum(1 for c in kinds if c == 13))}
+    return {"config": f"{n_req} requests, Poisson arrivals (mean gap {mean_gap_ms} ms), 2D FBP 256^2-1024^2 x "
+                      "360-1440 views, FDK 256^3-512^3 x 360-1080 views, CGLS-10 at 256^3; HBM budget 150 GB; "
+                      "batch 4, CUDA graphs",
+            "completed": ok, "mix": counts, "wall_s": round(wall, 3), "p50_ms": round(st["p50_ms"], 2),
+            "p99_ms": round(st["p99_ms"], 2), "mean_ms": round(st["mean_ms"], 2),
+            "queue_p50_ms": round(st["queue_p50_ms"], 2), "service_p50_ms": round(st["service_p50_ms"], 2),
+            "service_p99_ms": round(st["service_p99_ms"], 2), "gups": round(st["gups"], 2),
+            "slots": st["slots"], "classes": st["classes"], "evictions": st["evictions"],
+            "hbm_used_gb": round(st["hbm_used_gb"], 2)}
 
 
 # ---------------------------------------------------------------- CPU (reference) arm
@@ -538,6 +744,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cgls", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]

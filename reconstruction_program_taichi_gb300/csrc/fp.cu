@@ -222,6 +222,46 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         // reloaded only when the ray enters a new cell.
         int cell = -1;
         float2 e00 = make_float2(0.f, 0.f), e10 = e00, g00 = e00, g10 = e00;  // corners, x-differences
+        auto load_cell = [&](int off) {
+            if (off == cell) return;
+            cell = off;
+            if constexpr (ZP && std::is_same<ZT, uint4>::value) {
+                const uint4 q = __ldg(V2 + off);
+                e00 = bf16x2_to_float2(q.x);
+                g00 = bf16x2_to_float2(q.y);
+                e10 = bf16x2_to_float2(q.z);
+                g10 = bf16x2_to_float2(q.w);
+            } else if constexpr (ZP) {
+                const ZT* b2 = V2 + off;
+                e00 = ZPair<ZT>::load(b2);
+                const float2 e01 = ZPair<ZT>::load(b2 + sx);
+                e10 = ZPair<ZT>::load(b2 + sy);
+                const float2 e11 = ZPair<ZT>::load(b2 + sx + sy);
+                g00 = __fadd2_rn(e01, make_float2(-e00.x, -e00.y));
+                g10 = __fadd2_rn(e11, make_float2(-e10.x, -e10.y));
+            } else {
+                const float* b = V + off;
+                const float a00 = __ldg(b), a01 = __ldg(b + sx), a10 = __ldg(b + sy), a11 = __ldg(b + sx + sy);
+                float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+                if (CONE) {
+                    const float* c = b + plane;
+                    c00 = __ldg(c); c01 = __ldg(c + sx); c10 = __ldg(c + sy); c11 = __ldg(c + sx + sy);
+                }
+                e00 = make_float2(a00, c00);
+                e10 = make_float2(a10, c10);
+                g00 = __fadd2_rn(make_float2(a01, c01), make_float2(-a00, -c00));
+                g10 = __fadd2_rn(make_float2(a11, c11), make_float2(-a10, -c10));
+            }
+        };
+        // lower (.x) and upper (.y) z-plane bilinear values in packed f32x2 FMAs; per
+        // lane this is exactly fmaf(xw, a01 - a00, a00) etc.
+        auto interp = [&](float xw, float yw, float zw) -> float {
+            const float2 xw2 = make_float2(xw, xw), yw2 = make_float2(yw, yw);
+            const float2 l0 = __ffma2_rn(xw2, g00, e00);
+            const float2 l1 = __ffma2_rn(xw2, g10, e10);
+            const float2 pl = __ffma2_rn(yw2, __fadd2_rn(l1, make_float2(-l0.x, -l0.y)), l0);
+            return CONE ? fmaf(zw, pl.y - pl.x, pl.x) : pl.x;
+        };
         auto sample = [&](int k, bool check) {
             const float fk = (float)k;
             const float fx = fmaf(fk, r.dfx, r.fx0);
@@ -249,43 +289,8 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
                 zi = iv;
             }
             const int off = zi * plane + yi * sy + xi * sx;
-            if (off != cell) {
-                cell = off;
-                if constexpr (ZP && std::is_same<ZT, uint4>::value) {
-                    const uint4 q = __ldg(V2 + off);
-                    e00 = bf16x2_to_float2(q.x);
-                    g00 = bf16x2_to_float2(q.y);
-                    e10 = bf16x2_to_float2(q.z);
-                    g10 = bf16x2_to_float2(q.w);
-                } else if constexpr (ZP) {
-                    const ZT* b2 = V2 + off;
-                    e00 = ZPair<ZT>::load(b2);
-                    const float2 e01 = ZPair<ZT>::load(b2 + sx);
-                    e10 = ZPair<ZT>::load(b2 + sy);
-                    const float2 e11 = ZPair<ZT>::load(b2 + sx + sy);
-                    g00 = __fadd2_rn(e01, make_float2(-e00.x, -e00.y));
-                    g10 = __fadd2_rn(e11, make_float2(-e10.x, -e10.y));
-                } else {
-                    const float* b = V + off;
-                    const float a00 = __ldg(b), a01 = __ldg(b + sx), a10 = __ldg(b + sy), a11 = __ldg(b + sx + sy);
-                    float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
-                    if (CONE) {
-                        const float* c = b + plane;
-                        c00 = __ldg(c); c01 = __ldg(c + sx); c10 = __ldg(c + sy); c11 = __ldg(c + sx + sy);
-                    }
-                    e00 = make_float2(a00, c00);
-                    e10 = make_float2(a10, c10);
-                    g00 = __fadd2_rn(make_float2(a01, c01), make_float2(-a00, -c00));
-                    g10 = __fadd2_rn(make_float2(a11, c11), make_float2(-a10, -c10));
-                }
-            }
-            // lower (.x) and upper (.y) z-plane bilinear values in packed f32x2 FMAs;
-            // per lane this is exactly fmaf(xw, a01 - a00, a00) etc.
-            const float2 xw2 = make_float2(xw, xw), yw2 = make_float2(yw, yw);
-            const float2 l0 = __ffma2_rn(xw2, g00, e00);
-            const float2 l1 = __ffma2_rn(xw2, g10, e10);
-            const float2 pl = __ffma2_rn(yw2, __fadd2_rn(l1, make_float2(-l0.x, -l0.y)), l0);
-            const float val = CONE ? fmaf(zw, pl.y - pl.x, pl.x) : pl.x;
+            load_cell(off);
+            const float val = interp(xw, yw, zw);
             if (check) acc += ok ? val : 0.0f;
             else acc += val;
         };

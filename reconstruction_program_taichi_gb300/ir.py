@@ -69,9 +69,13 @@ class IrSystem:
         ops.pack_sinogram(self.dg, sgm, dtype=dtype, out=packed[dtype])
         return ops.bp_unmatched_packed(self.dg, packed[dtype], dtype=dtype, out=out)
 
-    def ptp(self, x, out=None):
-        """P^T P x (run_mgfbp_iterative_recon_IRN_CGLS.py:288-316)."""
+    def ptp(self, x, out=None, full_precision=False):
+        """P^T P x (run_mgfbp_iterative_recon_IRN_CGLS.py:288-316).  full_precision
+        forces float32 gathers whatever the storage precision."""
         self.ptp_calls += 1
+        if full_precision:
+            q = ops.fp(self.dg, x, mask=self.mask, out=self.fp_buf)
+            return self.bp(q, out=out, dtype=ops.MCT_F32)
         return self.bp(self.fp(x, out=self.fp_buf), out=out)
 
     def bp_b(self, sgm):
@@ -79,10 +83,7 @@ class IrSystem:
         data is packed at float32 whatever the storage precision: rounding b to bf16
         adds noise of the order of the photon noise, which the iterations would fit;
         only the operator applications inside CG use the reduced storage."""
-        out = self.bp(sgm * self.mask, dtype=ops.MCT_F32)
-        if self.dtype != ops.MCT_F32:  # the float32 operand is needed once per solve
-            self._packed.pop(ops.MCT_F32, None)
-        return out
+        return self.bp(sgm * self.mask, dtype=ops.MCT_F32)
 
     def dtwd_acc(self, x, wr, s, acc):
         """acc += s * D^T W D x (in place)."""
@@ -93,8 +94,13 @@ class IrSystem:
         """CG on (P^T P + sum_k s_k D^T W_k D) x = b' from x_seed, where
         b' = P^T b + sum (s, W, y) s * D^T W D y.  Follows TikhonovSol
         (run_mgfbp_iterative_recon_IRN_CGLS.py:188-232 and ..._piccs.py:112-145).
-        rhs_terms: list of (s, W, y); op_terms: list of (s, W)."""
-        d = self.ptp(x_seed)
+        rhs_terms: list of (s, W, y); op_terms: list of (s, W).
+        The initial residual uses float32 gathers whatever the storage precision: with a
+        warm start (the previous reweighting's solution, or the PICCS prior) P^T P x_seed
+        is of the size of P^T b, and rounding x_seed to bf16 would perturb the right-hand
+        side like measurement noise; the per-iteration products P^T P d use the storage
+        precision."""
+        d = self.ptp(x_seed, full_precision=True)
         torch.sub(self.bpb, d, out=d)  # d = P^T b - P^T P x0
         for s, w, y in rhs_terms:
             self.dtwd_acc(y, w, s, d)

@@ -15,6 +15,11 @@ Model
     a free slot; new slots are created while the HBM budget allows, and a slot is
     reused as soon as its previous batch finishes.  Batches on different slots run
     concurrently on their own streams.
+  * Slots are kept for reuse; when a request needs a new slot and the budget is
+    spent, idle slots of other classes are evicted, least recently used first.
+  * Inputs may be host arrays or CUDA tensors already resident on the device; the
+    result comes back in the same form (a new device tensor for device inputs, so
+    resident data never crosses the host link).
   * Results do not depend on the mix: every kernel is deterministic and a slot's
     graph always runs the same kernels on the same buffer layout.
 """
@@ -43,9 +48,16 @@ def _geom_key(obj, kind, extra=()):
     return (kind,) + g + tuple(extra)
 
 
+def _to_device(a, device):
+    """A host array or a tensor as a float32 tensor on device (no copy when it already is)."""
+    if isinstance(a, torch.Tensor):
+        return a.to(device=device, dtype=torch.float32)
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(device)
+
+
 class _Request:
     __slots__ = ("kind", "obj", "sgm", "x0", "n_iter", "storage", "key", "future", "t_arrive", "t_start",
-                 "t_done", "units")
+                 "t_done", "units", "on_device")
 
     def __init__(self, kind, obj, sgm, x0=None, n_iter=0, storage="f32"):
         self.kind, self.obj, self.sgm, self.x0, self.n_iter, self.storage = kind, obj, sgm, x0, n_iter, storage
@@ -56,6 +68,7 @@ class _Request:
         self.t_start = self.t_done = None
         nvox = obj.img_dim * obj.img_dim * obj.img_dim_z
         self.units = nvox * obj.view_num * (1 if kind == "fbp" else 2 * (n_iter + 1))
+        self.on_device = isinstance(sgm, torch.Tensor) and sgm.is_cuda
 
 
 class _FbpSlot:
@@ -74,6 +87,7 @@ class _FbpSlot:
         self.host_out = [torch.empty(self.pipes[0].dg.vol_shape, dtype=torch.float32, pin_memory=True)
                          for _ in range(batch)]
         self.graph = None
+        self.last_used = time.perf_counter()
         self.nbytes = sum(p.weighted.numel() * 4 + p.filtered.numel() * 4 + p.packed.numel() + p.vol.numel() * 4
                           for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
@@ -94,17 +108,26 @@ class _FbpSlot:
         self.graph = g
 
     def run(self, reqs):
+        dev_out = []
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
-                self.inp[i].copy_(torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)), non_blocking=False)
+                if r.on_device:
+                    self.inp[i].copy_(r.sgm)
+                else:
+                    self.inp[i].copy_(torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)))
             if self.graph is not None:
                 self.graph.replay()
             else:
                 self._body()
-            for i in range(len(reqs)):
-                self.host_out[i].copy_(self.out[i], non_blocking=True)
+            for i, r in enumerate(reqs):
+                if r.on_device:
+                    dev_out.append(self.out[i].clone())
+                else:
+                    dev_out.append(None)
+                    self.host_out[i].copy_(self.out[i], non_blocking=True)
         self.stream.synchronize()
-        return [self.host_out[i].numpy().copy() for i in range(len(reqs))]
+        self.last_used = time.perf_counter()
+        return [d if d is not None else self.host_out[i].numpy().copy() for i, d in enumerate(dev_out)]
 
 
 class _CglsSlot:
@@ -118,6 +141,7 @@ class _CglsSlot:
             self.sys = IrSystem(obj, device)
         self.obj = obj
         self.n_iter = n_iter
+        self.last_used = time.perf_counter()
         nvol = obj.img_dim * obj.img_dim * obj.img_dim_z
         self.nbytes = 8 * nvol * 4 + 3 * self.sys.fp_buf.numel() * 4
 
@@ -125,13 +149,15 @@ class _CglsSlot:
         r = reqs[0]
         obj = self.obj
         with torch.cuda.stream(self.stream):
-            sgm = torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)).to(self.sys.device)
-            x0 = torch.from_numpy(np.ascontiguousarray(r.x0, dtype=np.float32)).to(self.sys.device)
+            sgm = _to_device(r.sgm, self.sys.device)
+            x0 = _to_device(r.x0, self.sys.device)
             self.sys.bpb = self.sys.bp_b(sgm)
             wr = torch.ones_like(x0)
             lr = obj.coef_lambda * obj.pixel_count_ratio
             x = self.sys.cgls(x0, [], [(lr, wr)], self.n_iter)
-            out = x.cpu().numpy()
+            out = x if r.on_device else x.cpu().numpy()
+        self.stream.synchronize()
+        self.last_used = time.perf_counter()
         return [out]
 
 
@@ -153,6 +179,7 @@ class ReconServer:
         self.cv = threading.Condition()
         self.free_slots = {}    # key -> [slot]
         self.all_slots = {}     # key -> count
+        self.evictions = 0
         self.busy = 0
         self.done = []
         self.closed = False
@@ -163,11 +190,13 @@ class ReconServer:
 
     # ------------------------------------------------------------ API
     def submit_fbp(self, obj, sgm, storage="f32"):
-        """FBP/FDK of a host sinogram [rows, views, cols] for the parsed config obj."""
+        """FBP/FDK of a sinogram [rows, views, cols] (host array or CUDA tensor) for the
+        parsed config obj; the future's result is a host array or a new CUDA tensor."""
         return self._submit(_Request("fbp", obj, sgm, storage=storage))
 
     def submit_cgls(self, obj, sgm, x0, n_iter):
-        """n_iter CGLS iterations (Tikhonov-TV with unit weights) from x0."""
+        """n_iter CGLS iterations (Tikhonov-TV with unit weights) from x0 (host arrays
+        or CUDA tensors, as for submit_fbp)."""
         return self._submit(_Request("cgls", obj, sgm, x0=x0, n_iter=n_iter))
 
     def close(self, wait=True):
@@ -180,15 +209,23 @@ class ReconServer:
                 t.join()
 
     def stats(self):
-        lat = np.array([(r.t_done - r.t_arrive) * 1e3 for r in self.done]) if self.done else np.zeros(1)
-        t0 = min(r.t_arrive for r in self.done) if self.done else 0.0
-        t1 = max(r.t_done for r in self.done) if self.done else 1.0
-        units = sum(r.units for r in self.done)
-        return {"requests": len(self.done), "p50_ms": float(np.percentile(lat, 50)),
+        """Latency (arrival to result), its queueing and service parts, throughput."""
+        done = list(self.done)
+        lat = np.array([(r.t_done - r.t_arrive) * 1e3 for r in done]) if done else np.zeros(1)
+        wait = np.array([(r.t_start - r.t_arrive) * 1e3 for r in done]) if done else np.zeros(1)
+        serv = np.array([(r.t_done - r.t_start) * 1e3 for r in done]) if done else np.zeros(1)
+        t0 = min(r.t_arrive for r in done) if done else 0.0
+        t1 = max(r.t_done for r in done) if done else 1.0
+        units = sum(r.units for r in done)
+        slots = {}
+        for k, v in self.all_slots.items():
+            slots[k[0]] = slots.get(k[0], 0) + v
+        return {"requests": len(done), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                "gups": units / max(t1 - t0, 1e-9) / 1e9, "slots": dict((str(k[0]), v) for k, v in
-                                                                      self.all_slots.items()),
-                "hbm_used_gb": self.used / 1e9}
+                "queue_p50_ms": float(np.percentile(wait, 50)), "service_p50_ms": float(np.percentile(serv, 50)),
+                "service_p99_ms": float(np.percentile(serv, 99)),
+                "gups": units / max(t1 - t0, 1e-9) / 1e9, "slots": slots, "classes": len(self.all_slots),
+                "evictions": self.evictions, "hbm_used_gb": self.used / 1e9}
 
     # ------------------------------------------------------------ internals
     def _submit(self, req):
@@ -236,6 +273,8 @@ class ReconServer:
                     continue
                 need = self._estimate(head)
                 if self.used + need > self.budget:
+                    self._evict_idle(need, keep=key)
+                if self.used + need > self.budget:
                     if self.busy == 0 and not any(self.free_slots.values()):
                         head.future.set_exception(MemoryError("request exceeds the HBM budget"))
                         self.pending.pop(i)
@@ -259,6 +298,21 @@ class ReconServer:
             t.start()
             return True
         return False
+
+    def _evict_idle(self, need, keep):
+        """Release idle slots of other classes, least recently used first, until `need`
+        bytes fit in the budget (called with the lock held)."""
+        idle = [(s.last_used, k, s) for k, lst in self.free_slots.items() if k != keep for s in lst]
+        for _, k, s in sorted(idle, key=lambda t: t[0]):
+            if self.used + need <= self.budget:
+                break
+            self.free_slots[k].remove(s)
+            self.all_slots[k] -= 1
+            if self.all_slots[k] == 0:
+                del self.all_slots[k]
+            self.used -= s.nbytes
+            self.evictions += 1
+            del s
 
     def _run(self, slot, key, group):
         outs, err = None, None

@@ -116,6 +116,70 @@ IR_CASES = {
     "ir_piccs": _upd(BASE_IR, Alpha=0.5),
 }
 
+# FDK with projection matrices (run_mgfbp.py:549-627, 721-874, 1134-1141): the matrices
+# are synthesised from a circular geometry (see pmatrices()); "tilt" raises the source
+# path out of the z = 0 plane so that ModifyPMatrixToStandardForm has work to do.
+PM_CASES = {
+    "fdk_pmatrix": (_upd(BASE_CONE, DetectorOffsetHorizontal=0.0, DetectorOffsetVertical=0.0),
+                    dict(u_shift=0.3, v_shift=-0.2, tilt=0.0, scale=1.0)),
+    "fdk_pmatrix_standardise": (_upd(BASE_CONE, DetectorOffsetHorizontal=0.0, DetectorOffsetVertical=0.0,
+                                     ModifyPMatrixToStandardForm=True, PMatrixDetectorElementWidth=0.8,
+                                     PMatrixDetectorElementHeight=0.8, DetectorElementVerticalReconRange=[1, 12]),
+                                dict(u_shift=-0.4, v_shift=0.25, tilt=0.02, scale=0.5)),
+}
+
+
+def pmatrices(cfg, u_shift, v_shift, tilt, scale):
+    """3x4 matrices P_j = [e_u e_v d]^-1 [I | -s] of a circular scan: source s at angle
+    beta_j on a circle of radius SID (z = tilt * SID * sin(beta) when tilted), flat
+    detector at SDD with pixel vectors e_u, e_v (lengths = pixel size * scale, i.e. a
+    detector binned 1/scale relative to the scan) and the origin shifted by
+    (u_shift, v_shift) pixels.  Returned flattened, 12 values per view."""
+    nb, nu, nv = cfg["Views"], cfg["DetectorElementCountHorizontal"], cfg["DetectorElementCountVertical"]
+    sid, sdd = float(cfg["SourceIsocenterDistance"]), float(cfg["SourceDetectorDistance"])
+    du, dv = cfg["DetectorElementWidth"] * scale, cfg["DetectorElementHeight"] * scale
+    nu_p, nv_p = nu / scale, nv / scale
+    out = []
+    for j in range(nb):
+        b = 2 * np.pi * j / nb
+        c, s_ = np.cos(b), np.sin(b)
+        src = np.array([sid * c, sid * s_, tilt * sid * s_])
+        e_u = du * np.array([s_, -c, 0.0])
+        e_v = dv * np.array([0.0, 0.0, -1.0])
+        center = src - sdd * np.array([c, s_, tilt * s_]) / np.sqrt(1 + (tilt * s_) ** 2)
+        origin = center - ((nu_p - 1) / 2 + u_shift) * e_u - ((nv_p - 1) / 2 + v_shift) * e_v
+        m = np.linalg.inv(np.stack([e_u, e_v, origin - src], axis=1))
+        out.append(np.concatenate([m, (-m @ src)[:, None]], axis=1).reshape(-1))
+    return np.concatenate(out)
+
+
+def run_pmatrix_case(name, spec, R, rng):
+    cfg, geo = spec
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        pm = pmatrices(cfg, **geo)
+        path = os.path.join(d, "pmatrix.jsonc")
+        json.dump({"Value": [float(v) for v in pm]}, open(path, "w"))
+        cfg = dict(cfg, PMatrixFile=path)
+        out = run_fbp_case(name, cfg, R, rng)
+        out["pmatrix_input"] = pm
+        return out
+
+
+class _MathCompat:
+    """The math module with size-1 NumPy arrays accepted where scalars are expected."""
+
+    def __getattr__(self, name):
+        import math
+        f = getattr(math, name)
+        if not callable(f):
+            return f
+
+        def g(*a):
+            return f(*[float(np.asarray(x).reshape(-1)[0]) if isinstance(x, np.ndarray) and x.size == 1 else x
+                       for x in a])
+        return g
+
 
 def _clean(cfg):
     return {k: v for k, v in cfg.items() if v is not None}
@@ -169,6 +233,11 @@ def run_fbp_case(name, cfg, R, rng):
                    weighted=np.asarray(fbp.img_sgm, np.float64), filtered=_arr(fbp.img_sgm_filtered_taichi))
         if fbp.apply_gauss_vertical:
             out["gauss_v"] = _arr(fbp.array_kernel_gauss_vertical_taichi)
+        if getattr(fbp, "bool_apply_pmatrix", 0):
+            out["pmatrix"] = np.asarray(fbp.array_pmatrix, np.float64)
+            out["pm_params"] = np.array([fbp.source_isocenter_dis, fbp.source_det_dis, fbp.det_offset_horizontal,
+                                         fbp.det_offset_vertical, fbp.total_scan_angle, fbp.img_center_z],
+                                        np.float64)
         return out
 
 
@@ -268,9 +337,16 @@ def main():
     import run_mgfbp_iterative_recon_IRN_CGLS_piccs as RP
     import run_mgfpj as R1
     import run_mgfpj_v2 as R2
+    # NumPy >= 2 no longer turns size-1 arrays into Python scalars in math.cos & co.;
+    # the reference relies on that (run_mgfbp.py:738-741, on least-squares solutions of
+    # shape (3, 1)), so its modules get a math whose functions convert them first, as
+    # the NumPy of the reference's time did.
+    for mod in (R, R3, RI, RP, R1, R2):
+        if hasattr(mod, "math"):
+            mod.math = _MathCompat()
     jobs = [(k, v, "fbp") for k, v in FBP_CASES.items()] + [(k, v, "fpj") for k, v in FPJ_CASES.items()] \
         + [(k, v, "ir") for k, v in IR_CASES.items()] + [(k, v, "v1") for k, v in FPJ_V1_CASES.items()] \
-        + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()]
+        + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()] + [(k, v, "pm") for k, v in PM_CASES.items()]
     for i, (name, cfg, kind) in enumerate(jobs):
         if only and name not in only:
             continue
@@ -282,6 +358,8 @@ def main():
                 out = run_fbp_case(name, cfg, R, rng)
             elif kind == "fpj":
                 out = run_fpj_case(name, cfg, R3, rng)
+            elif kind == "pm":
+                out = run_pmatrix_case(name, cfg, R, rng)
             elif kind in ("v1", "v2"):
                 out = run_fpj_variant_case(name, cfg, R1 if kind == "v1" else R2, rng)
             else:

@@ -36,6 +36,9 @@ def _write_case(z, tmp_path, kind):
     if "prior" in z:
         z["prior"].astype(np.float32).tofile(tmp_path / "prior.raw")
         cfg["PriorImageFile"] = str(tmp_path / "prior.raw")
+    if "pmatrix_input" in z:
+        (tmp_path / "pmatrix.jsonc").write_text(json.dumps({"Value": [float(v) for v in z["pmatrix_input"]]}))
+        cfg["PMatrixFile"] = str(tmp_path / "pmatrix.jsonc")
     p = tmp_path / "config.jsonc"
     p.write_text(json.dumps(cfg))
     return str(p)

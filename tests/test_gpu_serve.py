@@ -58,3 +58,40 @@ def test_request_beyond_budget_is_refused(cuda):
     with pytest.raises(MemoryError):
         f.result(timeout=60)
     srv.close()
+
+
+def test_device_resident_requests_match_host_requests(cuda):
+    import torch
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(22)
+    o = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60)
+    s = rng.uniform(0, 1, (24, 60, 72)).astype(np.float32)
+    srv = ReconServer(batch=2, max_slots_per_class=1)
+    host = srv.submit_fbp(o, s).result(timeout=120)
+    dev = srv.submit_fbp(o, torch.from_numpy(s).cuda()).result(timeout=120)
+    srv.close()
+    assert isinstance(dev, torch.Tensor) and dev.is_cuda
+    assert np.array_equal(host, dev.cpu().numpy())
+
+
+def test_idle_slots_are_evicted_under_budget_pressure(cuda):
+    from reconstruction_program_taichi_gb300.serve import ReconServer, _Request
+    rng = np.random.default_rng(23)
+    objs = [_cone_obj(n=40, nz=16, nu=72, nv=24, views=60), _cone_obj(n=32, nz=8, nu=64, nv=16, views=45)]
+    sg = [rng.uniform(0, 1, (o.det_elem_count_vertical, o.view_num, o.det_elem_count_horizontal)).astype(np.float32)
+          for o in objs]
+    ref = []
+    srv = ReconServer(batch=1, max_slots_per_class=1)
+    for o, s in zip(objs, sg):
+        ref.append(srv.submit_fbp(o, s).result(timeout=120))
+    need = max(srv._estimate(_Request("fbp", o, s)) for o, s in zip(objs, sg))
+    srv.close()
+    # a budget that holds one slot at a time (the two slots together exceed it):
+    # alternating classes must evict
+    srv = ReconServer(hbm_budget_gb=need * 1.2 / 1e9, batch=1, max_slots_per_class=1)
+    outs = [srv.submit_fbp(objs[i % 2], sg[i % 2]).result(timeout=120) for i in range(4)]
+    st = srv.stats()
+    srv.close()
+    assert st["evictions"] >= 3
+    for i, out in enumerate(outs):
+        assert np.array_equal(out, ref[i % 2])

@@ -40,6 +40,9 @@ def test_fbp_oracle_matches_reference(name):
     else:
         taps = F.gaussian_apodized_ramp_taps(nu, du, c["GaussianApodizedRamp"], sdd, curved, c.get("DBTMode", False))
     assert rel_l2(taps, z["taps"]) < 1e-12
+    sid, cz, pm = c["SourceIsocenterDistance"], p["cz"], None
+    if "pmatrix" in z:  # parameters the reference derived from the projection matrices
+        sid, sdd, cz, pm = z["pm_params"][0], z["pm_params"][1], z["pm_params"][5], z["pmatrix"]
     sgm = z["input_sgm"].astype(np.float64)
     if p["rr"]:
         sgm = sgm[p["rr"][0]:p["rr"][1] + 1]
@@ -51,8 +54,8 @@ def test_fbp_oracle_matches_reference(name):
     assert rel_l2(filt, z["filtered"]) < 1e-12
     rec = F.fdk_bp(z["filtered"], z["angles"], z["u"], z["v"], nx=c["ImageDimension"], nz=p["nz"],
                    px=c["PixelSize"], pz=c.get("VoxelHeight", 0.0) if p["cone"] else 0.0,
-                   cx=c.get("ImageCenter", [0, 0])[0], cy=c.get("ImageCenter", [0, 0])[1], cz=p["cz"],
-                   sid=c["SourceIsocenterDistance"], sdd=sdd, dv=c.get("DetectorElementHeight", 0.0),
+                   cx=c.get("ImageCenter", [0, 0])[0], cy=c.get("ImageCenter", [0, 0])[1], cz=cz, pmatrix=pm,
+                   sid=sid, sdd=sdd, dv=c.get("DetectorElementHeight", 0.0),
                    img_rot=c.get("ImageRotation", 0) / 180 * PI, total_scan_angle=p["scan"], short_scan=p["short"],
                    cone_beam=p["cone"], curved=curved,
                    view_mode={"axial": 1, "coronal": 2, "sagittal": 3}[c.get("ReconViewMode", "axial")])
