@@ -127,10 +127,14 @@ int mct_filter_tc_status(const mct_geom* g, void* workspace, void* stream);
 /* Bytes of the packed backprojection operand for storage type dtype. */
 size_t mct_packed_size(const mct_geom* g, int32_t dtype);
 
-/* Pack a view-major filtered sinogram into the gather layout of mct_fdk_bp:
- * cone beam: per (view, row r<nv-1, col c<nu-1) the 2x2 bilinear stencil
- * {F[r][c], F[r][c+1], F[r+1][c], F[r+1][c+1]}; fan beam: per (view, row, col<nu-1)
- * the pair {F[r][c], F[r][c+1]}.  dtype MCT_F32 or MCT_BF16. */
+/* Pack a view-major filtered sinogram into the gather layout of mct_fdk_bp (buffer of
+ * mct_packed_size bytes, 16-byte aligned).  Cone beam: per (view, row r < nv, column
+ * c < nu-1) the bilinear coefficients {A, C-A, B-A, (D-C)-(B-A)} of the cell with
+ * corners A = F[r][c], B = F[r][c+1], C = F[r+1][c], D = F[r+1][c+1]; row nv-1 is NaN
+ * (an off-detector marker).  Fan beam: per (view, row, column c < nu-1) the pair
+ * {A, B-A}.  dtype MCT_F32, MCT_BF16, or MCT_F16: float16 values are stored times a
+ * power of two chosen from the input's largest magnitude (kept in the buffer's last
+ * 16 bytes), so any float32 range packs without overflow; the backprojectors undo it. */
 int mct_pack(const mct_geom* g, const float* filtered, void* packed, int32_t dtype, void* stream);
 
 /* mct_pack for a source with any (row, view) element strides: element (view j, row r,
@@ -165,14 +169,16 @@ int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float
            void* workspace, void* stream);
 
 /* Bytes of the mct_fp_storage workspace for dtype (MCT_F32: mct_fp_workspace_size;
- * MCT_BF16: two bf16 cell copies, 32 bytes per voxel; 0 if unsupported). */
+ * MCT_BF16 / MCT_F16: two 16-bit cell copies, 32 bytes per voxel (+16 for float16);
+ * 0 if unsupported). */
 size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype);
 
-/* mct_fp reading gather copies stored as dtype: MCT_F32 is mct_fp; MCT_BF16 (cone
- * beam, workspace of mct_fp_storage_workspace_size bytes required) stores every
- * voxel's whole 2x2x2 trilinear cell as 8 bf16 values, so a cell is one 16-byte
- * gather; the volume values are rounded to bf16, interpolation and sums stay
- * float32.  No counterpart in the reference (its projector is float32 only). */
+/* mct_fp reading gather copies stored as dtype: MCT_F32 is mct_fp; MCT_BF16 or MCT_F16
+ * (cone beam, workspace of mct_fp_storage_workspace_size bytes required) store every
+ * voxel's whole 2x2x2 trilinear cell as 8 16-bit values, so a cell is one 16-byte
+ * gather; the volume values are rounded to bf16 or (times a power of two chosen from
+ * the volume's largest magnitude) to float16; interpolation and sums stay float32.
+ * No counterpart in the reference (its projector is float32 only). */
 int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
                    void* workspace, int32_t dtype, void* stream);
 
@@ -214,7 +220,7 @@ int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sg
                          void* stream);
 
 /* The same operator reading the sinogram as packed stencils (mct_pack_strided of the
- * [nv][views][nu] sinogram, dtype MCT_F32 or MCT_BF16): one gather per voxel x view. */
+ * [nv][views][nu] sinogram, dtype MCT_F32, MCT_BF16 or MCT_F16): one gather per voxel x view. */
 int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
                                 float* vol, void* stream);
 

@@ -466,12 +466,12 @@ def parse_ir(self, cfg):
     if bp not in ("reference", "adjoint"):
         _err("BackProjector can only be reference or adjoint!")
     self.back_projector = bp
-    # storage of the operator gathers (an addition): "float32" (default) or "bfloat16"
-    # (bf16 volume gather copies in the FP, bf16 packed sinogram in the backprojector;
-    # all arithmetic, iterates and reductions stay float32 / float64)
+    # storage of the operator gathers (an addition): "float32" (default), "bfloat16" or
+    # "float16" (16-bit volume cells in the FP, 16-bit packed sinogram in the
+    # backprojector; all arithmetic, iterates and reductions stay float32 / float64)
     sp = cfg.get("StoragePrecision", "float32")
-    if sp not in ("float32", "bfloat16"):
-        _err("StoragePrecision can only be float32 or bfloat16!")
+    if sp not in ("float32", "bfloat16", "float16"):
+        _err("StoragePrecision can only be float32, bfloat16 or float16!")
     self.storage_precision = sp
 
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 #include <cstdio>
 
@@ -71,6 +72,60 @@ __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
 __device__ __forceinline__ float2 bf16x2_to_float2(uint32_t w) {
     return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
 }
+// ---- float16 storage with a power-of-two scale.
+// A float16 operand stores fp16(v * 2^e); e is chosen from the largest magnitude m of
+// the source so that m * 2^e lies in [2^12, 2^13): differences of up to four values (the
+// bilinear coefficients) stay below 2^15, inside fp16's range of 65504, and the
+// relative precision is fp16's 2^-11 for every value down to 2^-12 of the largest.
+// Readers multiply by 2^-e, which is exact.  m is reduced as float bits into a uint32
+// (non-negative floats order like unsigned integers) stored behind the operand.
+__device__ __forceinline__ int f16_scale_exp(uint32_t maxbits) {
+    const float m = __uint_as_float(maxbits);
+    if (!(m > 0.0f) || !(m <= 3.0e38f)) return 0;  // all zero, or inf/NaN in the source
+    return 12 - ilogbf(m);
+}
+struct __align__(8) h16x4 {  // four fp16: bilinear coefficients of one cell
+    uint32_t x, y;
+};
+struct h16x2 {  // two fp16: a column pair
+    uint32_t v;
+};
+struct __align__(16) h16x8 {  // eight fp16: a trilinear cell (forward projection)
+    uint32_t x, y, z, w;
+};
+__device__ __forceinline__ float2 h16x2_to_float2(uint32_t w) {
+    __half2 h;
+    *reinterpret_cast<uint32_t*>(&h) = w;
+    return __half22float2(h);
+}
+__device__ __forceinline__ uint32_t pack_h16x2(float lo, float hi) {
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+// The float16 operand's source maximum sits in the 16 bytes behind its body
+// (mct_packed_size includes them).
+inline uint32_t* f16_trailer(const mct_geom* g, const void* packed) {
+    const bool cone = (g->flags & MCT_CONE) != 0;
+    const size_t body = (size_t)g->views * g->nv * (g->nu - 1) * (cone ? 8 : 4);
+    return reinterpret_cast<uint32_t*>(static_cast<char*>(const_cast<void*>(packed)) + body);
+}
+template <typename T>
+struct IsF16 {
+    static constexpr bool value = false;
+};
+template <>
+struct IsF16<h16x4> {
+    static constexpr bool value = true;
+};
+template <>
+struct IsF16<h16x2> {
+    static constexpr bool value = true;
+};
+template <>
+struct IsF16<h16x8> {
+    static constexpr bool value = true;
+};
+
 template <typename QT>
 struct Quad;
 template <>
@@ -89,8 +144,22 @@ struct Quad<uint2> {
         hi = bf16x2_to_float2(q.y);
     }
 };
+template <>
+struct Quad<h16x4> {
+    static __device__ __forceinline__ void load(const h16x4* p, float2& lo, float2& hi) {
+        const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+        lo = h16x2_to_float2(q.x);
+        hi = h16x2_to_float2(q.y);
+    }
+};
 template <typename PT>
 struct Pair;
+template <>
+struct Pair<h16x2> {
+    static __device__ __forceinline__ float2 load(const h16x2* p) {
+        return h16x2_to_float2(__ldg(reinterpret_cast<const uint32_t*>(p)));
+    }
+};
 template <>
 struct Pair<float2> {
     static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }

@@ -52,7 +52,7 @@ struct BpParams {
 template <int MODE, bool CONE, typename QT, typename PT>
 __global__ void __launch_bounds__(BP_TX* BP_TY, bp_min_blocks<MODE, QT>())
 fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
-              const void* __restrict__ packed, float* __restrict__ vol) {
+              const void* __restrict__ packed, float* __restrict__ vol, const uint32_t* __restrict__ f16_max) {
     __shared__ float4 tab[BP_VCHUNK];  // {cos b, sin b, dbeta*div, unused}
     const int ix = blockIdx.x * BP_TX + threadIdx.x;
     const int iy = blockIdx.y * BP_TY + threadIdx.y;
@@ -71,6 +71,8 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     for (int k = 0; k < BP_ZC; ++k) acc[k] = 0.0f;
     uint32_t dead = 0;  // bit k: slice zb+k projected off the detector in some view
 
+    // float16 operands hold values scaled by 2^e: fold 2^-e (exact) into the view weight
+    const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
     for (int jc = 0; jc < p.views; jc += BP_VCHUNK) {
         const int nvc = min(BP_VCHUNK, p.views - jc);
         __syncthreads();
@@ -80,7 +82,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
             sincosf(angles[j] - p.img_rot, &s, &c);
             float db = (j == p.views - 1) ? fabsf(angles[p.views - 1] - angles[0]) / (p.views - 1)
                                           : fabsf(angles[j + 1] - angles[j]);
-            tab[q] = make_float4(c, s, db * p.div, 0.0f);
+            tab[q] = make_float4(c, s, db * p.div * unscale, 0.0f);
         }
         __syncthreads();
         if (!active || dead == 0xffffffffu) continue;
@@ -199,11 +201,13 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
 
 template <int MODE, bool CONE>
 void launch_bp(const BpParams& p, dim3 grid, dim3 block, cudaStream_t s, const float* angles, const float* pmat,
-               const void* packed, int dtype, float* vol) {
+               const void* packed, int dtype, float* vol, const uint32_t* f16_max) {
     if (dtype == MCT_BF16)
-        fdk_bp_kernel<MODE, CONE, uint2, uint32_t><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol);
+        fdk_bp_kernel<MODE, CONE, uint2, uint32_t><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol, nullptr);
+    else if (dtype == MCT_F16)
+        fdk_bp_kernel<MODE, CONE, h16x4, h16x2><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol, f16_max);
     else
-        fdk_bp_kernel<MODE, CONE, float4, float2><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol);
+        fdk_bp_kernel<MODE, CONE, float4, float2><<<grid, block, 0, s>>>(p, angles, pmat, packed, vol, nullptr);
 }
 
 }  // namespace
@@ -215,7 +219,8 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
                           void* stream) {
     MCT_TRY(check_geom(g, "mct_fdk_bp"));
     MCT_REQUIRE(t && t->angles && packed && vol, "mct_fdk_bp: NULL buffer");
-    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_fdk_bp: dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16 || dtype == MCT_F16,
+                "mct_fdk_bp: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
     const bool cone = (g->flags & MCT_CONE) != 0;
     const bool pm = (g->flags & MCT_PMATRIX) != 0;
     MCT_REQUIRE(!pm || (cone && t->pmatrix), "mct_fdk_bp: projection matrices need cone beam and the table");
@@ -264,10 +269,11 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     dim3 grid((g->nx + BP_TX - 1) / BP_TX, (g->nx + BP_TY - 1) / BP_TY, (g->nz + BP_ZC - 1) / BP_ZC);
     cudaStream_t s = as_stream(stream);
     const bool axial_fast = g->view_mode == 1 && !pm;
-    if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol);
-    else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
-    else if (axial_fast) launch_bp<0, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
-    else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
-    else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol);
+    const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
+    if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
+    else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
+    else if (axial_fast) launch_bp<0, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
+    else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
+    else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     return launched("fdk_bp_kernel");
 }

@@ -181,8 +181,16 @@ __device__ __forceinline__ uint2 make_quad<uint2>(float a, float b, float c, flo
     r.y = *reinterpret_cast<uint32_t*>(&hi);
     return r;
 }
+template <>
+__device__ __forceinline__ h16x4 make_quad<h16x4>(float a, float b, float c, float d) {
+    return h16x4{pack_h16x2(a, b), pack_h16x2(c, d)};
+}
 template <typename PT>
 __device__ __forceinline__ PT make_pair(float a, float b);
+template <>
+__device__ __forceinline__ h16x2 make_pair<h16x2>(float a, float b) {
+    return h16x2{pack_h16x2(a, b)};
+}
 template <>
 __device__ __forceinline__ float2 make_pair<float2>(float a, float b) { return make_float2(a, b); }
 template <>
@@ -202,6 +210,26 @@ template <>
 __device__ __forceinline__ float stored_base<float2>(float a) { return a; }
 template <>
 __device__ __forceinline__ float stored_base<uint32_t>(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
+template <>
+__device__ __forceinline__ float stored_base<h16x4>(float a) { return __half2float(__float2half_rn(a)); }
+template <>
+__device__ __forceinline__ float stored_base<h16x2>(float a) { return __half2float(__float2half_rn(a)); }
+
+// Largest |F| over a strided [rows][views][cols] source, as float bits, into *maxbits
+// (which the caller zeroes first); NaN counts as larger than every finite value.
+__global__ void absmax_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
+                              uint32_t* __restrict__ maxbits) {
+    const int64_t n = (int64_t)nv * views * nu;
+    uint32_t m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i % nu);
+        const int64_t rj = i / nu;
+        const int j = (int)(rj % views), r = (int)(rj / views);
+        m = max(m, __float_as_uint(F[r * rs + j * vs + c]) & 0x7fffffffu);
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, m);
+}
 
 // Source element (view j, row r, column c) is F[r*rs + j*vs + c].
 // cone: Q[j][r][c], r < nv, c < nu-1.  For r < nv-1 the bilinear coefficients of
@@ -214,8 +242,9 @@ __device__ __forceinline__ float stored_base<uint32_t>(float a) { return __bfloa
 // off-detector voxel ends up NaN and is written as 0.
 template <typename QT>
 __global__ void pack_quad_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
-                                 QT* __restrict__ Q) {
+                                 QT* __restrict__ Q, const uint32_t* __restrict__ maxbits) {
     const int nq = nu - 1, rq = nv;
+    const float sc = IsF16<QT>::value ? ldexpf(1.0f, f16_scale_exp(*maxbits)) : 1.0f;
     int64_t n = (int64_t)views * rq * nq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int c = (int)(i % nq);
@@ -228,7 +257,7 @@ __global__ void pack_quad_kernel(int nu, int nv, int views, int64_t rs, int64_t 
             continue;
         }
         const float* f = F + r * rs + j * vs + c;
-        const float a = stored_base<QT>(f[0]), b = f[1], cc = f[rs], d = f[rs + 1];
+        const float a = stored_base<QT>(f[0] * sc), b = f[1] * sc, cc = f[rs] * sc, d = f[rs + 1] * sc;
         const float bma = b - a, dmc = d - cc;
         Q[i] = make_quad<QT>(a, cc - a, bma, dmc - bma);
     }
@@ -237,8 +266,9 @@ __global__ void pack_quad_kernel(int nu, int nv, int views, int64_t rs, int64_t 
 // fan: P[j][r][c] = {A', F(j,r,c+1) - A'} with A' = F(j,r,c) as stored, c < nu-1
 template <typename PT>
 __global__ void pack_pair_kernel(int nu, int nv, int views, int64_t rs, int64_t vs, const float* __restrict__ F,
-                                 PT* __restrict__ P) {
+                                 PT* __restrict__ P, const uint32_t* __restrict__ maxbits) {
     const int nq = nu - 1;
+    const float sc = IsF16<PT>::value ? ldexpf(1.0f, f16_scale_exp(*maxbits)) : 1.0f;
     int64_t n = (int64_t)views * nv * nq;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int c = (int)(i % nq);
@@ -246,8 +276,8 @@ __global__ void pack_pair_kernel(int nu, int nv, int views, int64_t rs, int64_t 
         int r = (int)(jr % nv);
         int j = (int)(jr / nv);
         const float* f = F + r * rs + j * vs + c;
-        const float a = stored_base<PT>(f[0]);
-        P[i] = make_pair<PT>(a, f[1] - a);
+        const float a = stored_base<PT>(f[0] * sc);
+        P[i] = make_pair<PT>(a, f[1] * sc - a);
     }
 }
 
@@ -309,31 +339,54 @@ size_t mct_packed_size(const mct_geom* g, int32_t dtype) {
     // cone: 4 coefficients per (view, row incl. the NaN row nv-1, col < nu-1); fan: 2
     const bool cone = (g->flags & MCT_CONE) != 0;
     if (cone && g->nv < 2) return 0;
-    const size_t esz = (cone ? 2 : 1) * (dtype == MCT_BF16 ? 4 : 8);
-    return (size_t)g->views * g->nv * (g->nu - 1) * esz;
+    const size_t esz = (cone ? 2 : 1) * (dtype == MCT_F32 ? 8 : 4);
+    const size_t body = (size_t)g->views * g->nv * (g->nu - 1) * esz;
+    return dtype == MCT_F16 ? body + 16 : body;  // float16: the scale's source maximum behind the body
 }
 
 int mct_pack_strided(const mct_geom* g, const float* src, int64_t row_stride, int64_t view_stride, void* packed,
                      int32_t dtype, void* stream) {
     MCT_TRY(check_geom(g, "mct_pack"));
     MCT_REQUIRE(src && packed, "mct_pack: NULL buffer");
-    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_pack: dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16 || dtype == MCT_F16,
+                "mct_pack: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
+    MCT_REQUIRE(((uintptr_t)packed & 15) == 0, "mct_pack: packed buffer must be 16-byte aligned");
     cudaStream_t s = as_stream(stream);
     const int64_t rs = row_stride, vs = view_stride;
-    if (g->flags & MCT_CONE) {
-        MCT_REQUIRE(g->nv >= 2, "mct_pack: cone beam needs at least 2 detector rows");
-        int64_t n = (int64_t)g->views * g->nv * (g->nu - 1);
+    const bool cone = (g->flags & MCT_CONE) != 0;
+    MCT_REQUIRE(!cone || g->nv >= 2, "mct_pack: cone beam needs at least 2 detector rows");
+    const int64_t n = (int64_t)g->views * g->nv * (g->nu - 1);
+    uint32_t* maxbits = nullptr;
+    if (dtype == MCT_F16) {
+        maxbits = f16_trailer(g, packed);
+        cudaError_t e = cudaMemsetAsync(maxbits, 0, sizeof(uint32_t), s);
+        if (e != cudaSuccess) {
+            set_error("mct_pack: %s", cudaGetErrorString(e));
+            return MCT_E_CUDA;
+        }
+        absmax_kernel<<<grid_for(sgm_elems(*g)), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, maxbits);
+        MCT_TRY(launched("absmax_kernel"));
+    }
+    if (cone) {
         if (dtype == MCT_F32)
-            pack_quad_kernel<float4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float4*)packed);
+            pack_quad_kernel<float4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float4*)packed,
+                                                                 maxbits);
+        else if (dtype == MCT_BF16)
+            pack_quad_kernel<uint2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (uint2*)packed,
+                                                                maxbits);
         else
-            pack_quad_kernel<uint2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (uint2*)packed);
+            pack_quad_kernel<h16x4><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (h16x4*)packed,
+                                                                maxbits);
     } else {
-        int64_t n = (int64_t)g->views * g->nv * (g->nu - 1);
         if (dtype == MCT_F32)
-            pack_pair_kernel<float2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float2*)packed);
-        else
+            pack_pair_kernel<float2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (float2*)packed,
+                                                                 maxbits);
+        else if (dtype == MCT_BF16)
             pack_pair_kernel<uint32_t><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src,
-                                                                 (uint32_t*)packed);
+                                                                   (uint32_t*)packed, maxbits);
+        else
+            pack_pair_kernel<h16x2><<<grid_for(n), 256, 0, s>>>(g->nu, g->nv, g->views, rs, vs, src, (h16x2*)packed,
+                                                                maxbits);
     }
     return launched("pack_kernel");
 }

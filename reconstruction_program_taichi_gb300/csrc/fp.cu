@@ -196,7 +196,7 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
           const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
           const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
           const ZT* __restrict__ zp_x, const ZT* __restrict__ zp_y, const float* __restrict__ mask,
-          float* __restrict__ sgm) {
+          float* __restrict__ sgm, const uint32_t* __restrict__ f16_max) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.z * blockDim.y + threadIdx.y;
     const int j = blockIdx.y;
@@ -231,6 +231,12 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
                 g00 = bf16x2_to_float2(q.y);
                 e10 = bf16x2_to_float2(q.z);
                 g10 = bf16x2_to_float2(q.w);
+            } else if constexpr (ZP && std::is_same<ZT, h16x8>::value) {
+                const uint4 q = __ldg(reinterpret_cast<const uint4*>(V2 + off));
+                e00 = h16x2_to_float2(q.x);
+                g00 = h16x2_to_float2(q.y);
+                e10 = h16x2_to_float2(q.z);
+                g10 = h16x2_to_float2(q.w);
             } else if constexpr (ZP) {
                 const ZT* b2 = V2 + off;
                 e00 = ZPair<ZT>::load(b2);
@@ -301,6 +307,7 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         for (int k = kis; k <= kie; ++k) sample(k, false);
         for (int k = max(kie + 1, kis); k <= r.ke; ++k) sample(k, true);
     }
+    if constexpr (IsF16<ZT>::value) acc *= ldexpf(1.0f, -f16_scale_exp(*f16_max));  // float16 cells hold v * 2^e
     sgm[oidx] = acc * p.stepvd;
 }
 
@@ -329,29 +336,43 @@ __global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, ZT* __
     }
 }
 
-// bf16 cell copies (layout above): cx[z][y][x] and cy[z][x][y] both hold the cell at
+// Largest |v| of the volume as float bits into *maxbits (zeroed by the caller).
+__global__ void vol_absmax_kernel(int64_t n, const float* __restrict__ v, uint32_t* __restrict__ maxbits) {
+    uint32_t m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, __float_as_uint(v[i]) & 0x7fffffffu);
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, m);
+}
+
+// 16-bit cell copies (layout above; float16 cells hold v * 2^e, see f16_scale_exp): cx[z][y][x] and cy[z][x][y] both hold the cell at
 // voxel (z, y, x); corners outside the volume are 0 (no in-volume sample uses them).
 // 32x32 tiles, the transposed copy through shared memory.
-__global__ void cell_bf16_kernel(int nx, int nz, const float* __restrict__ v, uint4* __restrict__ cx,
-                                 uint4* __restrict__ cy) {
+template <bool F16>
+__global__ void cell16_kernel(int nx, int nz, const float* __restrict__ v, uint4* __restrict__ cx,
+                              uint4* __restrict__ cy, const uint32_t* __restrict__ f16_max) {
     __shared__ uint4 tile[32][33];
     const int64_t plane = (int64_t)nx * nx;
     const int z = blockIdx.z;
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const float sc = F16 ? ldexpf(1.0f, f16_scale_exp(*f16_max)) : 1.0f;
     auto at = [&](int zz, int yy, int xx) -> float {
-        return (zz < nz && yy < nx && xx < nx) ? v[zz * plane + (int64_t)yy * nx + xx] : 0.0f;
+        return (zz < nz && yy < nx && xx < nx) ? v[zz * plane + (int64_t)yy * nx + xx] * sc : 0.0f;
     };
-    auto rb = [](float a) { return __bfloat162float(__float2bfloat16_rn(a)); };
+    auto rb = [](float a) {
+        return F16 ? __half2float(__float2half_rn(a)) : __bfloat162float(__float2bfloat16_rn(a));
+    };
+    auto pk = [](float lo, float hi) { return F16 ? pack_h16x2(lo, hi) : pack_bf16x2(lo, hi); };
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
         const int y = y0 + i, x = x0 + threadIdx.x;
         if (y < nx && x < nx) {
             const float a0 = rb(at(z, y, x)), a1 = rb(at(z + 1, y, x));
             const float c0 = rb(at(z, y + 1, x)), c1 = rb(at(z + 1, y + 1, x));
             uint4 q;
-            q.x = pack_bf16x2(a0, a1);
-            q.y = pack_bf16x2(at(z, y, x + 1) - a0, at(z + 1, y, x + 1) - a1);
-            q.z = pack_bf16x2(c0, c1);
-            q.w = pack_bf16x2(at(z, y + 1, x + 1) - c0, at(z + 1, y + 1, x + 1) - c1);
+            q.x = pk(a0, a1);
+            q.y = pk(at(z, y, x + 1) - a0, at(z + 1, y, x + 1) - a1);
+            q.z = pk(c0, c1);
+            q.w = pk(at(z, y + 1, x + 1) - c0, at(z + 1, y + 1, x + 1) - c1);
             cx[z * plane + (int64_t)y * nx + x] = q;
             tile[i][threadIdx.x] = q;
         }
@@ -642,9 +663,10 @@ size_t mct_fp_workspace_size(const mct_geom* g) {
 
 size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype) {
     if (!g || g->nx < 1 || g->nz < 1) return 0;
-    if (dtype != MCT_BF16) return mct_fp_workspace_size(g);
-    if (!(g->flags & MCT_CONE)) return 0;
-    return 2 * (size_t)g->nz * g->nx * g->nx * sizeof(uint4);  // two bf16 cell copies
+    if (dtype == MCT_F32) return mct_fp_workspace_size(g);
+    if (!(g->flags & MCT_CONE) || (dtype != MCT_BF16 && dtype != MCT_F16)) return 0;
+    // two 16-bit cell copies (+16 bytes for the float16 scale's source maximum)
+    return 2 * (size_t)g->nz * g->nx * g->nx * sizeof(uint4) + (dtype == MCT_F16 ? 16 : 0);
 }
 
 int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
@@ -655,8 +677,9 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp: projection-matrix tables missing");
     MCT_REQUIRE(workspace != (void*)vol, "mct_fp: workspace aliases the volume");
     MCT_REQUIRE(((uintptr_t)workspace & 15) == 0, "mct_fp: workspace must be 16-byte aligned");
-    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_fp: dtype must be MCT_F32 or MCT_BF16");
-    MCT_REQUIRE(dtype == MCT_F32 || (p.cone && workspace), "mct_fp: bf16 storage needs cone beam and a workspace");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16 || dtype == MCT_F16,
+                "mct_fp: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
+    MCT_REQUIRE(dtype == MCT_F32 || (p.cone && workspace), "mct_fp: 16-bit storage needs cone beam and a workspace");
     cudaStream_t s = as_stream(stream);
     dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
     dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
@@ -664,17 +687,34 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
     if (p.cone && workspace && dtype == MCT_BF16) {
         uint4* cx = static_cast<uint4*>(workspace);
         uint4* cy = cx + n;
-        cell_bf16_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy);
-        MCT_TRY(launched("cell_bf16_kernel"));
+        cell16_kernel<false><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy, nullptr);
+        MCT_TRY(launched("cell16_kernel"));
         fp_kernel<true, true, uint4><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
-                                                            nullptr, cx, cy, mask, sgm);
+                                                            nullptr, cx, cy, mask, sgm, nullptr);
+    } else if (p.cone && workspace && dtype == MCT_F16) {
+        uint4* cx = static_cast<uint4*>(workspace);
+        uint4* cy = cx + n;
+        uint32_t* vmax = reinterpret_cast<uint32_t*>(cy + n);
+        cudaError_t e = cudaMemsetAsync(vmax, 0, sizeof(uint32_t), s);
+        if (e != cudaSuccess) {
+            set_error("mct_fp: %s", cudaGetErrorString(e));
+            return MCT_E_CUDA;
+        }
+        const int64_t blocks = ((int64_t)n + 255) / 256;
+        vol_absmax_kernel<<<(int)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, s>>>((int64_t)n, vol, vmax);
+        MCT_TRY(launched("vol_absmax_kernel"));
+        cell16_kernel<true><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy, vmax);
+        MCT_TRY(launched("cell16_kernel"));
+        fp_kernel<true, true, h16x8><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
+                                                            nullptr, reinterpret_cast<const h16x8*>(cx),
+                                                            reinterpret_cast<const h16x8*>(cy), mask, sgm, vmax);
     } else if (p.cone && workspace) {
         float2* zx = static_cast<float2*>(workspace);
         float2* zy = zx + n;
         zpair_kernel<float2><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
         MCT_TRY(launched("zpair_kernel"));
         fp_kernel<true, true, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
-                                                             vol, nullptr, zx, zy, mask, sgm);
+                                                             vol, nullptr, zx, zy, mask, sgm, nullptr);
     } else {
         float* vt = static_cast<float*>(workspace);
         if (vt) {
@@ -683,10 +723,12 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
         }
         if (p.cone)
             fp_kernel<true, false, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a,
-                                                                  t->pmat_xs, vol, vt, nullptr, nullptr, mask, sgm);
+                                                                  t->pmat_xs, vol, vt, nullptr, nullptr, mask, sgm,
+                                                                  nullptr);
         else
             fp_kernel<false, false, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a,
-                                                                   t->pmat_xs, vol, vt, nullptr, nullptr, mask, sgm);
+                                                                   t->pmat_xs, vol, vt, nullptr, nullptr, mask, sgm,
+                                                                   nullptr);
     }
     return launched("fp_kernel");
 }

@@ -25,13 +25,14 @@ struct UbParams {
 };
 
 // All views of the per-view backprojector, accumulated in registers in view order.
-// SRC 0 reads the plain sinogram [nv][views][nu] (4 gathers per update); SRC 1 / 2
-// read the packed bilinear coefficients of mct_pack_strided (one 16-byte float32 or
-// 8-byte bf16 gather per update; the same bilinear value up to float32 rounding).
+// SRC 0 reads the plain sinogram [nv][views][nu] (4 gathers per update); SRC 1 reads
+// the packed bilinear coefficients of mct_pack_strided (one 16-byte float32 or 8-byte
+// bf16 / float16 gather per update; the same bilinear value up to float32 rounding).
 template <int SRC, typename QT, typename PT>
 __global__ void __launch_bounds__(UB_TX* UB_TY)
 bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
-                    const float* __restrict__ sgm, const void* __restrict__ packed, float* __restrict__ vol) {
+                    const float* __restrict__ sgm, const void* __restrict__ packed, float* __restrict__ vol,
+                    const uint32_t* __restrict__ f16_max) {
     const int nq = p.nu - 1;  // packed: nv rows of nu-1 stencils per view
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, unused}
     const int ix = blockIdx.x * UB_TX + threadIdx.x;
@@ -120,9 +121,11 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
     }
     if (!active) return;
     const int64_t plane = (int64_t)p.nx * p.nx;
+    const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
 #pragma unroll
     for (int k = 0; k < UB_ZC; ++k)
-        if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = ((trunc >> k) & 1u) ? 0.0f : acc[k];
+        if (zb + k < p.nz)
+            vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = ((trunc >> k) & 1u) ? 0.0f : acc[k] * unscale;
 }
 
 // Axial view mode over packed coefficients.  For a voxel column (x, y) the rotation,
@@ -137,7 +140,8 @@ constexpr int UA_ZC = 16;
 template <bool CONE, typename QT, typename PT>
 __global__ void __launch_bounds__(UB_TX* UB_TY)
 bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
-                          const void* __restrict__ packed, float* __restrict__ vol) {
+                          const void* __restrict__ packed, float* __restrict__ vol,
+                          const uint32_t* __restrict__ f16_max) {
     const int nq = p.nu - 1;  // packed: nv rows of nu-1 coefficient sets per view
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, sid*cos b}
     __shared__ float tab_s[UB_VCHUNK];  // sid*sin b
@@ -220,9 +224,10 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
     }
     if (!active) return;
     const int64_t plane = (int64_t)p.nx * p.nx;
+    const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
 #pragma unroll
     for (int k = 0; k < UA_ZC; ++k)
-        if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = trunc ? 0.0f : acc[k];
+        if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = trunc ? 0.0f : acc[k] * unscale;
 }
 
 // Forward differences (y, x, z) with zero at the far edge; z only when nz > 2.
@@ -366,6 +371,25 @@ inline int ew_grid(int64_t n) {
 
 using namespace mct;
 
+template <typename QT, typename PT>
+void launch_unmatched_packed(const mct_geom* g, const UbParams& p, const mct_tables* t, const void* packed,
+                                    float* vol, const uint32_t* f16_max, cudaStream_t s) {
+    dim3 block(UB_TX, UB_TY);
+    if (g->view_mode == 1) {
+        dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UA_ZC - 1) / UA_ZC);
+        if (p.cone)
+            bp_unmatched_axial_kernel<true, QT, PT><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed, vol,
+                                                                           f16_max);
+        else
+            bp_unmatched_axial_kernel<false, QT, PT><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed, vol,
+                                                                            f16_max);
+    } else {
+        dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
+        bp_unmatched_kernel<1, QT, PT><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, nullptr, packed, vol,
+                                                              f16_max);
+    }
+}
+
 extern "C" {
 
 static int unmatched_params(const mct_geom* g, UbParams& p);
@@ -377,7 +401,7 @@ int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sg
     dim3 block(UB_TX, UB_TY);
     dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
     bp_unmatched_kernel<0, float4, float2><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz, sgm,
-                                                                                  nullptr, vol);
+                                                                                  nullptr, vol, nullptr);
     return launched("bp_unmatched_kernel");
 }
 
@@ -386,32 +410,16 @@ int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const vo
     UbParams p{};
     MCT_TRY(unmatched_params(g, p));
     MCT_REQUIRE(t && t->angles && packed && vol, "mct_bp_ref_unmatched_packed: NULL buffer");
-    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_bp_ref_unmatched_packed: dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16 || dtype == MCT_F16,
+                "mct_bp_ref_unmatched_packed: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
     MCT_REQUIRE((int64_t)g->nv * (g->nu - 1) < ((int64_t)1 << 31), "mct_bp_ref_unmatched_packed: detector too large");
-    dim3 block(UB_TX, UB_TY);
     cudaStream_t s = as_stream(stream);
-    if (g->view_mode == 1) {
-        dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UA_ZC - 1) / UA_ZC);
-        const bool bf = dtype == MCT_BF16;
-        if (p.cone && bf)
-            bp_unmatched_axial_kernel<true, uint2, uint32_t><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed, vol);
-        else if (p.cone)
-            bp_unmatched_axial_kernel<true, float4, float2><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed, vol);
-        else if (bf)
-            bp_unmatched_axial_kernel<false, uint2, uint32_t><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed,
-                                                                                    vol);
-        else
-            bp_unmatched_axial_kernel<false, float4, float2><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz, packed,
-                                                                                   vol);
-        return launched("bp_unmatched_axial_kernel");
-    }
-    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
     if (dtype == MCT_F32)
-        bp_unmatched_kernel<1, float4, float2><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz,
-                                                                                      nullptr, packed, vol);
+        launch_unmatched_packed<float4, float2>(g, p, t, packed, vol, nullptr, s);
+    else if (dtype == MCT_BF16)
+        launch_unmatched_packed<uint2, uint32_t>(g, p, t, packed, vol, nullptr, s);
     else
-        bp_unmatched_kernel<2, uint2, uint32_t><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz,
-                                                                                       nullptr, packed, vol);
+        launch_unmatched_packed<h16x4, h16x2>(g, p, t, packed, vol, f16_trailer(g, packed), s);
     return launched("bp_unmatched_kernel");
 }
 

@@ -14,12 +14,13 @@ import numpy as np
 import torch
 
 from . import ops
-from ._lib import MCT_BF16, MCT_F32
+from ._lib import MCT_BF16, MCT_F16, MCT_F32
 from .config import ConfigError, ReadConfigFile, parse_fbp
 from .geometry import fbp_geometry, gaussian_taps, recon_taps
 from .io import imwriteRaw, imwriteTiff, read_sinogram_file, read_sinogram_raw_layout
 
-STORAGE = {"f32": MCT_F32, "float32": MCT_F32, "bf16": MCT_BF16, "bfloat16": MCT_BF16}
+STORAGE = {"f32": MCT_F32, "float32": MCT_F32, "bf16": MCT_BF16, "bfloat16": MCT_BF16, "f16": MCT_F16,
+           "float16": MCT_F16}
 
 
 def _device(device=None):

@@ -39,11 +39,12 @@ class IrSystem:
         self.device = self.dg.device
         self.matched = getattr(obj, "back_projector", "reference") == "adjoint"
         storage = storage or getattr(obj, "storage_precision", "float32")
-        if storage not in ("float32", "bfloat16"):
-            raise ValueError("storage must be float32 or bfloat16")
-        # bf16 gathers: FP volume copies (cone beam) and the packed sinogram of the
+        kinds = {"float32": ops.MCT_F32, "bfloat16": ops.MCT_BF16, "float16": ops.MCT_F16}
+        if storage not in kinds:
+            raise ValueError("storage must be float32, bfloat16 or float16")
+        # 16-bit gathers: FP volume cells (cone beam) and the packed sinogram of the
         # reference backprojector; the exact adjoint scatters float32 either way
-        self.dtype = ops.MCT_BF16 if storage == "bfloat16" else ops.MCT_F32
+        self.dtype = kinds[storage]
         self.fp_dtype = self.dtype if self.dg.geom.flags & ops.MCT_CONE else ops.MCT_F32
         self.mask = ops.effective_map(self.dg)
         f32 = dict(dtype=torch.float32, device=self.device)

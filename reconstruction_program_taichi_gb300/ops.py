@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import MCT_BF16, MCT_CONE, MCT_F32, Geom, Tables
+from ._lib import MCT_BF16, MCT_CONE, MCT_F16, MCT_F32, Geom, Tables
 
 
 def _ptr(t):
@@ -201,8 +201,8 @@ def fp_workspace(dg, dtype=MCT_F32):
 
 def fp(dg, vol, mask=None, out=None, workspace=True, dtype=MCT_F32):
     """P vol.  workspace=True uses the geometry's cached gather-copy buffer (coalesced
-    gathers for every view); None runs without it.  dtype=MCT_BF16 (cone beam) stores
-    the gather copies as bf16 (mct_fp_storage)."""
+    gathers for every view); None runs without it.  dtype=MCT_BF16 or MCT_F16 (cone
+    beam) stores the gather copies as 16-bit cells (mct_fp_storage)."""
     _check(vol, "vol", dg.vol_shape)
     if mask is not None:
         _check(mask, "mask", dg.sgm_shape)

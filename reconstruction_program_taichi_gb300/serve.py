@@ -239,16 +239,28 @@ class ReconServer:
     def _make_slot(self, req):
         torch.cuda.set_device(self.device)
         if req.kind == "fbp":
-            return _FbpSlot(req.obj, self.batch, req.storage, self.device, self.use_graphs)
+            return _FbpSlot(req.obj, self._batch_for(req), req.storage, self.device, self.use_graphs)
         return _CglsSlot(req.obj, req.n_iter, self.device)
 
-    def _estimate(self, req):
+    @staticmethod
+    def _per_request_bytes(req):
         o = req.obj
         nvol = o.img_dim * o.img_dim * o.img_dim_z * 4
         nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
         if req.kind == "fbp":
-            return self.batch * (nsgm * 7 + 2 * nvol)
+            return nsgm * 7 + 2 * nvol
         return 8 * nvol + 3 * nsgm
+
+    def _batch_for(self, req):
+        """Requests per FBP slot: `batch`, reduced so that one slot takes at most an
+        eighth of the budget (large geometries get small slots, so that several classes
+        stay resident)."""
+        if req.kind != "fbp":
+            return 1
+        return max(1, min(self.batch, int(self.budget / 8 // max(self._per_request_bytes(req), 1))))
+
+    def _estimate(self, req):
+        return self._batch_for(req) * self._per_request_bytes(req)
 
     def _schedule(self):
         while True:

@@ -131,16 +131,21 @@ def test_fdk_ops_vs_oracle(kw, cuda):
     assert rel_l2(vol[keep], ref[keep]) < TOL
 
 
-def test_fdk_bf16_storage_error_is_small(cuda):
+@pytest.mark.parametrize("storage,tol", [("bf16", 5e-3), ("f16", 8e-4)])
+@pytest.mark.parametrize("scale", [1.0, 1e6, 1e-6])
+def test_fdk_16bit_storage_error_is_small(storage, tol, scale, cuda):
+    """16-bit backprojection operands; float16 is stored with a power-of-two scale, so
+    its error does not depend on the data's magnitude (no overflow at 1e6)."""
     import torch
     from reconstruction_program_taichi_gb300 import fbp
     o = _cone_obj()
     rng = np.random.default_rng(6)
-    sgm = torch.from_numpy(rng.uniform(0, 1, (o.det_elem_count_vertical, o.view_num,
-                                              o.det_elem_count_horizontal)).astype(np.float32)).cuda()
+    sgm = torch.from_numpy(scale * rng.uniform(0, 1, (o.det_elem_count_vertical, o.view_num,
+                                                      o.det_elem_count_horizontal)).astype(np.float32)).cuda()
     a = fbp.FdkPipeline(o, storage="f32").run(sgm).cpu().numpy()
-    b = fbp.FdkPipeline(o, storage="bf16").run(sgm).cpu().numpy()
-    assert rel_l2(b, a) < 5e-3
+    b = fbp.FdkPipeline(o, storage=storage).run(sgm).cpu().numpy()
+    assert np.array_equal(a == 0, b == 0)
+    assert rel_l2(b, a) < tol
 
 
 @pytest.mark.parametrize("kw", [{}, {"CurvedDetector": True}, {"HelicalPitch": 0.7, "TotalScanAngle": 720},
@@ -325,7 +330,7 @@ def test_fp_bf16_storage_error_is_small(cuda):
     stays far below that, and which rays are zero is unchanged."""
     import torch
     from reconstruction_program_taichi_gb300 import geometry, ops
-    from reconstruction_program_taichi_gb300._lib import MCT_BF16
+    from reconstruction_program_taichi_gb300._lib import MCT_BF16, MCT_F16
     o = _cone_obj(views=60)
     dg = geometry.fpj_geometry(o)
     vol = torch.from_numpy(_smooth(np.random.default_rng(9), o.img_dim_z, o.img_dim)).cuda()
@@ -333,6 +338,11 @@ def test_fp_bf16_storage_error_is_small(cuda):
     b = ops.fp(dg, vol, dtype=MCT_BF16)
     assert torch.equal(a == 0, b == 0)
     assert float((a - b).norm() / a.norm()) < 2e-3
+    # float16 cells with the power-of-two scale: ~8x smaller error at any magnitude
+    for scale in (1.0, 1e6, 1e-6):
+        c = ops.fp(dg, vol * scale, dtype=MCT_F16) / scale
+        assert torch.equal(a == 0, c == 0)
+        assert float((a - c).norm() / a.norm()) < 3e-4
     # with a bf16-representable volume only the rounded differences remain
     vb = vol.to(torch.bfloat16).float()
     ab, bb = ops.fp(dg, vb), ops.fp(dg, vb, dtype=MCT_BF16)
@@ -343,7 +353,7 @@ def test_fp_bf16_storage_error_is_small(cuda):
 def test_packed_unmatched_bp_bf16_error_is_small(cone, cuda):
     import torch
     from reconstruction_program_taichi_gb300 import config, geometry, ops
-    from reconstruction_program_taichi_gb300._lib import MCT_BF16
+    from reconstruction_program_taichi_gb300._lib import MCT_BF16, MCT_F16
     kw = {} if cone else {"ConeBeam": False, "DetectorElementCountVertical": 6, "ImageDimensionZ": 6}
     o = _cone_obj(n=40, nz=12, nu=64, nv=20, views=36, DetectorElementHeight=1.2, **kw)
     config.parse_ir(o, {"Lambda": 1e-3})
@@ -354,3 +364,7 @@ def test_packed_unmatched_bp_bf16_error_is_small(cone, cuda):
     b = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm, dtype=MCT_BF16), dtype=MCT_BF16)
     assert torch.equal(a == 0, b == 0)
     assert float((a - b).norm() / a.norm()) < 5e-3
+    for scale in (1.0, 1e7):
+        c = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm * scale, dtype=MCT_F16), dtype=MCT_F16) / scale
+        assert torch.equal(a == 0, c == 0)
+        assert float((a - c).norm() / a.norm()) < 8e-4
