@@ -224,7 +224,7 @@ def run_gpu(args, w):
     ell = ellipsoids(w)
     sgm = noisy(ops.project_ellipsoids(pipe.dg, ell), w["photons"], w["seed"])
     fp_out = torch.empty(fpg.sgm_shape, dtype=torch.float32, device=dev)
-    fp_dtype = ops.MCT_BF16 if args.storage == "bf16" else ops.MCT_F32
+    fp_dtype = {"f32": ops.MCT_F32, "bf16": ops.MCT_BF16, "f16": ops.MCT_F16}[args.storage]
     stream = torch.cuda.current_stream(dev)
 
     def step(evs=None):
@@ -277,8 +277,8 @@ def run_gpu(args, w):
     # roofline of the dominant kernel (bp or fp), algorithmic bytes per launch
     hbm, _, peak_kind = peaks()
     n_samples = ops.fp_count_samples(fpg)
-    bp_bytes = nvox * w["views"] * (8 if pipe.dtype == 1 else 16) + nvox * 4
-    fp_bytes = n_samples * (16 if fp_dtype == ops.MCT_BF16 else 32) + fpg.geom.nv * fpg.geom.views * fpg.geom.nu * 4
+    bp_bytes = nvox * w["views"] * (16 if pipe.dtype == ops.MCT_F32 else 8) + nvox * 4
+    fp_bytes = n_samples * (32 if fp_dtype == ops.MCT_F32 else 16) + fpg.geom.nv * fpg.geom.views * fpg.geom.nu * 4
     dom = "fp_kernel" if st[3] >= st[2] else "fdk_bp_kernel"
     dom_ms, dom_bytes = (st[3], fp_bytes) if dom == "fp_kernel" else (st[2], bp_bytes)
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
@@ -401,7 +401,7 @@ def run_gpu(args, w):
             "metric": "GUPS (cone-beam FDK + forward projection, voxel x view updates per second)",
             "value": round(value, 3), "unit": "GUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if args.storage == "f32" else "bf16-storage/f32-compute",
+            "vs_baseline": None, "dtype": "f32" if args.storage == "f32" else f"{args.storage}-storage/f32-compute",
             "data": "synthetic: 20 seeded ellipsoids, exact line integrals, Poisson noise at 1e5 photons",
             "config": {"workload": f"FDK+FP {w['nx']}x{w['nx']}x{w['nz']} vol @{w['px']}mm, {w['views']} views/360deg, "
                                    f"{w['nu']}x{w['nv']} flat det @{w['du']}mm, SID {w['sid']:.0f} SDD {w['sdd']:.0f}",
@@ -740,7 +740,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--storage", default="f32", choices=["f32", "bf16"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
                     help="c2: the benchmark; small: quick checks; prof: short launches for ncu captures")
     ap.add_argument("--no-cpu", action="store_true")
