@@ -39,6 +39,7 @@ extern "C" {
 #define MCT_CURVED 2      /* CurvedDetector */
 #define MCT_SHORT_SCAN 4  /* |TotalScanAngle| mod 360 >= 0.01 deg */
 #define MCT_PMATRIX 8     /* PMatrixFile geometry */
+#define MCT_ACCUMULATE 16 /* mct_fdk_bp adds to vol (view-chunked FBP); finish with mct_fdk_bp_finish */
 
 /* storage types of packed / reduced-precision buffers */
 #define MCT_F32 0
@@ -68,6 +69,8 @@ typedef struct mct_geom {
     float total_scan_angle; /* [rad] */
     float fp_step;       /* fpj_step_size, as a fraction of the voxel diagonal */
     float fp_z_per_view; /* helical gantry advance per view [mm] (0: circular) */
+    int32_t view_begin;  /* scan index of this call's first view (view-chunked FBP; else 0) */
+    int32_t views_total; /* views of the whole scan when chunked (0: equal to views) */
 } mct_geom;
 
 /* Per-view and per-element tables (DEVICE pointers, float32). */
@@ -149,6 +152,38 @@ int mct_pack_strided(const mct_geom* g, const float* src, int64_t row_stride, in
  * detector in any view is zero. */
 int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype, float* vol,
                void* stream);
+
+/* View-chunked FDK (Mgfbp_v2, run_mgfbp_v2.py:62-103, which backprojects view by view
+ * to bound device memory): call mct_weight / mct_filter / mct_pack / mct_fdk_bp per
+ * chunk of views with g->views = the chunk's views, g->view_begin = its first scan
+ * view, g->views_total = the scan's views, the tables of the WHOLE scan, and (for the
+ * backprojection) MCT_ACCUMULATE in g->flags on a volume zeroed before the first chunk.
+ * A voxel that leaves the detector in any chunk is carried as NaN; this call, after
+ * the last chunk, writes those voxels as 0 (SetTruncatedRegionToZero, :229-233). */
+int mct_fdk_bp_finish(const mct_geom* g, float* vol, void* stream);
+
+/* ---------------------------------------------------------------- helical FBP */
+
+/* Helical rebinning parameters (Mgfbp_helical.__init__, run_mgfbp_helical.py:59-95). */
+typedef struct mct_helical {
+    int32_t nu;            /* detector columns */
+    int32_t nv;            /* detector rows of the helical sinogram (det_elem_count_vertical) */
+    int32_t views;         /* helical views (view_num before rebinning) */
+    int32_t view_count;    /* views of each rebinned fan sinogram */
+    int32_t n_slices;      /* reconstructed slices (len(array_z_pos)) */
+    float dv;              /* det_elem_height [mm] */
+    float sdd;             /* source_det_dis [mm] */
+    float mag;             /* mag_ratio_isocenter = SDD / SID */
+    float det_offset_vertical; /* [mm] */
+    float dis_per_view;    /* table advance per view [mm] */
+} mct_helical;
+
+/* Rebin a helical sinogram sgm [nv][views][nu] into one fan sinogram per slice:
+ * out [n_slices][view_count][nu], slice s at z = z_pos[s] (device array).  Replaces
+ * Mgfbp_helical.SinogramRebinning run_mgfbp_helical.py:178-205 for all slices in one
+ * launch: linear interpolation along the rows where the slice plane meets view
+ * view_begin(s) + i, times SDD / sqrt(SDD^2 + v^2); 0 for views outside [0, views-2]. */
+int mct_helical_rebin(const mct_helical* h, const float* sgm, const float* z_pos, float* out, void* stream);
 
 /* ---------------------------------------------------------------- forward projection */
 

@@ -14,6 +14,7 @@ MCT_CONE = 1
 MCT_CURVED = 2
 MCT_SHORT_SCAN = 4
 MCT_PMATRIX = 8
+MCT_ACCUMULATE = 16
 MCT_F32 = 0
 MCT_BF16 = 1
 MCT_F16 = 2
@@ -35,6 +36,7 @@ class Geom(ctypes.Structure):
         ("cx", ctypes.c_float), ("cy", ctypes.c_float), ("cz", ctypes.c_float), ("sid", ctypes.c_float),
         ("sdd", ctypes.c_float), ("img_rot", ctypes.c_float), ("total_scan_angle", ctypes.c_float),
         ("fp_step", ctypes.c_float), ("fp_z_per_view", ctypes.c_float),
+        ("view_begin", ctypes.c_int32), ("views_total", ctypes.c_int32),
     ]
 
     def copy(self, **kw):
@@ -50,6 +52,15 @@ class Tables(ctypes.Structure):
 
     _fields_ = [("angles", ctypes.c_void_p), ("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("cz", ctypes.c_void_p),
                 ("pmatrix", ctypes.c_void_p), ("pmat_a", ctypes.c_void_p), ("pmat_xs", ctypes.c_void_p)]
+
+
+class Helical(ctypes.Structure):
+    """Mirror of struct mct_helical."""
+
+    _fields_ = [("nu", ctypes.c_int32), ("nv", ctypes.c_int32), ("views", ctypes.c_int32),
+                ("view_count", ctypes.c_int32), ("n_slices", ctypes.c_int32), ("dv", ctypes.c_float),
+                ("sdd", ctypes.c_float), ("mag", ctypes.c_float), ("det_offset_vertical", ctypes.c_float),
+                ("dis_per_view", ctypes.c_float)]
 
 
 _P = ctypes.c_void_p
@@ -74,6 +85,8 @@ SIGNATURES = {
     "mct_pack_strided": (ctypes.c_int, [_G, _P, _i64, _i64, _P, _i32, _P]),
     "mct_bp_ref_unmatched_packed": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
     "mct_fdk_bp": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
+    "mct_fdk_bp_finish": (ctypes.c_int, [_G, _P, _P]),
+    "mct_helical_rebin": (ctypes.c_int, [ctypes.POINTER(Helical), _P, _P, _P, _P]),
     "mct_fp_workspace_size": (ctypes.c_size_t, [_G]),
     "mct_fp": (ctypes.c_int, [_G, _T, _P, _P, _P, _P, _P]),
     "mct_fp_storage_workspace_size": (ctypes.c_size_t, [_G, _i32]),

@@ -27,6 +27,10 @@ int check_geom(const mct_geom* g, const char* who) {
     MCT_REQUIRE(g->nx >= 2 && g->nz >= 1, "%s: bad image size nx=%d nz=%d", who, g->nx, g->nz);
     MCT_REQUIRE((int64_t)g->nu * g->nv * g->views < (int64_t)1 << 40, "%s: sinogram too large", who);
     MCT_REQUIRE(g->view_mode >= 1 && g->view_mode <= 3, "%s: view_mode must be 1, 2 or 3", who);
+    MCT_REQUIRE(g->view_begin >= 0 && (g->views_total == 0 || g->view_begin + g->views <= g->views_total),
+                "%s: view chunk [%d, %d) outside the scan's %d views", who, g->view_begin, g->view_begin + g->views,
+                g->views_total);
+    MCT_REQUIRE(g->views_total == 0 || g->views_total >= 2 || g->view_begin == 0, "%s: bad views_total", who);
     return MCT_OK;
 }
 
@@ -44,6 +48,14 @@ double div_factor(const mct_geom& g) {
         div = 1.0 / (num_rounds * 2.0);
     }
     return div;
+}
+
+// Entry points that do not take view chunks (everything but weighting and FDK
+// backprojection) reject them.
+int check_whole_scan(const mct_geom* g, const char* who) {
+    MCT_REQUIRE(g->view_begin == 0 && (g->views_total == 0 || g->views_total == g->views),
+                "%s: view-chunked geometry is only supported by mct_weight and mct_fdk_bp", who);
+    return MCT_OK;
 }
 
 }  // namespace mct

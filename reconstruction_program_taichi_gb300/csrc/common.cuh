@@ -46,6 +46,7 @@ inline int launched(const char* what) {
 
 // Geometry validation shared by all entry points.
 int check_geom(const mct_geom* g, const char* who);
+int check_whole_scan(const mct_geom* g, const char* who);
 
 inline int64_t vol_elems(const mct_geom& g) { return (int64_t)g.nz * g.nx * g.nx; }
 inline int64_t sgm_elems(const mct_geom& g) { return (int64_t)g.nv * g.views * g.nu; }

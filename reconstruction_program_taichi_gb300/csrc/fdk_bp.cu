@@ -35,6 +35,7 @@ constexpr int bp_min_blocks() {
 
 struct BpParams {
     int nx, nz, nu, nv, views, cone, curved;
+    int view_begin, views_total, accumulate;  // view-chunked FBP (scan index of view 0, scan size)
     float sid, sdd, img_rot;
     float u0, inv_ustep;   // uidx = (u - u0) * inv_ustep
     float v0, kv;          // vidx = (mag*z - v0) * kv, kv = sign(v_step)/dv
@@ -77,11 +78,11 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
         const int nvc = min(BP_VCHUNK, p.views - jc);
         __syncthreads();
         for (int q = tid; q < nvc; q += BP_TX * BP_TY) {
-            int j = jc + q;
+            const int jg = p.view_begin + jc + q;  // scan index (angles is the whole scan's table)
+            const int vt = p.views_total;
             float s, c;
-            sincosf(angles[j] - p.img_rot, &s, &c);
-            float db = (j == p.views - 1) ? fabsf(angles[p.views - 1] - angles[0]) / (p.views - 1)
-                                          : fabsf(angles[j + 1] - angles[j]);
+            sincosf(angles[jg] - p.img_rot, &s, &c);
+            float db = (jg == vt - 1) ? fabsf(angles[vt - 1] - angles[0]) / (vt - 1) : fabsf(angles[jg + 1] - angles[jg]);
             tab[q] = make_float4(c, s, db * p.div * unscale, 0.0f);
         }
         __syncthreads();
@@ -136,7 +137,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     }
                 }
             } else {
-                const float* P = pmat + 12 * j;
+                const float* P = pmat + 12 * (p.view_begin + j);
                 float P0 = 0, P1 = 0, P2 = 0, P3 = 0, P4 = 0, P5 = 0, P6 = 0, P7 = 0, P8 = 0, P9 = 0, P10 = 0, P11 = 0;
                 if (MODE == 2) {
                     P0 = __ldg(P + 0); P1 = __ldg(P + 1); P2 = __ldg(P + 2); P3 = __ldg(P + 3);
@@ -195,8 +196,19 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     float* out = vol + (int64_t)zb * plane + (int64_t)iy * p.nx + ix;
 #pragma unroll
     for (int k = 0; k < BP_ZC; ++k) {
-        if (zb + k < p.nz) out[(int64_t)k * plane] = (((dead >> k) & 1u) || acc[k] != acc[k]) ? 0.0f : acc[k];
+        if (zb + k < p.nz) {
+            const bool off_detector = ((dead >> k) & 1u) || acc[k] != acc[k];
+            if (p.accumulate)  // a voxel off the detector in any chunk stays NaN until mct_fdk_bp_finish
+                out[(int64_t)k * plane] = off_detector ? __int_as_float(0x7fffffff) : out[(int64_t)k * plane] + acc[k];
+            else
+                out[(int64_t)k * plane] = off_detector ? 0.0f : acc[k];
+        }
     }
+}
+
+__global__ void nan_to_zero_kernel(int64_t n, float* __restrict__ v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (v[i] != v[i]) v[i] = 0.0f;
 }
 
 template <int MODE, bool CONE>
@@ -230,6 +242,9 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     MCT_REQUIRE((int64_t)g->nv * (g->nu - 1) < ((int64_t)1 << 31), "mct_fdk_bp: detector too large");
     BpParams p{};
     p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views;
+    p.view_begin = g->view_begin;
+    p.views_total = g->views_total > 0 ? g->views_total : g->views;
+    p.accumulate = (g->flags & MCT_ACCUMULATE) != 0;
     p.cone = cone; p.curved = (g->flags & MCT_CURVED) != 0;
     p.sid = g->sid; p.sdd = g->sdd; p.img_rot = g->img_rot;
     p.u0 = g->u0; p.inv_ustep = (float)(1.0 / (double)g->u_step);
@@ -276,4 +291,12 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     return launched("fdk_bp_kernel");
+}
+
+extern "C" int mct_fdk_bp_finish(const mct_geom* g, float* vol, void* stream) {
+    MCT_REQUIRE(g && vol && g->nx >= 1 && g->nz >= 1, "mct_fdk_bp_finish: bad arguments");
+    const int64_t n = (int64_t)g->nz * g->nx * g->nx;
+    const int64_t blocks = (n + 255) / 256;
+    nan_to_zero_kernel<<<(int)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, as_stream(stream)>>>(n, vol);
+    return launched("nan_to_zero_kernel");
 }

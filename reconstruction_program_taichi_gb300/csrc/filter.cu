@@ -10,7 +10,7 @@ namespace mct {
 namespace {
 
 struct WeightParams {
-    int nu, nv, views, curved, short_scan, n_bh;
+    int nu, nv, views, curved, short_scan, n_bh, view_begin;
     int64_t row_stride, view_stride;
     float u0, u_step, v0, v_step, sdd, scan;
     float num_rounds, remain;  // short-scan constants
@@ -68,7 +68,7 @@ __global__ void weight_kernel(WeightParams p, const float* __restrict__ in, cons
         float sdd = p.sdd;
         if (p.curved) val = val * sdd * cosf((-1.0f) * u / sdd) * sdd / sqrtf(sdd * sdd + v * v);
         else val = (val * sdd * sdd) / sqrtf(sdd * sdd + u * u + v * v);
-        if (p.short_scan) val *= parker(p, fabsf(angles[j] - angles[0]), u);
+        if (p.short_scan) val *= parker(p, fabsf(angles[p.view_begin + j] - angles[0]), u);
         out[i] = val;
     }
 }
@@ -302,6 +302,7 @@ int mct_weight(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t
     MCT_REQUIRE(!short_scan || (t && t->angles), "mct_weight: short scan needs the angle table");
     WeightParams p{};
     p.nu = g->nu; p.nv = g->nv; p.views = g->views;
+    p.view_begin = g->view_begin;  // angles is the whole scan's table (view-chunked FBP)
     p.curved = (g->flags & MCT_CURVED) != 0;
     p.short_scan = short_scan;
     p.n_bh = n_bh;

@@ -620,6 +620,7 @@ ellipsoid_kernel(FpParams p, const float* __restrict__ angles, const float* __re
 
 int make_params(const mct_geom* g, FpParams& p, const char* who) {
     MCT_TRY(check_geom(g, who));
+    MCT_TRY(check_whole_scan(g, who));
     p = FpParams{};
     p.nx = g->nx; p.nz = g->nz; p.nu = g->nu; p.nv = g->nv; p.views = g->views; p.K = g->fp_steps;
     p.cone = (g->flags & MCT_CONE) != 0;

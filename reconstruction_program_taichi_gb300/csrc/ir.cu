@@ -425,6 +425,7 @@ int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const vo
 
 static int unmatched_params(const mct_geom* g, UbParams& p) {
     MCT_TRY(check_geom(g, "mct_bp_ref_unmatched"));
+    MCT_TRY(check_whole_scan(g, "mct_bp_ref_unmatched"));
     MCT_REQUIRE(!(g->flags & MCT_PMATRIX), "mct_bp_ref_unmatched: projection-matrix geometry is not supported");
     const bool cone = (g->flags & MCT_CONE) != 0;
     MCT_REQUIRE(!cone || g->nv >= 2, "mct_bp_ref_unmatched: cone beam needs at least 2 rows");

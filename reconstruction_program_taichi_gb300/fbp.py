@@ -172,6 +172,121 @@ class Mgfbp:
             imwriteTiff(self.img_recon, self.output_path, dtype=np.float32)
 
 
+class Mgfbp_v2(Mgfbp):  # noqa: N801 - reference name
+    """Drop-in for Mgfbp_v2 (run_mgfbp_v2.py:61-364), the FBP that backprojects view by
+    view to bound device memory.  Here the sinogram stays on the host and streams to
+    the device in chunks of `views_per_chunk` views: while chunk c is weighted,
+    filtered, packed and backprojected (accumulating into the volume) on the compute
+    stream, chunk c+1 is staged into pinned memory by the CPU and copied on a second
+    stream.  Device memory is the volume plus two chunks, whatever the number of views.
+    Voxels that leave the detector in any view are 0, as in the reference
+    (SetTruncatedRegionToZero :229-233 after its per-view -10000 marks)."""
+
+    def __init__(self, config_dict, device=None, storage="f32", verbose=True, views_per_chunk=64):
+        super().__init__(config_dict, device=device, storage=storage, verbose=verbose)
+        if views_per_chunk < 1:
+            raise ValueError("views_per_chunk must be positive")
+        self.views_per_chunk = int(views_per_chunk)
+
+    def MainFunction(self):  # noqa: N802 - reference name
+        """run_mgfbp_v2.py:62-103."""
+        if self.kernel_name is None:
+            raise ConfigError("ERROR: no reconstruction kernel (HammingFilter, GaussianApodizedRamp or None) "
+                              "in the config!")
+        pipe = self.pipeline
+        self.file_processed_count = 0
+        for file in os.listdir(self.input_dir):
+            if re.match(self.input_files_pattern, file):
+                if self.ReadSinogram(file):
+                    self.file_processed_count += 1
+                    self._log("Reconstructing %s ..." % self.input_path)
+                    vol = self._stream_file(pipe)
+                    self.img_recon = vol.cpu().numpy()
+                    self._log("Saving to %s !" % self.output_path)
+                    self.SaveReconImg()
+        return self.img_recon
+
+    def _stream_file(self, pipe):
+        dg, dev = pipe.dg, pipe.device
+        g = dg.geom
+        nb, V = g.views, min(self.views_per_chunk, g.views)
+        raw = self._raw
+        sino_layout = self._view_stride == g.nu  # [rows][views][cols] (else [views][rows][cols])
+        shape = (g.nv, V, g.nu) if sino_layout else (V, g.nv, g.nu)
+        staging = [torch.empty(shape, dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        dev_in = [torch.empty(shape, dtype=torch.float32, device=dev) for _ in range(2)]
+        copy_stream = torch.cuda.Stream(device=dev)
+        compute = torch.cuda.current_stream(dev)
+        copied = [torch.cuda.Event() for _ in range(2)]
+        consumed = [torch.cuda.Event() for _ in range(2)]
+        vol = torch.zeros(dg.vol_shape, dtype=torch.float32, device=dev)
+        f32 = dict(dtype=torch.float32, device=dev)
+        weighted = torch.empty((g.nv, V, g.nu), **f32)
+        smoothed = torch.empty((g.nv, V, g.nu), **f32) if pipe.gauss_v is not None else None
+        filtered = torch.empty((V, g.nv, g.nu), **f32)
+        chunk0 = ops.ViewChunk(dg, 0, V)
+        packed = torch.empty(max(ops.packed_bytes(chunk0, pipe.dtype), 16), dtype=torch.uint8, device=dev)
+        chunks = [(j0, min(j0 + V, nb)) for j0 in range(0, nb, V)]
+
+        def stage(i):
+            j0, j1 = chunks[i]
+            n = j1 - j0
+            b = i % 2
+            consumed[b].synchronize()  # the pinned buffer's previous copy has been consumed
+            src = raw[:, j0:j1, :] if sino_layout else raw[j0:j1]
+            dst = staging[b][:, :n, :] if sino_layout else staging[b][:n]
+            dst.copy_(torch.from_numpy(src))
+            with torch.cuda.stream(copy_stream):
+                copy_stream.wait_event(consumed[b])
+                (dev_in[b][:, :n, :] if sino_layout else dev_in[b][:n]).copy_(dst, non_blocking=True)
+                copied[b].record(copy_stream)
+
+        for e in consumed:
+            e.record(compute)
+        stage(0)
+        for i, (j0, j1) in enumerate(chunks):
+            n, b = j1 - j0, i % 2
+            if i + 1 < len(chunks):
+                stage(i + 1)
+            compute.wait_event(copied[b])
+            cg = ops.ViewChunk(dg, j0, n, accumulate=True)
+            rs, vs = (V * g.nu, g.nu) if sino_layout else (g.nu, g.nv * g.nu)
+            w = ops.weight(cg, dev_in[b], rs, vs, pipe.bh, out=weighted if n == V else None)
+            if smoothed is not None:
+                w = ops.vgauss(cg, w, pipe.gauss_v, out=smoothed if n == V else None)
+            if pipe.kernel_none:
+                f = w.permute(1, 0, 2).contiguous()
+            else:
+                f = ops.filter_rows(cg, w, pipe.taps, out=filtered[:n])
+            pk = ops.pack(cg, f, pipe.dtype, out=packed)
+            ops.fdk_bp(cg, pk, pipe.dtype, out=vol)
+            consumed[b].record(compute)
+        ops.fdk_bp_finish(dg, vol)
+        return vol
+
+
+def run_mgfbp_v2(file_path, device=None, storage="f32", verbose=True, views_per_chunk=64):
+    """Drop-in for run_mgfbp_v2.run_mgfbp_v2 (run_mgfbp_v2.py:26-57)."""
+    if verbose:
+        print("Performing FBP from MandoCT-GB300 (view-streaming) ...")
+    start = time.time()
+    if not os.path.exists(file_path):
+        raise ConfigError(f"ERROR: Config File {file_path} does not exist!")
+    fbp = Mgfbp_v2(ReadConfigFile(file_path), device=device, storage=storage, verbose=verbose,
+                   views_per_chunk=views_per_chunk)
+    img = fbp.MainFunction()
+    if verbose:
+        if fbp.file_processed_count > 0:
+            print(f"\nA total of {fbp.file_processed_count:d} file(s) are reconstructed!")
+            print(f"Time cost is {time.time() - start:.3} sec\n")
+        else:
+            print(f"\nWarning: Did not find files like {fbp.input_files_pattern:s} in {fbp.input_dir:s}.")
+            print("No images are reconstructed!\n")
+    del fbp
+    gc.collect()
+    return img
+
+
 def run_mgfbp(file_path, device=None, storage="f32", verbose=True):
     """Drop-in for run_mgfbp.run_mgfbp (run_mgfbp.py:18-47): FBP of every file that
     matches the config, returning the last reconstruction [z, y, x] (HU if WaterMu)."""

@@ -73,6 +73,36 @@ class DeviceGeometry:
         return ctypes.byref(self.tables)
 
 
+class ViewChunk:
+    """Views [view_begin, view_begin + views) of a DeviceGeometry for view-chunked FBP:
+    the whole scan's device tables with a geometry whose views / view_begin /
+    views_total select the range (mct_weight, mct_filter, mct_pack and mct_fdk_bp
+    accept it; accumulate=True adds the backprojection to the volume)."""
+
+    def __init__(self, dg, view_begin, views, accumulate=False):
+        g = dg.geom
+        if not (0 <= view_begin and views >= 1 and view_begin + views <= g.views):
+            raise ValueError("view chunk outside the scan")
+        self.geom = g.copy(views=views, view_begin=view_begin, views_total=g.views,
+                           flags=g.flags | (_lib.MCT_ACCUMULATE if accumulate else 0))
+        self.tables = dg.tables
+        self.device = dg.device
+        self._parent = dg  # keeps the tables alive
+
+    sgm_shape = DeviceGeometry.sgm_shape
+    vol_shape = DeviceGeometry.vol_shape
+    g = DeviceGeometry.g
+    t = DeviceGeometry.t
+
+
+def fdk_bp_finish(dg, vol):
+    """Write the voxels that left the detector in some chunk as 0 (after the last
+    chunk of a view-chunked FBP)."""
+    _check(vol, "vol", dg.vol_shape)
+    _lib.call("mct_fdk_bp_finish", dg.g(), _ptr(vol), _stream())
+    return vol
+
+
 # ---------------------------------------------------------------- FBP / FDK
 
 def weight(dg, sgm, row_stride, view_stride, bh=None, out=None):

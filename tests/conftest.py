@@ -22,8 +22,9 @@ def load_golden(name):
     return out
 
 
-def golden_names(prefix):
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith(prefix))
+def golden_names(prefix, exclude=()):
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and f.startswith(prefix) and not f.startswith(tuple(exclude)))
 
 
 def rel_l2(a, b):

@@ -116,6 +116,13 @@ IR_CASES = {
     "ir_piccs": _upd(BASE_IR, Alpha=0.5),
 }
 
+# the view-by-view FBP (run_mgfbp_v2.py): same configs, its own driver
+FBPV2_CASES = {
+    "fbpv2_cone": _upd(BASE_CONE),
+    "fbpv2_fan_short_curved": _upd(BASE_FAN, CurvedDetector=True, TotalScanAngle=250, Views=36,
+                                   HammingFilter=0.6, BeamHardeningCorrectionCoefficients=[1.0, 0.05]),
+}
+
 # FDK with projection matrices (run_mgfbp.py:549-627, 721-874, 1134-1141): the matrices
 # are synthesised from a circular geometry (see pmatrices()); "tilt" raises the source
 # path out of the z = 0 plane so that ModifyPMatrixToStandardForm has work to do.
@@ -151,6 +158,20 @@ def pmatrices(cfg, u_shift, v_shift, tilt, scale):
         m = np.linalg.inv(np.stack([e_u, e_v, origin - src], axis=1))
         out.append(np.concatenate([m, (-m @ src)[:, None]], axis=1).reshape(-1))
     return np.concatenate(out)
+
+
+def run_fbpv2_case(name, cfg, RV2, rng):
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("sgm")
+        cfg.update(InputDir=d + "/sgm", OutputDir=d + "/rec")
+        sgm = rng.uniform(0.0, 1.0, (cfg["DetectorElementCountVertical"], cfg["Views"],
+                                     cfg["DetectorElementCountHorizontal"])).astype(np.float32)
+        sgm.tofile("sgm/sgm_a.raw")
+        json.dump(cfg, open("config.jsonc", "w"))
+        fbp = RV2.Mgfbp_v2(RV2.ReadConfigFile("config.jsonc"))
+        img = fbp.MainFunction()
+        return dict(config=json.dumps(cfg), input_sgm=sgm, recon=np.asarray(img, np.float64))
 
 
 def run_pmatrix_case(name, spec, R, rng):
@@ -337,16 +358,18 @@ def main():
     import run_mgfbp_iterative_recon_IRN_CGLS_piccs as RP
     import run_mgfpj as R1
     import run_mgfpj_v2 as R2
+    import run_mgfbp_v2 as RV2
     # NumPy >= 2 no longer turns size-1 arrays into Python scalars in math.cos & co.;
     # the reference relies on that (run_mgfbp.py:738-741, on least-squares solutions of
     # shape (3, 1)), so its modules get a math whose functions convert them first, as
     # the NumPy of the reference's time did.
-    for mod in (R, R3, RI, RP, R1, R2):
+    for mod in (R, R3, RI, RP, R1, R2, RV2):
         if hasattr(mod, "math"):
             mod.math = _MathCompat()
     jobs = [(k, v, "fbp") for k, v in FBP_CASES.items()] + [(k, v, "fpj") for k, v in FPJ_CASES.items()] \
         + [(k, v, "ir") for k, v in IR_CASES.items()] + [(k, v, "v1") for k, v in FPJ_V1_CASES.items()] \
-        + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()] + [(k, v, "pm") for k, v in PM_CASES.items()]
+        + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()] + [(k, v, "pm") for k, v in PM_CASES.items()] \
+        + [(k, v, "fbpv2") for k, v in FBPV2_CASES.items()]
     for i, (name, cfg, kind) in enumerate(jobs):
         if only and name not in only:
             continue
@@ -360,6 +383,8 @@ def main():
                 out = run_fpj_case(name, cfg, R3, rng)
             elif kind == "pm":
                 out = run_pmatrix_case(name, cfg, R, rng)
+            elif kind == "fbpv2":
+                out = run_fbpv2_case(name, cfg, RV2, rng)
             elif kind in ("v1", "v2"):
                 out = run_fpj_variant_case(name, cfg, R1 if kind == "v1" else R2, rng)
             else:

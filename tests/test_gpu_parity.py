@@ -46,6 +46,8 @@ def _write_case(z, tmp_path, kind):
 
 @pytest.mark.parametrize("name", golden_names("fbp") + golden_names("fdk"))
 def test_run_mgfbp_matches_reference(name, tmp_path, cuda):
+    """run_mgfbp against Mgfbp's fixtures, and against Mgfbp_v2's (fbpv2_*: the same
+    reconstruction computed view by view)."""
     from reconstruction_program_taichi_gb300 import run_mgfbp
     z = load_golden(name)
     img = run_mgfbp(_write_case(z, tmp_path, "fbp"), verbose=False)
@@ -368,3 +370,16 @@ def test_packed_unmatched_bp_bf16_error_is_small(cone, cuda):
         c = ops.bp_unmatched_packed(dg, ops.pack_sinogram(dg, sgm * scale, dtype=MCT_F16), dtype=MCT_F16) / scale
         assert torch.equal(a == 0, c == 0)
         assert float((a - c).norm() / a.norm()) < 8e-4
+
+
+@pytest.mark.parametrize("chunk", [1, 7, 64])
+@pytest.mark.parametrize("name", golden_names("fbpv2") + ["fdk_cone", "fbp2d_curved_short"])
+def test_run_mgfbp_v2_matches_reference(name, chunk, tmp_path, cuda):
+    """The view-streaming drop-in (host sinogram streamed in chunks of views, pinned
+    staging and a copy stream) against the reference's view-by-view FBP and Mgfbp."""
+    from reconstruction_program_taichi_gb300 import run_mgfbp_v2
+    z = load_golden(name)
+    img = run_mgfbp_v2(_write_case(z, tmp_path, "fbp"), verbose=False, views_per_chunk=chunk)
+    assert img.shape == z["recon"].shape
+    assert int(np.sum((img == 0) != (z["recon"] == 0))) == 0
+    assert rel_l2(img, z["recon"]) < TOL

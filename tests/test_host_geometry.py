@@ -34,7 +34,7 @@ def _parse(cfg, kind, tmp_path, z=None):
     return o
 
 
-@pytest.mark.parametrize("name", golden_names("fbp") + golden_names("fdk"))
+@pytest.mark.parametrize("name", golden_names("fbp", exclude=["fbpv2"]) + golden_names("fdk"))
 def test_fbp_arrays_and_taps(name, tmp_path):
     z = load_golden(name)
     o = _parse(z["config"], "fbp", tmp_path, z)

@@ -28,7 +28,7 @@ def _fbp_params(c):
     return dict(cone=cone, scan=scan, short=short, rr=rr, nz=nz, cz=cz or 0.0)
 
 
-@pytest.mark.parametrize("name", golden_names("fbp") + golden_names("fdk"))
+@pytest.mark.parametrize("name", golden_names("fbp", exclude=["fbpv2"]) + golden_names("fdk"))
 def test_fbp_oracle_matches_reference(name):
     z = load_golden(name)
     c = z["config"]
