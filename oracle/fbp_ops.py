@@ -282,3 +282,31 @@ def fdk_bp(F, angles, u_arr, v_arr, *, nx, nz, px, pz, cx, cy, cz, sid, sdd, dv,
         term = (sid * dw) * val * dbeta * div
         acc += np.where(dead, 0.0, term)
     return np.where(dead, 0.0, acc)
+
+
+def helical_rebin(sgm, z_pos, *, view_count, dis_per_view, mag, det_offset_vertical, dv, sdd):
+    """Per-slice fan sinograms from a helical sinogram sgm [rows, views, cols]:
+    out [slices, view_count, cols].  Mgfbp_helical.SinogramRebinning,
+    run_mgfbp_helical.py:178-205 (float64 here)."""
+    sgm = np.asarray(sgm, dtype=np.float64)
+    nv, nb, nu = sgm.shape
+    out = np.zeros((len(z_pos), view_count, nu))
+    for s, z in enumerate(np.asarray(z_pos, dtype=np.float64)):
+        v0 = (z - det_offset_vertical / mag) / dis_per_view
+        begin = math.floor(v0 - 0.5 * view_count + 0.5)
+        for i in range(view_count):
+            vi = begin + i
+            if not (0 <= vi <= nb - 2):
+                continue
+            v_pos = (z - vi * dis_per_view) * mag - det_offset_vertical
+            v_idx = -v_pos / dv + (nv - 1.0) / 2.0
+            if v_idx >= nv - 1:
+                row = sgm[nv - 1, int(vi)]
+            elif v_idx <= 0:
+                row = sgm[0, int(vi)]
+            else:
+                f = math.floor(v_idx)
+                w = v_idx - f
+                row = sgm[f, int(vi)] * (1 - w) + sgm[f + 1, int(vi)] * w
+            out[s, i] = row * sdd / math.sqrt(sdd ** 2 + v_pos ** 2)
+    return out

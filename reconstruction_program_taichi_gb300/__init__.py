@@ -9,11 +9,12 @@ and streams.  There is no CPU fallback.
 from ._lib import NativeLibraryError, launch_count
 from .config import ConfigError, ReadConfigFile, load_jsonc, remove_comments, save_jsonc
 from .fbp import FdkPipeline, Mgfbp, Mgfbp_v2, run_mgfbp, run_mgfbp_v2
+from .helical import Mgfbp_helical, run_mgfbp_helical
 from .fpj import FpPipeline, Mgfpj_v3, run_mgfpj_v3
 from .ir import IrSystem, Mgfbp_ir, Mgfbp_ir_piccs, run_mgfbp_ir, run_mgfbp_ir_piccs
 
 __all__ = [
     "ConfigError", "NativeLibraryError", "ReadConfigFile", "load_jsonc", "remove_comments", "save_jsonc",
-    "FdkPipeline", "Mgfbp", "run_mgfbp", "Mgfbp_v2", "run_mgfbp_v2", "FpPipeline", "Mgfpj_v3", "run_mgfpj_v3",
+    "FdkPipeline", "Mgfbp", "run_mgfbp", "Mgfbp_v2", "run_mgfbp_v2", "Mgfbp_helical", "run_mgfbp_helical", "FpPipeline", "Mgfpj_v3", "run_mgfpj_v3",
     "IrSystem", "Mgfbp_ir", "Mgfbp_ir_piccs", "run_mgfbp_ir", "run_mgfbp_ir_piccs", "launch_count",
 ]

@@ -123,6 +123,15 @@ FBPV2_CASES = {
                                    HammingFilter=0.6, BeamHardeningCorrectionCoefficients=[1.0, 0.05]),
 }
 
+# helical FBP by per-slice rebinning (run_mgfbp_helical.py)
+BASE_HELICAL = _upd(BASE_CONE, Views=72, TotalScanAngle=1080, HelicalPitch=1.0, DetectorOffsetVertical=0.0)
+HELICAL_CASES = {
+    "helical_full": _upd(BASE_HELICAL),
+    "helical_short_curved": _upd(BASE_HELICAL, Views=90, HelicalPitch=-1.5, CurvedDetector=True, HammingFilter=0.8,
+                                 DetectorOffsetVertical=0.8, ImageRotation=12,
+                                 BeamHardeningCorrectionCoefficients=[1.0, 0.03]),
+}
+
 # FDK with projection matrices (run_mgfbp.py:549-627, 721-874, 1134-1141): the matrices
 # are synthesised from a circular geometry (see pmatrices()); "tilt" raises the source
 # path out of the z = 0 plane so that ModifyPMatrixToStandardForm has work to do.
@@ -172,6 +181,23 @@ def run_fbpv2_case(name, cfg, RV2, rng):
         fbp = RV2.Mgfbp_v2(RV2.ReadConfigFile("config.jsonc"))
         img = fbp.MainFunction()
         return dict(config=json.dumps(cfg), input_sgm=sgm, recon=np.asarray(img, np.float64))
+
+
+def run_helical_case(name, cfg, RH, rng):
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("sgm")
+        cfg.update(InputDir=d + "/sgm", OutputDir=d + "/rec")
+        sgm = rng.uniform(0.0, 1.0, (cfg["DetectorElementCountVertical"], cfg["Views"],
+                                     cfg["DetectorElementCountHorizontal"])).astype(np.float32)
+        sgm.tofile("sgm/sgm_a.raw")
+        json.dump(cfg, open("config.jsonc", "w"))
+        fbp = RH.Mgfbp_helical(RH.ReadConfigFile("config.jsonc"))
+        img = fbp.MainFunction()
+        rebinned = np.fromfile("sgm/temp/sgm_rebin.raw", dtype=np.float32)
+        return dict(config=json.dumps(cfg), input_sgm=sgm, recon=np.asarray(img, np.float64),
+                    rebinned=rebinned.reshape(len(fbp.array_z_pos), fbp.view_count, -1).astype(np.float64),
+                    z_pos=np.asarray(fbp.array_z_pos, np.float64))
 
 
 def run_pmatrix_case(name, spec, R, rng):
@@ -359,17 +385,18 @@ def main():
     import run_mgfpj as R1
     import run_mgfpj_v2 as R2
     import run_mgfbp_v2 as RV2
+    import run_mgfbp_helical as RH
     # NumPy >= 2 no longer turns size-1 arrays into Python scalars in math.cos & co.;
     # the reference relies on that (run_mgfbp.py:738-741, on least-squares solutions of
     # shape (3, 1)), so its modules get a math whose functions convert them first, as
     # the NumPy of the reference's time did.
-    for mod in (R, R3, RI, RP, R1, R2, RV2):
+    for mod in (R, R3, RI, RP, R1, R2, RV2, RH):
         if hasattr(mod, "math"):
             mod.math = _MathCompat()
     jobs = [(k, v, "fbp") for k, v in FBP_CASES.items()] + [(k, v, "fpj") for k, v in FPJ_CASES.items()] \
         + [(k, v, "ir") for k, v in IR_CASES.items()] + [(k, v, "v1") for k, v in FPJ_V1_CASES.items()] \
         + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()] + [(k, v, "pm") for k, v in PM_CASES.items()] \
-        + [(k, v, "fbpv2") for k, v in FBPV2_CASES.items()]
+        + [(k, v, "fbpv2") for k, v in FBPV2_CASES.items()] + [(k, v, "helical") for k, v in HELICAL_CASES.items()]
     for i, (name, cfg, kind) in enumerate(jobs):
         if only and name not in only:
             continue
@@ -385,6 +412,8 @@ def main():
                 out = run_pmatrix_case(name, cfg, R, rng)
             elif kind == "fbpv2":
                 out = run_fbpv2_case(name, cfg, RV2, rng)
+            elif kind == "helical":
+                out = run_helical_case(name, cfg, RH, rng)
             elif kind in ("v1", "v2"):
                 out = run_fpj_variant_case(name, cfg, R1 if kind == "v1" else R2, rng)
             else:

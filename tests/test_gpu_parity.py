@@ -383,3 +383,32 @@ def test_run_mgfbp_v2_matches_reference(name, chunk, tmp_path, cuda):
     assert img.shape == z["recon"].shape
     assert int(np.sum((img == 0) != (z["recon"] == 0))) == 0
     assert rel_l2(img, z["recon"]) < TOL
+
+
+@pytest.mark.parametrize("name", golden_names("helical"))
+def test_helical_rebin_matches_reference(name, tmp_path, cuda):
+    import torch
+    from reconstruction_program_taichi_gb300 import Mgfbp_helical
+    z = load_golden(name)
+    cfg = _write_case(z, tmp_path, "fbp")
+    from reconstruction_program_taichi_gb300.config import ReadConfigFile
+    h = Mgfbp_helical(ReadConfigFile(cfg), verbose=False)
+    np.testing.assert_allclose(h.array_z_pos, z["z_pos"], rtol=0, atol=1e-6)
+    assert h.view_count == z["rebinned"].shape[1]
+    # the full drop-in: reconstruction and the rebinned stack it leaves in InputDir/temp
+    img = h.MainFunction()
+    reb = np.fromfile(os.path.join(h.input_dir, "temp", "sgm_rebin.raw"), dtype=np.float32).reshape(z["rebinned"].shape)
+    assert np.array_equal(reb == 0, z["rebinned"] == 0)
+    assert rel_l2(reb, z["rebinned"]) < 1e-5
+    assert img.shape == z["recon"].shape
+    assert int(np.sum((img == 0) != (z["recon"] == 0))) == 0
+    assert rel_l2(img, z["recon"]) < TOL
+
+
+@pytest.mark.parametrize("name", golden_names("helical"))
+def test_run_mgfbp_helical_matches_reference(name, tmp_path, cuda):
+    from reconstruction_program_taichi_gb300 import run_mgfbp_helical
+    z = load_golden(name)
+    img = run_mgfbp_helical(_write_case(z, tmp_path, "fbp"), verbose=False)
+    assert img.shape == z["recon"].shape
+    assert rel_l2(img, z["recon"]) < TOL
