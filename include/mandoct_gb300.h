@@ -259,6 +259,19 @@ int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sg
 int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
                                 float* vol, void* stream);
 
+/* ADMM-TV splitting step of run_mgfbp_iterative_recon_ADMM_CGLS.py:128-143, in place
+ * on volume-sized vy, vx (split variables) and py, px (scaled duals): with the in-plane
+ * forward differences D_y x, D_x x (0 at the far edge) and w = D x + p / rho, v = w
+ * where |w| > threshold (else 0; the reference's rule is a hard threshold), then
+ * p += rho * (D x - v).  No counterpart name in the reference (NumPy there). */
+int mct_admm_shrink(const mct_geom* g, const float* x, float rho, float threshold, float* vy, float* vx, float* py,
+                    float* px, void* stream);
+
+/* Right-hand side of the ADMM x-step (FunctionY, :160-162): out = bpb + rho * (Dt vy + Dt vx)
+ * - (Dt py + Dt px), Dt a [i] = a[i-1] - a[i] on interior indices, 0 at both ends. */
+int mct_admm_rhs(const mct_geom* g, const float* bpb, const float* vy, const float* vx, const float* py,
+                 const float* px, float rho, float* out, void* stream);
+
 /* TV reweighting WR = 1/sqrt(|D x|^2 + beta) (forward differences, zero at the far
  * edge; z differences only when nz > 2).  Replaces Mgfbp_ir.GenerateWR
  * run_mgfbp_iterative_recon_IRN_CGLS.py:234-243.  x, wr: [nz][nx][nx]. */

@@ -223,3 +223,62 @@ def irn_piccs(ops, sgm, prior, lam, alpha, beta_tv, n_irn, n_iter):
         wrp = generate_wr(x - prior, beta_tv)
         x = tikhonov_piccs(ops, mask, bp_b, x, prior, wr, wrp, lam, alpha, ratio, n_iter)
     return x
+
+
+def _diff(x, axis):
+    """Forward difference with 0 at the last index (ADMM script Diff, :185-193)."""
+    out = np.zeros_like(x)
+    sl_a = [slice(None)] * 3
+    sl_b = [slice(None)] * 3
+    sl_a[axis], sl_b[axis] = slice(1, None), slice(None, -1)
+    out[tuple(sl_b)] = x[tuple(sl_a)] - x[tuple(sl_b)]
+    return out
+
+
+def _diff_t(x, axis):
+    """out[i] = x[i-1] - x[i] on interior indices (ADMM script DiffT, :195-203)."""
+    out = np.zeros_like(x)
+    sl_o = [slice(None)] * 3
+    sl_p = [slice(None)] * 3
+    sl_o[axis], sl_p[axis] = slice(1, -1), slice(0, -2)
+    out[tuple(sl_o)] = x[tuple(sl_p)] - x[tuple(sl_o)]
+    return out
+
+
+def admm_tv(ops, sgm, x_seed, lam, n_outer, n_iter, rho=0.1):
+    """ADMM-TV driver of run_mgfbp_iterative_recon_ADMM_CGLS.py:79-162 (float64):
+    x-step CGLS on (P^T P + rho D^T D) x = P^T b + rho Dt v - Dt p; hard-threshold
+    v-step; dual ascent.  Returns (x, v_y, v_x, p_y, p_x) with y = axis 1, x = axis 2."""
+    g = ops.g
+    mask = ops.emap()
+    bp_b = ops.bp(sgm * mask)
+    ratio = float(g["rows"] * g["views"] * g["nu"] / (g["nz"] * g["nx"] * g["nx"]))
+    ones = np.ones_like(x_seed)
+    x = x_seed
+    vy, vx = _diff(x, 1), _diff(x, 2)
+    py, px = np.zeros_like(x), np.zeros_like(x)
+    for _ in range(n_outer):
+        rhs = bp_b + rho * (_diff_t(vy, 1) + _diff_t(vx, 2)) - (_diff_t(py, 1) + _diff_t(px, 2))
+
+        def fx(a):
+            return ops.ptp(a, mask) + rho * dtwd(a, ones)
+
+        out = x
+        d = rhs - fx(x)
+        r = d
+        for _ in range(n_iter):
+            q = fx(d)
+            rr = np.sum(r * r)
+            alpha = rr / np.sum(d * q)
+            out = out + alpha * d
+            r = r - alpha * q
+            d = r + np.sum(r * r) / rr * d
+        x = out
+        wy = _diff(x, 1) + py / rho
+        wx = _diff(x, 2) + px / rho
+        t = np.sqrt(wy * wy + wx * wx)
+        keep = ((t - lam * ratio / rho) > 0) & (t != 0)
+        vy, vx = np.where(keep, wy, 0.0), np.where(keep, wx, 0.0)
+        py = py + rho * (_diff(x, 1) - vy)
+        px = px + rho * (_diff(x, 2) - vx)
+    return x, vy, vx, py, px

@@ -256,6 +256,48 @@ __global__ void tv_weights_kernel(int nx, int nz, float beta, const float* __res
     }
 }
 
+// ADMM-TV splitting updates (run_mgfbp_iterative_recon_ADMM_CGLS.py:128-143), one pass:
+// w = D x + p / rho per in-plane axis (Diff along y and x, 0 at the far edge);
+// v = w where |w| = sqrt(wy^2 + wx^2) exceeds thr, else 0 (the reference's rule is a
+// hard threshold: it multiplies w by (|w| - thr > 0) * |w| / |w|); p += rho * (D x - v).
+__global__ void admm_shrink_kernel(int nx, int nz, const float* __restrict__ x, float rho, float thr,
+                                   float* __restrict__ vy, float* __restrict__ vx, float* __restrict__ py,
+                                   float* __restrict__ px) {
+    const int64_t n = (int64_t)nz * nx * nx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % nx);
+        const int iy = (int)((i / nx) % nx);
+        const float c = x[i];
+        const float dy = iy < nx - 1 ? x[i + nx] - c : 0.0f;
+        const float dx = ix < nx - 1 ? x[i + 1] - c : 0.0f;
+        const float wy = dy + py[i] / rho, wx = dx + px[i] / rho;
+        const float t = sqrtf(wy * wy + wx * wx);
+        const bool keep = (t - thr) > 0.0f && t != 0.0f;
+        const float ny = keep ? wy : 0.0f, nx_ = keep ? wx : 0.0f;
+        vy[i] = ny;
+        vx[i] = nx_;
+        py[i] = py[i] + rho * (dy - ny);
+        px[i] = px[i] + rho * (dx - nx_);
+    }
+}
+
+// Right-hand side of the ADMM x-step (FunctionY, :160-162):
+// out = bpb + rho * (DiffT(vy, y) + DiffT(vx, x)) - (DiffT(py, y) + DiffT(px, x)), with
+// DiffT(a)[i] = a[i-1] - a[i] on interior indices and 0 on the first and last.
+__global__ void admm_rhs_kernel(int nx, int nz, const float* __restrict__ bpb, const float* __restrict__ vy,
+                                const float* __restrict__ vx, const float* __restrict__ py,
+                                const float* __restrict__ px, float rho, float* __restrict__ out) {
+    const int64_t n = (int64_t)nz * nx * nx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % nx);
+        const int iy = (int)((i / nx) % nx);
+        const bool iny = iy >= 1 && iy <= nx - 2, inx = ix >= 1 && ix <= nx - 2;
+        const float tvy = iny ? vy[i - nx] - vy[i] : 0.0f, tvx = inx ? vx[i - 1] - vx[i] : 0.0f;
+        const float tpy = iny ? py[i - nx] - py[i] : 0.0f, tpx = inx ? px[i - 1] - px[i] : 0.0f;
+        out[i] = bpb[i] + rho * (tvy + tvx) - (tpy + tpx);
+    }
+}
+
 // out = a*out_in + s * (D^T W D x), run_mgfbp_iterative_recon_IRN_CGLS.py:267-286.
 __global__ void dtwd_kernel(int nx, int nz, const float* __restrict__ x, const float* __restrict__ wr, float s,
                             const float* __restrict__ out_in, float a, float* __restrict__ out) {
@@ -470,6 +512,23 @@ int mct_tv_weights(const mct_geom* g, const float* x, float beta, float* wr, voi
     MCT_REQUIRE(g && x && wr && x != wr && g->nx >= 1 && g->nz >= 1, "mct_tv_weights: bad arguments");
     tv_weights_kernel<<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, beta, x, wr);
     return launched("tv_weights_kernel");
+}
+
+int mct_admm_shrink(const mct_geom* g, const float* x, float rho, float threshold, float* vy, float* vx, float* py,
+                    float* px, void* stream) {
+    MCT_REQUIRE(g && x && vy && vx && py && px && g->nx >= 1 && g->nz >= 1 && rho != 0.0f,
+                "mct_admm_shrink: bad arguments");
+    admm_shrink_kernel<<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, x, rho, threshold, vy, vx,
+                                                                             py, px);
+    return launched("admm_shrink_kernel");
+}
+
+int mct_admm_rhs(const mct_geom* g, const float* bpb, const float* vy, const float* vx, const float* py,
+                 const float* px, float rho, float* out, void* stream) {
+    MCT_REQUIRE(g && bpb && vy && vx && py && px && out && g->nx >= 1 && g->nz >= 1, "mct_admm_rhs: bad arguments");
+    admm_rhs_kernel<<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, bpb, vy, vx, py, px, rho,
+                                                                          out);
+    return launched("admm_rhs_kernel");
 }
 
 int mct_dtwd(const mct_geom* g, const float* x, const float* wr, float s, const float* out_in, float a, float* out,

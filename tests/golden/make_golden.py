@@ -116,6 +116,12 @@ IR_CASES = {
     "ir_piccs": _upd(BASE_IR, Alpha=0.5),
 }
 
+# ADMM-TV (run_mgfbp_iterative_recon_ADMM_CGLS.py); Lambda puts the shrink threshold
+# (lambda * ratio / rho) inside the range of the image gradients
+ADMM_CASES = {
+    "ir_admm": _upd(BASE_IR, Alpha=0.5, Lambda=4e-4, NumberOfIRNIterations=3, NumberOfIterations=2),
+}
+
 # the view-by-view FBP (run_mgfbp_v2.py): same configs, its own driver
 FBPV2_CASES = {
     "fbpv2_cone": _upd(BASE_CONE),
@@ -198,6 +204,32 @@ def run_helical_case(name, cfg, RH, rng):
         return dict(config=json.dumps(cfg), input_sgm=sgm, recon=np.asarray(img, np.float64),
                     rebinned=rebinned.reshape(len(fbp.array_z_pos), fbp.view_count, -1).astype(np.float64),
                     z_pos=np.asarray(fbp.array_z_pos, np.float64))
+
+
+def run_admm_case(name, cfg, RA, R, rng):
+    cfg = _clean(cfg)
+    with tempfile.TemporaryDirectory() as d, _chdir(d):
+        os.makedirs("sgm")
+        cfg.update(InputDir=d + "/sgm", OutputDir=d + "/rec")
+        n, nz = cfg["ImageDimension"], cfg["ImageDimensionZ"]
+        nu, nv, nb = cfg["DetectorElementCountHorizontal"], cfg["DetectorElementCountVertical"], cfg["Views"]
+        sgm = (rng.uniform(0.0, 0.4, (nv, nb, nu)) + 0.1).astype(np.float32)
+        sgm.transpose(1, 0, 2).tofile("sgm/sgm_a.raw")
+        prior = (rng.uniform(-200, 200, (nz, n, n))).astype(np.float32)
+        prior.tofile("prior.raw")
+        cfg["PriorImageFile"] = d + "/prior.raw"
+        json.dump(cfg, open("config.jsonc", "w"))
+        seed = R.Mgfbp(R.ReadConfigFile("config.jsonc")).MainFunction()
+        obj = RA.Mgfbp_ir_piccs(R.ReadConfigFile("config.jsonc"))
+        img = obj.MainFunction(np.array(seed))
+        return dict(config=json.dumps(cfg), input_sgm=sgm, prior=prior, fbp_seed=np.asarray(seed, np.float64),
+                    recon=np.asarray(img, np.float64), v_x=np.asarray(obj.v_x, np.float64),
+                    v_y=np.asarray(obj.v_y, np.float64), p_x=np.asarray(obj.p_x, np.float64),
+                    p_y=np.asarray(obj.p_y, np.float64), ptp_calls=obj.num_iter_runned,
+                    emap=np.asarray(obj.img_fp_effective_map, np.float64),
+                    bp_b=np.asarray(obj.img_bp_b, np.float64), u=_arr(obj.array_u_taichi),
+                    v=_arr(obj.array_v_taichi), angles=_arr(obj.array_angle_taichi),
+                    cz=_arr(obj.array_img_center_z_taichi).ravel())
 
 
 def run_pmatrix_case(name, spec, R, rng):
@@ -386,17 +418,19 @@ def main():
     import run_mgfpj_v2 as R2
     import run_mgfbp_v2 as RV2
     import run_mgfbp_helical as RH
+    import run_mgfbp_iterative_recon_ADMM_CGLS as RA
     # NumPy >= 2 no longer turns size-1 arrays into Python scalars in math.cos & co.;
     # the reference relies on that (run_mgfbp.py:738-741, on least-squares solutions of
     # shape (3, 1)), so its modules get a math whose functions convert them first, as
     # the NumPy of the reference's time did.
-    for mod in (R, R3, RI, RP, R1, R2, RV2, RH):
+    for mod in (R, R3, RI, RP, R1, R2, RV2, RH, RA):
         if hasattr(mod, "math"):
             mod.math = _MathCompat()
     jobs = [(k, v, "fbp") for k, v in FBP_CASES.items()] + [(k, v, "fpj") for k, v in FPJ_CASES.items()] \
         + [(k, v, "ir") for k, v in IR_CASES.items()] + [(k, v, "v1") for k, v in FPJ_V1_CASES.items()] \
         + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()] + [(k, v, "pm") for k, v in PM_CASES.items()] \
-        + [(k, v, "fbpv2") for k, v in FBPV2_CASES.items()] + [(k, v, "helical") for k, v in HELICAL_CASES.items()]
+        + [(k, v, "fbpv2") for k, v in FBPV2_CASES.items()] + [(k, v, "helical") for k, v in HELICAL_CASES.items()] \
+        + [(k, v, "admm") for k, v in ADMM_CASES.items()]
     for i, (name, cfg, kind) in enumerate(jobs):
         if only and name not in only:
             continue
@@ -414,6 +448,8 @@ def main():
                 out = run_fbpv2_case(name, cfg, RV2, rng)
             elif kind == "helical":
                 out = run_helical_case(name, cfg, RH, rng)
+            elif kind == "admm":
+                out = run_admm_case(name, cfg, RA, R, rng)
             elif kind in ("v1", "v2"):
                 out = run_fpj_variant_case(name, cfg, R1 if kind == "v1" else R2, rng)
             else:

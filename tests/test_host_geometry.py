@@ -63,7 +63,7 @@ def test_fpj_arrays(name, tmp_path):
     np.testing.assert_allclose(o.array_img_center_z, z["cz"], rtol=0, atol=1e-6)  # float32 in the reference
 
 
-@pytest.mark.parametrize("name", golden_names("ir"))
+@pytest.mark.parametrize("name", golden_names("ir", exclude=["ir_admm"]))
 def test_ir_arrays(name, tmp_path):
     z = load_golden(name)
     o = _parse(z["config"], "ir", tmp_path)
