@@ -218,7 +218,7 @@ def run_gpu(args, w):
         dist.init_process_group("nccl")
     o = parse(w)
     pipe = fbp.FdkPipeline(o, device=dev, storage=args.storage)
-    pipe.taps.copy_(torch.tensor(hann_from_ramp(geometry.recon_taps(o)), dtype=torch.float32))
+    pipe.set_taps(hann_from_ramp(geometry.recon_taps(o)))
     fpg = geometry.fpj_geometry(o, device=dev)
     # synthetic data (not timed)
     ell = ellipsoids(w)
@@ -355,11 +355,12 @@ def run_gpu(args, w):
             "fdk_rmse_vs_phantom": {"plain": r_plain, "mixed": r_mixed, "ratio": round(r_mixed / r_plain, 5)},
             "fdk_rel_l2_vs_plain": float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol)),
             "fp_rel_l2_vs_plain": float(torch.linalg.vector_norm(fp_m - ref_fp) / torch.linalg.vector_norm(ref_fp)),
-            "storage": "sinogram filter split-bf16 on tcgen05; bf16 backprojection coefficients; bf16 FP cells",
+            "storage": "split-bf16 tcgen05 row filter; bf16 backprojection coefficients; bf16 FP cells",
         }
         del pm, ph, live, fp_m
-        for name, storage in (("tc_filter", "f32"), ("tc_filter_bf16_bp", "bf16")):
-            pm = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl="tc")
+        for name, storage, impl in (("tc_filter", "f32", "tc"), ("tc_filter_bf16_bp", "bf16", "tc"),
+                                    ("tc_filter_f16_bp", "f16", "tc")):
+            pm = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl=impl)
             pm.set_taps(pipe.taps.cpu().numpy())
             for _ in range(2):
                 mv = pm.run(sgm)
@@ -374,7 +375,8 @@ def run_gpu(args, w):
             pm.filter(sgm)
             f1.record(stream)
             barrier()
-            pm.tc.status()
+            if pm.tc is not None:
+                pm.tc.status()
             mms = m0.elapsed_time(m1) / args.steps
             rel = float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol))
             mixed[name] = {"fdk_ms": round(mms, 3), "weight_filter_ms": round(f0.elapsed_time(f1), 3),
@@ -405,7 +407,8 @@ def run_gpu(args, w):
             "data": "synthetic: 20 seeded ellipsoids, exact line integrals, Poisson noise at 1e5 photons",
             "config": {"workload": f"FDK+FP {w['nx']}x{w['nx']}x{w['nz']} vol @{w['px']}mm, {w['views']} views/360deg, "
                                    f"{w['nu']}x{w['nv']} flat det @{w['du']}mm, SID {w['sid']:.0f} SDD {w['sdd']:.0f}",
-                       "filter": "ramp x Hann (spatial composition of the reference ramp)",
+                       "filter": "ramp x Hann (spatial composition of the reference ramp); float32 Toeplitz row "
+                                 "filter (the mixed step uses the split-bf16 tcgen05 product)",
                        "fp_step": w["step"], "l2": "inputs larger than L2 (sinogram 1.13 GB, volume 268 MB)",
                        "parallelism": "replicas only" if world > 1 else "single GPU"},
             "stages_ms": {"weight_filter": round(float(st[0]), 3), "pack": round(float(st[1]), 3),

@@ -89,6 +89,7 @@ class _FbpSlot:
         self.graph = None
         self.last_used = time.perf_counter()
         self.nbytes = sum(p.weighted.numel() * 4 + p.filtered.numel() * 4 + p.packed.numel() + p.vol.numel() * 4
+                          + (p.tc._buf.numel() if p.tc is not None else 0)
                           for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
             self._capture()
@@ -247,8 +248,8 @@ class ReconServer:
         o = req.obj
         nvol = o.img_dim * o.img_dim * o.img_dim_z * 4
         nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
-        if req.kind == "fbp":
-            return nsgm * 7 + 2 * nvol
+        if req.kind == "fbp":  # input, weighted, filtered, packed (4x), tensor-core operand tiles
+            return nsgm * 8 + 2 * nvol
         return 8 * nvol + 3 * nsgm
 
     def _batch_for(self, req):
