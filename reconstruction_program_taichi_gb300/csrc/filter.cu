@@ -46,30 +46,35 @@ __device__ float parker(const WeightParams& p, float beta, float u) {
     return w;
 }
 
+// One block per (row, view) line of nu elements (grid-stride over lines), so the
+// line's row, view and source offset are computed once per line, not per element.
 __global__ void weight_kernel(WeightParams p, const float* __restrict__ in, const float* __restrict__ bh,
                               const float* __restrict__ angles, float* __restrict__ out) {
-    int64_t n = (int64_t)p.nv * p.views * p.nu;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int c = (int)(i % p.nu);
-        int64_t rj = i / p.nu;
-        int j = (int)(rj % p.views);
-        int r = (int)(rj / p.views);
-        float val = in[r * p.row_stride + j * p.view_stride + c];
-        if (p.n_bh > 0) {
-            float acc = 0.0f, pw = val;
-            for (int t = 0; t < p.n_bh; ++t) {
-                acc += bh[t] * pw;
-                pw *= val;
+    const int64_t lines = (int64_t)p.nv * p.views;
+    for (int64_t rj = blockIdx.x; rj < lines; rj += gridDim.x) {
+        const int j = (int)(rj % p.views);
+        const int r = (int)(rj / p.views);
+        const float* src = in + r * p.row_stride + j * p.view_stride;
+        float* dst = out + rj * p.nu;
+        const float v = p.v0 + r * p.v_step;
+        const float beta = p.short_scan ? fabsf(angles[p.view_begin + j] - angles[0]) : 0.0f;
+        for (int c = threadIdx.x; c < p.nu; c += blockDim.x) {
+            float val = src[c];
+            if (p.n_bh > 0) {
+                float acc = 0.0f, pw = val;
+                for (int t = 0; t < p.n_bh; ++t) {
+                    acc += bh[t] * pw;
+                    pw *= val;
+                }
+                val = acc;
             }
-            val = acc;
+            const float u = p.u0 + c * p.u_step;
+            const float sdd = p.sdd;
+            if (p.curved) val = val * sdd * cosf((-1.0f) * u / sdd) * sdd / sqrtf(sdd * sdd + v * v);
+            else val = (val * sdd * sdd) / sqrtf(sdd * sdd + u * u + v * v);
+            if (p.short_scan) val *= parker(p, beta, u);
+            dst[c] = val;
         }
-        float u = p.u0 + c * p.u_step;
-        float v = p.v0 + r * p.v_step;
-        float sdd = p.sdd;
-        if (p.curved) val = val * sdd * cosf((-1.0f) * u / sdd) * sdd / sqrtf(sdd * sdd + v * v);
-        else val = (val * sdd * sdd) / sqrtf(sdd * sdd + u * u + v * v);
-        if (p.short_scan) val *= parker(p, fabsf(angles[p.view_begin + j] - angles[0]), u);
-        out[i] = val;
     }
 }
 
@@ -312,8 +317,9 @@ int mct_weight(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t
     float PI = (float)kPI;
     p.num_rounds = floorf(fabsf(p.scan) / (PI * 2));
     p.remain = fabsf(p.scan) - p.num_rounds * PI * 2;
-    int64_t n = sgm_elems(*g);
-    weight_kernel<<<grid_for(n), 256, 0, as_stream(stream)>>>(p, sgm, bh_coeffs, t ? t->angles : nullptr, weighted);
+    const int64_t lines = (int64_t)g->nv * g->views;
+    const int blocks = (int)(lines < 152 * 64 ? lines : 152 * 64);
+    weight_kernel<<<blocks, 256, 0, as_stream(stream)>>>(p, sgm, bh_coeffs, t ? t->angles : nullptr, weighted);
     return launched("weight_kernel");
 }
 

@@ -8,13 +8,16 @@
 //
 // Operand layout.  A and B^T are stored pre-tiled in global memory exactly as one
 // pipeline stage needs them in shared memory (tcgen05 canonical K-major layout, no
-// swizzle): a 128x64 (A) or 256x64 (B^T) bf16 tile is one contiguous block of 8x8
+// swizzle): a 128x32 (A) or 256x32 (B^T) bf16 tile is one contiguous block of 8x8
 // "core matrices" (8 rows x 16 bytes each); core (row group i, k group j) sits at
-// byte (i*8 + j)*128.  So the K-direction core stride (LBO) is 128 B and the
-// row-direction stride (SBO) is 1 KiB, and each stage is filled by plain bulk copies
+// byte (i*4 + j)*128.  So the K-direction core stride (LBO) is 128 B and the
+// row-direction stride (SBO) is 512 B, and each stage is filled by plain bulk copies
 // (cp.async.bulk, the TMA engine) of contiguous tiles.
 //
-// Kernel structure: 128 threads.  Thread 0 issues the bulk copies of a 2-stage ring,
+// Kernel structure: 128 threads, two CTAs per SM (98 KiB of shared memory and 256
+// tensor-memory columns each), so that one CTA's epilogue overlaps the other's MMAs
+// (with one CTA per SM the tensor pipe idled during every epilogue: 29 % busy).
+// Thread 0 issues the bulk copies of a 2-stage ring (48 KiB per stage),
 // thread 32 issues tcgen05.mma (M=128, N=256, K=16; 3 products per K step) and
 // commits each stage back to the producer; after the last stage all four warps read
 // the 128x256 float32 accumulator from tensor memory (warp w owns lanes 32w..32w+31)
@@ -29,10 +32,13 @@
 namespace mct {
 namespace {
 
-constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 2;
-constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                    // 16 KiB
-constexpr int TC_B_TILE = TC_BN * TC_BK * 2;                    // 32 KiB
-constexpr int TC_STAGE_BYTES = 2 * TC_A_TILE + 2 * TC_B_TILE;   // 96 KiB
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 32, TC_STAGES = 2;
+constexpr int TC_KG = TC_BK / 8;                                // core matrices along K per tile row group
+constexpr int TC_SBO = TC_KG * 128;                             // bytes between row groups (512)
+constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                    // 8 KiB
+constexpr int TC_B_TILE = TC_BN * TC_BK * 2;                    // 16 KiB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_TILE + 2 * TC_B_TILE;   // 48 KiB
+static_assert(TC_STAGES * TC_STAGE_BYTES + 2048 <= 227 * 1024, "shared memory budget");
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 2048;      // + 1 KiB alignment slack + barriers
 constexpr int TC_TMEM_COLS = 256;
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;        // 2 s
@@ -69,9 +75,10 @@ __global__ void split_a_kernel(const float* __restrict__ x, int64_t rows, int nu
                                uint4* __restrict__ a_hi, uint4* __restrict__ a_lo) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
         const int r8 = (int)(i & 7);
-        const int kj = (int)((i >> 3) & 7);
-        const int mi = (int)((i >> 6) & 15);
-        const int64_t tile = i >> 10;
+        const int kj = (int)((i >> 3) % TC_KG);
+        const int64_t rest = (i >> 3) / TC_KG;
+        const int mi = (int)(rest % (TC_BM / 8));
+        const int64_t tile = rest / (TC_BM / 8);
         const int kb = (int)(tile % KB);
         const int64_t mb = tile / KB;
         const int64_t R = mb * TC_BM + mi * 8 + r8;
@@ -94,9 +101,10 @@ __global__ void build_b_kernel(const float* __restrict__ taps, int nu, int KB, i
                                uint4* __restrict__ b_hi, uint4* __restrict__ b_lo) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
         const int r8 = (int)(i & 7);
-        const int kj = (int)((i >> 3) & 7);
-        const int ni = (int)((i >> 6) & 31);
-        const int64_t tile = i >> 11;
+        const int kj = (int)((i >> 3) % TC_KG);
+        const int64_t rest = (i >> 3) / TC_KG;
+        const int ni = (int)(rest % (TC_BN / 8));
+        const int64_t tile = rest / (TC_BN / 8);
         const int kb = (int)(tile % KB);
         const int nb = (int)(tile / KB);
         const int n = nb * TC_BN + ni * 8 + r8;
@@ -194,7 +202,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
 tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict__ a_hi, const uint4* __restrict__ a_lo,
                  const uint4* __restrict__ b_hi, const uint4* __restrict__ b_lo, float* __restrict__ F,
                  int* __restrict__ err) {
@@ -265,8 +273,8 @@ tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict_
 #pragma unroll
             for (int ks = 0; ks < TC_BK / 16; ++ks) {
                 const uint32_t off = ks * 256;  // two core matrices along K
-                const uint64_t dah = smem_desc(ahi + off, 128, 1024), dal = smem_desc(alo + off, 128, 1024);
-                const uint64_t dbh = smem_desc(bhi + off, 128, 1024), dbl = smem_desc(blo + off, 128, 1024);
+                const uint64_t dah = smem_desc(ahi + off, 128, TC_SBO), dal = smem_desc(alo + off, 128, TC_SBO);
+                const uint64_t dbh = smem_desc(bhi + off, 128, TC_SBO), dbl = smem_desc(blo + off, 128, TC_SBO);
                 mma_bf16(tmem, dah, dbh, idesc, (kb | ks) != 0);
                 mma_bf16(tmem, dah, dbl, idesc, 1);
                 mma_bf16(tmem, dal, dbh, idesc, 1);
@@ -294,9 +302,16 @@ tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict_
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
             if (row_ok) {
                 const int n0 = nbk * TC_BN + c0;
+                if ((d.nu & 3) == 0 && n0 + 16 <= d.nu) {  // 16-byte aligned full chunk: vector stores
+                    float4* q = reinterpret_cast<float4*>(dst + n0);
 #pragma unroll
-                for (int i = 0; i < 16; ++i)
-                    if (n0 + i < d.nu) dst[n0 + i] = v[i] * du;
+                    for (int i = 0; i < 4; ++i)
+                        q[i] = make_float4(v[4 * i] * du, v[4 * i + 1] * du, v[4 * i + 2] * du, v[4 * i + 3] * du);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        if (n0 + i < d.nu) dst[n0 + i] = v[i] * du;
+                }
             }
         }
     }
