@@ -355,11 +355,11 @@ def run_gpu(args, w):
             "fdk_rmse_vs_phantom": {"plain": r_plain, "mixed": r_mixed, "ratio": round(r_mixed / r_plain, 5)},
             "fdk_rel_l2_vs_plain": float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol)),
             "fp_rel_l2_vs_plain": float(torch.linalg.vector_norm(fp_m - ref_fp) / torch.linalg.vector_norm(ref_fp)),
-            "storage": "split-bf16 tcgen05 row filter; bf16 backprojection coefficients; bf16 FP cells",
+            "storage": "two-part split-bf16 tcgen05 row filter; bf16 backprojection coefficients; bf16 FP cells",
         }
         del pm, ph, live, fp_m
-        for name, storage, impl in (("tc_filter", "f32", "tc"), ("tc_filter_bf16_bp", "bf16", "tc"),
-                                    ("tc_filter_f16_bp", "f16", "tc")):
+        for name, storage, impl in (("simt_filter_f32", "f32", "simt"), ("tc2_filter_f32", "f32", "tc"),
+                                    ("tc2_filter_bf16_bp", "bf16", "tc"), ("tc2_filter_f16_bp", "f16", "tc")):
             pm = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl=impl)
             pm.set_taps(pipe.taps.cpu().numpy())
             for _ in range(2):
@@ -407,8 +407,9 @@ def run_gpu(args, w):
             "data": "synthetic: 20 seeded ellipsoids, exact line integrals, Poisson noise at 1e5 photons",
             "config": {"workload": f"FDK+FP {w['nx']}x{w['nx']}x{w['nz']} vol @{w['px']}mm, {w['views']} views/360deg, "
                                    f"{w['nu']}x{w['nv']} flat det @{w['du']}mm, SID {w['sid']:.0f} SDD {w['sdd']:.0f}",
-                       "filter": "ramp x Hann (spatial composition of the reference ramp); float32 Toeplitz row "
-                                 "filter (the mixed step uses the split-bf16 tcgen05 product)",
+                       "filter": "ramp x Hann (spatial composition of the reference ramp); Toeplitz row product on "
+                                 "tcgen05 tensor cores from three bf16 parts per float32 operand (~1e-6 of float32); "
+                                 "the mixed step uses two parts",
                        "fp_step": w["step"], "l2": "inputs larger than L2 (sinogram 1.13 GB, volume 268 MB)",
                        "parallelism": "replicas only" if world > 1 else "single GPU"},
             "stages_ms": {"weight_filter": round(float(st[0]), 3), "pack": round(float(st[1]), 3),

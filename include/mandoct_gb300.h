@@ -114,18 +114,23 @@ int mct_vgauss(const mct_geom* g, const float* weighted, const float* gauss_taps
 int mct_filter(const mct_geom* g, const float* weighted, const float* taps, float* filtered,
                void* stream);
 
-/* Tensor-core (tcgen05) split-BF16 variant of mct_filter: the float32 operands are
- * split into bf16 hi + lo parts and A_hi B_hi + A_hi B_lo + A_lo B_hi is accumulated in
- * float32 tensor memory (relative error ~1e-5).  workspace: device buffer of
- * mct_filter_tc_workspace_size bytes, 1 KiB aligned, holding the tiled operands; call
- * mct_filter_tc_prepare once per filter taps (it also clears the timeout flag), then
- * mct_filter_tc per sinogram.  Replaces Mgfbp.ConvolveSgmAndKernel run_mgfbp.py:1030-1046.
+/* Tensor-core (tcgen05) variant of mct_filter: the float32 operands are split into
+ * bf16 parts and the part products are accumulated in float32 tensor memory.
+ * dtype MCT_F32: hi + mid + lo parts, the six products of total order <= 2 (the dropped
+ * terms are ~2^-24 relative; ~1e-6 overall, the tensor pipe's float32 accumulation).
+ * dtype MCT_BF16: hi + lo parts, A_hi B_hi + A_hi B_lo + A_lo B_hi (~1e-5 relative; up to
+ * ~1e-4 on small detectors).
+ * workspace: device buffer of mct_filter_tc_workspace_size(g, dtype) bytes, 1 KiB
+ * aligned, holding the tiled operands; call mct_filter_tc_prepare once per filter taps
+ * (it also clears the timeout flag), then mct_filter_tc per sinogram, with the same
+ * dtype.  Replaces Mgfbp.ConvolveSgmAndKernel run_mgfbp.py:1030-1046.
  * mct_filter_tc_status synchronises the stream and returns MCT_E_TIMEOUT if a bounded
  * pipeline wait of an earlier launch gave up. */
-size_t mct_filter_tc_workspace_size(const mct_geom* g);
-int mct_filter_tc_prepare(const mct_geom* g, const float* taps, void* workspace, void* stream);
-int mct_filter_tc(const mct_geom* g, const float* weighted, void* workspace, float* filtered, void* stream);
-int mct_filter_tc_status(const mct_geom* g, void* workspace, void* stream);
+size_t mct_filter_tc_workspace_size(const mct_geom* g, int32_t dtype);
+int mct_filter_tc_prepare(const mct_geom* g, const float* taps, int32_t dtype, void* workspace, void* stream);
+int mct_filter_tc(const mct_geom* g, const float* weighted, int32_t dtype, void* workspace, float* filtered,
+                  void* stream);
+int mct_filter_tc_status(const mct_geom* g, int32_t dtype, void* workspace, void* stream);
 
 /* Bytes of the packed backprojection operand for storage type dtype. */
 size_t mct_packed_size(const mct_geom* g, int32_t dtype);

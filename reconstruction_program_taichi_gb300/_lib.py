@@ -76,10 +76,10 @@ SIGNATURES = {
     "mct_weight": (ctypes.c_int, [_G, _T, _P, _i64, _i64, _P, _i32, _P, _P]),
     "mct_vgauss": (ctypes.c_int, [_G, _P, _P, _P, _P]),
     "mct_filter": (ctypes.c_int, [_G, _P, _P, _P, _P]),
-    "mct_filter_tc_workspace_size": (ctypes.c_size_t, [_G]),
-    "mct_filter_tc_prepare": (ctypes.c_int, [_G, _P, _P, _P]),
-    "mct_filter_tc": (ctypes.c_int, [_G, _P, _P, _P, _P]),
-    "mct_filter_tc_status": (ctypes.c_int, [_G, _P, _P]),
+    "mct_filter_tc_workspace_size": (ctypes.c_size_t, [_G, _i32]),
+    "mct_filter_tc_prepare": (ctypes.c_int, [_G, _P, _i32, _P, _P]),
+    "mct_filter_tc": (ctypes.c_int, [_G, _P, _i32, _P, _P, _P]),
+    "mct_filter_tc_status": (ctypes.c_int, [_G, _i32, _P, _P]),
     "mct_packed_size": (ctypes.c_size_t, [_G, _i32]),
     "mct_pack": (ctypes.c_int, [_G, _P, _P, _i32, _P]),
     "mct_pack_strided": (ctypes.c_int, [_G, _P, _i64, _i64, _P, _i32, _P]),

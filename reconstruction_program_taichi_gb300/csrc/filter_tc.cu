@@ -32,16 +32,37 @@
 namespace mct {
 namespace {
 
-constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 32, TC_STAGES = 2;
-constexpr int TC_KG = TC_BK / 8;                                // core matrices along K per tile row group
-constexpr int TC_SBO = TC_KG * 128;                             // bytes between row groups (512)
-constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                    // 8 KiB
-constexpr int TC_B_TILE = TC_BN * TC_BK * 2;                    // 16 KiB
-constexpr int TC_STAGE_BYTES = 2 * TC_A_TILE + 2 * TC_B_TILE;   // 48 KiB
-static_assert(TC_STAGES * TC_STAGE_BYTES + 2048 <= 227 * 1024, "shared memory budget");
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 2048;      // + 1 KiB alignment slack + barriers
+constexpr int TC_BM = 128, TC_BN = 256, TC_STAGES = 2;
 constexpr int TC_TMEM_COLS = 256;
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;        // 2 s
+
+// NS = number of bf16 parts each float32 operand is split into:
+//   2: x = hi + lo, products hi*hi + hi*lo + lo*hi (~1e-5 relative; the mixed path);
+//   3: x = hi + mid + lo, products of total order <= 2 (hi*hi, hi*mid, mid*hi, hi*lo,
+//      lo*hi, mid*mid): the dropped terms are ~2^-24 relative; the result is within
+//      ~1e-6 of float32 (the level of the tensor pipe's float32 accumulation).
+// BK (K depth of one pipeline stage) keeps a stage small enough for two CTAs per SM.
+template <int NS>
+struct TcCfg;
+template <>
+struct TcCfg<2> {
+    static constexpr int BK = 32, NPROD = 3;
+};
+template <>
+struct TcCfg<3> {
+    static constexpr int BK = 16, NPROD = 6;
+};
+template <int NS>
+struct TcTiles {
+    static constexpr int BK = TcCfg<NS>::BK;
+    static constexpr int KG = BK / 8;                          // core matrices along K per row group
+    static constexpr int SBO = KG * 128;                       // bytes between row groups
+    static constexpr int A_TILE = TC_BM * BK * 2;
+    static constexpr int B_TILE = TC_BN * BK * 2;
+    static constexpr int STAGE = NS * (A_TILE + B_TILE);
+    static constexpr int SMEM = TC_STAGES * STAGE + 2048;      // + 1 KiB alignment slack + barriers
+    static_assert(2 * SMEM <= 228 * 1024, "two CTAs per SM");
+};
 
 struct TcDims {
     int64_t rows;    // M (sinogram rows)
@@ -49,75 +70,92 @@ struct TcDims {
     int mb, kb, nb;  // tile counts along M, K, N
 };
 
+template <int NS>
 inline TcDims tc_dims(int64_t rows, int nu) {
     TcDims d;
     d.rows = rows;
     d.nu = nu;
     d.mb = (int)((rows + TC_BM - 1) / TC_BM);
-    d.kb = (nu + TC_BK - 1) / TC_BK;
+    d.kb = (nu + TcTiles<NS>::BK - 1) / TcTiles<NS>::BK;
     d.nb = (nu + TC_BN - 1) / TC_BN;
     return d;
 }
 
-__device__ __forceinline__ uint32_t bf16_bits(float x) { return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x)); }
-
-// split x into bf16 hi + lo (bit patterns)
-__device__ __forceinline__ void split2(float x, uint32_t& hi, uint32_t& lo) {
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    hi = (uint32_t)__bfloat16_as_ushort(h);
-    lo = bf16_bits(x - __bfloat162float(h));
+// x as NS bf16 parts (bit patterns), largest first; each part is the bf16 rounding of
+// what the previous parts leave
+template <int NS>
+__device__ __forceinline__ void split_parts(float x, uint32_t* out) {
+    float r = x;
+#pragma unroll
+    for (int p = 0; p < NS; ++p) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(r);
+        out[p] = (uint32_t)__bfloat16_as_ushort(h);
+        r = r - __bfloat162float(h);
+    }
 }
 
-// Thread i writes one 16-byte core-matrix row (8 bf16 along K) of the hi and lo
-// A tiles.  i enumerates (tile = mb*KB + kb, row group mi, k group kj, row r8) in
-// storage order, so consecutive threads write consecutive 16-byte chunks.
-__global__ void split_a_kernel(const float* __restrict__ x, int64_t rows, int nu, int KB, int64_t n_chunks,
-                               uint4* __restrict__ a_hi, uint4* __restrict__ a_lo) {
+// One 16-byte core-matrix row (8 bf16 along K) of every part of a tile.  Chunk i
+// enumerates (tile, row group, k group kj, row r8) in storage order, so consecutive
+// threads write consecutive 16-byte chunks.  ROWS = 128 (A) or 256 (B^T).
+template <int NS, int ROWS>
+__device__ __forceinline__ void tile_coords(int64_t i, int KB, int& r8, int& kj, int& gi, int& kb, int64_t& tb) {
+    constexpr int KG = TcTiles<NS>::KG;
+    r8 = (int)(i & 7);
+    kj = (int)((i >> 3) % KG);
+    const int64_t rest = (i >> 3) / KG;
+    gi = (int)(rest % (ROWS / 8));
+    const int64_t tile = rest / (ROWS / 8);
+    kb = (int)(tile % KB);
+    tb = tile / KB;
+}
+
+template <int NS>
+__device__ __forceinline__ void store_parts(uint4* const* dst, int64_t i, const uint32_t (*v)[NS]) {
+#pragma unroll
+    for (int p = 0; p < NS; ++p)
+        dst[p][i] = make_uint4(v[0][p] | (v[1][p] << 16), v[2][p] | (v[3][p] << 16), v[4][p] | (v[5][p] << 16),
+                               v[6][p] | (v[7][p] << 16));
+}
+
+struct Parts {
+    uint4* p[3];
+};
+
+template <int NS>
+__global__ void split_a_kernel(const float* __restrict__ x, int64_t rows, int nu, int KB, int64_t n_chunks, Parts a) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
-        const int r8 = (int)(i & 7);
-        const int kj = (int)((i >> 3) % TC_KG);
-        const int64_t rest = (i >> 3) / TC_KG;
-        const int mi = (int)(rest % (TC_BM / 8));
-        const int64_t tile = rest / (TC_BM / 8);
-        const int kb = (int)(tile % KB);
-        const int64_t mb = tile / KB;
+        int r8, kj, mi, kb;
+        int64_t mb;
+        tile_coords<NS, TC_BM>(i, KB, r8, kj, mi, kb, mb);
         const int64_t R = mb * TC_BM + mi * 8 + r8;
-        const int m0 = kb * TC_BK + kj * 8;
-        uint32_t h[8], l[8];
+        const int m0 = kb * TcTiles<NS>::BK + kj * 8;
+        uint32_t v[8][NS];
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             const int m = m0 + c;
-            const float v = (R < rows && m < nu) ? x[R * nu + m] : 0.0f;
-            split2(v, h[c], l[c]);
+            split_parts<NS>((R < rows && m < nu) ? x[R * nu + m] : 0.0f, v[c]);
         }
-        a_hi[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
-        a_lo[i] = make_uint4(l[0] | (l[1] << 16), l[2] | (l[3] << 16), l[4] | (l[5] << 16), l[6] | (l[7] << 16));
+        store_parts<NS>(a.p, i, v);
     }
 }
 
 // B^T element (n, k) = T[k][n] = h[n - k + nu - 1] (output column n, input column k),
-// tiled like A with 256-row tiles: chunk i enumerates (tile = nb*KB + kb, ni, kj, r8).
-__global__ void build_b_kernel(const float* __restrict__ taps, int nu, int KB, int64_t n_chunks,
-                               uint4* __restrict__ b_hi, uint4* __restrict__ b_lo) {
+// tiled like A with 256-row tiles.
+template <int NS>
+__global__ void build_b_kernel(const float* __restrict__ taps, int nu, int KB, int64_t n_chunks, Parts b) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
-        const int r8 = (int)(i & 7);
-        const int kj = (int)((i >> 3) % TC_KG);
-        const int64_t rest = (i >> 3) / TC_KG;
-        const int ni = (int)(rest % (TC_BN / 8));
-        const int64_t tile = rest / (TC_BN / 8);
-        const int kb = (int)(tile % KB);
-        const int nb = (int)(tile / KB);
-        const int n = nb * TC_BN + ni * 8 + r8;
-        const int k0 = kb * TC_BK + kj * 8;
-        uint32_t h[8], l[8];
+        int r8, kj, ni, kb;
+        int64_t nb;
+        tile_coords<NS, TC_BN>(i, KB, r8, kj, ni, kb, nb);
+        const int n = (int)nb * TC_BN + ni * 8 + r8;
+        const int k0 = kb * TcTiles<NS>::BK + kj * 8;
+        uint32_t v[8][NS];
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             const int k = k0 + c;
-            const float v = (n < nu && k < nu) ? taps[n - k + nu - 1] : 0.0f;
-            split2(v, h[c], l[c]);
+            split_parts<NS>((n < nu && k < nu) ? taps[n - k + nu - 1] : 0.0f, v[c]);
         }
-        b_hi[i] = make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
-        b_lo[i] = make_uint4(l[0] | (l[1] << 16), l[2] | (l[3] << 16), l[4] | (l[5] << 16), l[6] | (l[7] << 16));
+        store_parts<NS>(b.p, i, v);
     }
 }
 
@@ -202,14 +240,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+template <int NS>
 __global__ void __launch_bounds__(128, 2)
-tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict__ a_hi, const uint4* __restrict__ a_lo,
-                 const uint4* __restrict__ b_hi, const uint4* __restrict__ b_lo, float* __restrict__ F,
-                 int* __restrict__ err) {
+tc_filter_kernel(TcDims d, int nv, int views, float du, Parts a, Parts b, float* __restrict__ F, int* __restrict__ err) {
+    using T = TcTiles<NS>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1 KiB-aligned stage buffers
+    // 1 KiB-aligned stage buffers: [A part 0..NS-1][B part 0..NS-1] per stage
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* ctrl = smem + TC_STAGES * TC_STAGE_BYTES;  // barriers and the TMEM address
+    unsigned char* ctrl = smem + TC_STAGES * T::STAGE;  // barriers and the TMEM address
     uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);
     uint64_t* empty = full + TC_STAGES;
     uint64_t* done = empty + TC_STAGES;
@@ -239,21 +277,23 @@ tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict_
 
     bool ok = true;
     if (threadIdx.x == 0) {
-        // producer: bulk copies of A (hi, lo) and B (hi, lo) tiles for every K block
+        // producer: bulk copies of the A and B part tiles of every K block
         int issued = 0;
         for (int kb = 0; kb < d.kb && ok; ++kb) {
             const int s = kb % TC_STAGES;
             if (kb >= TC_STAGES) ok = mbar_wait(smem_u32(&empty[s]), ((kb / TC_STAGES) - 1) & 1, err, 1);
             if (!ok) break;
-            unsigned char* st = smem + s * TC_STAGE_BYTES;
+            unsigned char* st = smem + s * T::STAGE;
             const uint32_t bar = smem_u32(&full[s]);
-            mbar_expect_tx(bar, TC_STAGE_BYTES);
+            mbar_expect_tx(bar, T::STAGE);
             const int64_t at = mbk * d.kb + kb;
             const int64_t bt = (int64_t)nbk * d.kb + kb;
-            bulk_g2s(smem_u32(st), a_hi + at * (TC_A_TILE / 16), TC_A_TILE, bar);
-            bulk_g2s(smem_u32(st + TC_A_TILE), a_lo + at * (TC_A_TILE / 16), TC_A_TILE, bar);
-            bulk_g2s(smem_u32(st + 2 * TC_A_TILE), b_hi + bt * (TC_B_TILE / 16), TC_B_TILE, bar);
-            bulk_g2s(smem_u32(st + 2 * TC_A_TILE + TC_B_TILE), b_lo + bt * (TC_B_TILE / 16), TC_B_TILE, bar);
+#pragma unroll
+            for (int p = 0; p < NS; ++p) {
+                bulk_g2s(smem_u32(st + p * T::A_TILE), a.p[p] + at * (T::A_TILE / 16), T::A_TILE, bar);
+                bulk_g2s(smem_u32(st + NS * T::A_TILE + p * T::B_TILE), b.p[p] + bt * (T::B_TILE / 16), T::B_TILE,
+                         bar);
+            }
             issued = kb + 1;
         }
         // drain: the copies of the last issued block of every stage must have landed
@@ -261,23 +301,26 @@ tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict_
         for (int kb = (issued > TC_STAGES ? issued - TC_STAGES : 0); kb < issued; ++kb)
             mbar_wait(smem_u32(&full[kb % TC_STAGES]), (kb / TC_STAGES) & 1, err, 4);
     } else if (threadIdx.x == 32) {
-        // MMA issuer
+        // MMA issuer: the products of total order <= 1 (NS = 2) or <= 2 (NS = 3)
+        constexpr int NP = TcCfg<NS>::NPROD;
+        constexpr int pa[6] = {0, 0, 1, 0, 2, 1};
+        constexpr int pb[6] = {0, 1, 0, 2, 0, 1};
         const uint32_t idesc = idesc_bf16(TC_BM, TC_BN);
         for (int kb = 0; kb < d.kb && ok; ++kb) {
             const int s = kb % TC_STAGES;
             ok = mbar_wait(smem_u32(&full[s]), (kb / TC_STAGES) & 1, err, 2);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t st = smem_u32(smem + s * TC_STAGE_BYTES);
-            const uint32_t ahi = st, alo = st + TC_A_TILE, bhi = st + 2 * TC_A_TILE, blo = bhi + TC_B_TILE;
+            const uint32_t st = smem_u32(smem + s * T::STAGE);
 #pragma unroll
-            for (int ks = 0; ks < TC_BK / 16; ++ks) {
+            for (int ks = 0; ks < T::BK / 16; ++ks) {
                 const uint32_t off = ks * 256;  // two core matrices along K
-                const uint64_t dah = smem_desc(ahi + off, 128, TC_SBO), dal = smem_desc(alo + off, 128, TC_SBO);
-                const uint64_t dbh = smem_desc(bhi + off, 128, TC_SBO), dbl = smem_desc(blo + off, 128, TC_SBO);
-                mma_bf16(tmem, dah, dbh, idesc, (kb | ks) != 0);
-                mma_bf16(tmem, dah, dbl, idesc, 1);
-                mma_bf16(tmem, dal, dbh, idesc, 1);
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    const uint64_t da = smem_desc(st + pa[q] * T::A_TILE + off, 128, T::SBO);
+                    const uint64_t db = smem_desc(st + NS * T::A_TILE + pb[q] * T::B_TILE + off, 128, T::SBO);
+                    mma_bf16(tmem, da, db, idesc, (kb | ks | q) != 0);
+                }
             }
             mma_commit(smem_u32(&empty[s]));  // stage free once these MMAs complete
         }
@@ -322,6 +365,63 @@ tc_filter_kernel(TcDims d, int nv, int views, float du, const uint4* __restrict_
     }
 }
 
+// Workspace layout: [A parts][B parts][flag]
+template <int NS>
+size_t tc_workspace(const mct_geom* g, Parts* a, Parts* b, int** flag, void* ws) {
+    using T = TcTiles<NS>;
+    const TcDims d = tc_dims<NS>((int64_t)g->nv * g->views, g->nu);
+    const size_t as = (size_t)d.mb * d.kb * T::A_TILE, bs = (size_t)d.nb * d.kb * T::B_TILE;
+    if (ws) {
+        unsigned char* p = static_cast<unsigned char*>(ws);
+        for (int i = 0; i < NS; ++i) {
+            a->p[i] = reinterpret_cast<uint4*>(p + i * as);
+            b->p[i] = reinterpret_cast<uint4*>(p + NS * as + i * bs);
+        }
+        *flag = reinterpret_cast<int*>(p + NS * (as + bs));
+    }
+    return NS * (as + bs) + 256;
+}
+
+template <int NS>
+int tc_prepare(const mct_geom* g, const float* taps, void* ws, cudaStream_t s) {
+    Parts a{}, b{};
+    int* flag;
+    tc_workspace<NS>(g, &a, &b, &flag, ws);
+    const TcDims d = tc_dims<NS>((int64_t)g->nv * g->views, g->nu);
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    if (e != cudaSuccess) {
+        set_error("mct_filter_tc_prepare: %s", cudaGetErrorString(e));
+        return MCT_E_CUDA;
+    }
+    const int64_t chunks = (int64_t)d.nb * d.kb * (TcTiles<NS>::B_TILE / 16);
+    const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
+    build_b_kernel<NS><<<grid, 256, 0, s>>>(taps, g->nu, d.kb, chunks, b);
+    return launched("build_b_kernel");
+}
+
+template <int NS>
+int tc_run(const mct_geom* g, const float* weighted, void* ws, float* filtered, cudaStream_t s) {
+    Parts a{}, b{};
+    int* flag;
+    tc_workspace<NS>(g, &a, &b, &flag, ws);
+    const TcDims d = tc_dims<NS>((int64_t)g->nv * g->views, g->nu);
+    MCT_REQUIRE(d.mb < 65535 * 32, "mct_filter_tc: too many rows");
+    const int64_t chunks = (int64_t)d.mb * d.kb * (TcTiles<NS>::A_TILE / 16);
+    const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
+    split_a_kernel<NS><<<grid, 256, 0, s>>>(weighted, d.rows, g->nu, d.kb, chunks, a);
+    MCT_TRY(launched("split_a_kernel"));
+    // opt in to the large dynamic shared memory (per device, idempotent)
+    cudaError_t e = cudaFuncSetAttribute(tc_filter_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         TcTiles<NS>::SMEM);
+    if (e != cudaSuccess) {
+        set_error("mct_filter_tc: cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        return MCT_E_CUDA;
+    }
+    dim3 grid2(d.nb, d.mb);
+    tc_filter_kernel<NS><<<grid2, 128, TcTiles<NS>::SMEM, s>>>(d, g->nv, g->views, g->du, a, b, filtered, flag);
+    return launched("tc_filter_kernel");
+}
+
 }  // namespace
 }  // namespace mct
 
@@ -329,81 +429,41 @@ using namespace mct;
 
 extern "C" {
 
-size_t mct_filter_tc_workspace_size(const mct_geom* g) {
-    if (!g || g->nu < 2 || g->nv < 1 || g->views < 1) return 0;
-    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
-    const size_t a = (size_t)d.mb * d.kb * TC_A_TILE;
-    const size_t b = (size_t)d.nb * d.kb * TC_B_TILE;
-    return 2 * a + 2 * b + 256;  // hi+lo tiles of A and B, error flag
+size_t mct_filter_tc_workspace_size(const mct_geom* g, int32_t dtype) {
+    if (!g || g->nu < 2 || g->nv < 1 || g->views < 1 || (dtype != MCT_F32 && dtype != MCT_BF16)) return 0;
+    Parts a, b;
+    int* f;
+    return dtype == MCT_F32 ? tc_workspace<3>(g, &a, &b, &f, nullptr) : tc_workspace<2>(g, &a, &b, &f, nullptr);
 }
 
-// Workspace layout: [A_hi][A_lo][B_hi][B_lo][flag]
-static void tc_parts(const mct_geom* g, void* ws, uint4** ahi, uint4** alo, uint4** bhi, uint4** blo, int** flag) {
-    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
-    const size_t a = (size_t)d.mb * d.kb * TC_A_TILE;
-    const size_t b = (size_t)d.nb * d.kb * TC_B_TILE;
-    unsigned char* p = static_cast<unsigned char*>(ws);
-    *ahi = reinterpret_cast<uint4*>(p);
-    *alo = reinterpret_cast<uint4*>(p + a);
-    *bhi = reinterpret_cast<uint4*>(p + 2 * a);
-    *blo = reinterpret_cast<uint4*>(p + 2 * a + b);
-    *flag = reinterpret_cast<int*>(p + 2 * a + 2 * b);
-}
-
-int mct_filter_tc_prepare(const mct_geom* g, const float* taps, void* workspace, void* stream) {
+int mct_filter_tc_prepare(const mct_geom* g, const float* taps, int32_t dtype, void* workspace, void* stream) {
     MCT_TRY(check_geom(g, "mct_filter_tc_prepare"));
     MCT_REQUIRE(taps && workspace, "mct_filter_tc_prepare: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_filter_tc_prepare: dtype must be MCT_F32 or MCT_BF16");
     MCT_REQUIRE(((uintptr_t)workspace & 1023) == 0, "mct_filter_tc_prepare: workspace must be 1 KiB aligned");
-    uint4 *ahi, *alo, *bhi, *blo;
-    int* flag;
-    tc_parts(g, workspace, &ahi, &alo, &bhi, &blo, &flag);
-    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
-    cudaStream_t s = as_stream(stream);
-    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
-    if (e != cudaSuccess) {
-        set_error("mct_filter_tc_prepare: %s", cudaGetErrorString(e));
-        return MCT_E_CUDA;
-    }
-    const int64_t chunks = (int64_t)d.nb * d.kb * (TC_B_TILE / 16);
-    const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
-    build_b_kernel<<<grid, 256, 0, s>>>(taps, g->nu, d.kb, chunks, bhi, blo);
-    return launched("build_b_kernel");
+    return dtype == MCT_F32 ? tc_prepare<3>(g, taps, workspace, as_stream(stream))
+                            : tc_prepare<2>(g, taps, workspace, as_stream(stream));
 }
 
-int mct_filter_tc(const mct_geom* g, const float* weighted, void* workspace, float* filtered, void* stream) {
+int mct_filter_tc(const mct_geom* g, const float* weighted, int32_t dtype, void* workspace, float* filtered,
+                  void* stream) {
     MCT_TRY(check_geom(g, "mct_filter_tc"));
     MCT_REQUIRE(weighted && workspace && filtered, "mct_filter_tc: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_filter_tc: dtype must be MCT_F32 or MCT_BF16");
     MCT_REQUIRE(((uintptr_t)workspace & 1023) == 0, "mct_filter_tc: workspace must be 1 KiB aligned");
-    uint4 *ahi, *alo, *bhi, *blo;
-    int* flag;
-    tc_parts(g, workspace, &ahi, &alo, &bhi, &blo, &flag);
-    TcDims d = tc_dims((int64_t)g->nv * g->views, g->nu);
-    MCT_REQUIRE(d.mb < 65535 * 32, "mct_filter_tc: too many rows");
-    cudaStream_t s = as_stream(stream);
-    const int64_t chunks = (int64_t)d.mb * d.kb * (TC_A_TILE / 16);
-    const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
-    split_a_kernel<<<grid, 256, 0, s>>>(weighted, d.rows, g->nu, d.kb, chunks, ahi, alo);
-    MCT_TRY(launched("split_a_kernel"));
-    {
-        // opt in to the large dynamic shared memory (per device, idempotent)
-        cudaError_t e = cudaFuncSetAttribute(tc_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-        if (e != cudaSuccess) {
-            set_error("mct_filter_tc: cudaFuncSetAttribute: %s", cudaGetErrorString(e));
-            return MCT_E_CUDA;
-        }
-    }
-    dim3 grid2(d.nb, d.mb);
-    tc_filter_kernel<<<grid2, 128, TC_SMEM, s>>>(d, g->nv, g->views, g->du, ahi, alo, bhi, blo, filtered, flag);
-    return launched("tc_filter_kernel");
+    return dtype == MCT_F32 ? tc_run<3>(g, weighted, workspace, filtered, as_stream(stream))
+                            : tc_run<2>(g, weighted, workspace, filtered, as_stream(stream));
 }
 
 // 0 if no tensor-core filter launch on this workspace has timed out, else MCT_E_TIMEOUT
 // (synchronises the stream).
-int mct_filter_tc_status(const mct_geom* g, void* workspace, void* stream) {
+int mct_filter_tc_status(const mct_geom* g, int32_t dtype, void* workspace, void* stream) {
     MCT_REQUIRE(g && workspace, "mct_filter_tc_status: NULL argument");
-    uint4 *ahi, *alo, *bhi, *blo;
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_filter_tc_status: dtype must be MCT_F32 or MCT_BF16");
+    Parts a, b;
     int* flag;
-    tc_parts(g, workspace, &ahi, &alo, &bhi, &blo, &flag);
+    if (dtype == MCT_F32) tc_workspace<3>(g, &a, &b, &flag, workspace);
+    else tc_workspace<2>(g, &a, &b, &flag, workspace);
     int h = 0;
     cudaStream_t s = as_stream(stream);
     cudaError_t e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s);

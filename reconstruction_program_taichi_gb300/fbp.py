@@ -35,13 +35,14 @@ def _device(device=None):
 class FdkPipeline:
     """Weight -> filter -> pack -> backproject for one FBP geometry, with reusable
     device buffers.  `storage` selects the backprojection operand precision: 'f32'
-    (plain), 'bf16' or 'f16' (16-bit storage).  `filter_impl` selects the row filter:
-    'simt' (default: float32 FMA) or 'tc' (the Toeplitz product on the tensor cores
-    as split-bf16 hi+lo products with float32 accumulation: ~1e-5 relative to float32
-    at benchmark sizes, but up to ~1e-4 on small detectors where the ramp's
-    cancellation amplifies the dropped 2^-16 terms, so it belongs to the mixed path)."""
+    (plain), 'bf16' or 'f16' (16-bit storage).  `filter_impl` selects the row filter,
+    the Toeplitz product on the tensor cores with float32 accumulation:
+    'tc3' (default: bf16 hi + mid + lo parts, ~1e-6 relative) or 'tc' (hi + lo parts:
+    ~1e-5 relative at benchmark sizes, up to ~1e-4 on small detectors where the ramp's
+    cancellation amplifies the dropped 2^-16 terms; the mixed path) — or 'simt'
+    (float32 FMA on the SIMT cores)."""
 
-    def __init__(self, obj, device=None, storage="f32", filter_impl="simt"):
+    def __init__(self, obj, device=None, storage="f32", filter_impl="tc3"):
         dev = _device(device)
         self.obj = obj
         self.dg = fbp_geometry(obj, dev)
@@ -50,12 +51,13 @@ class FdkPipeline:
         self.kernel_none = obj.kernel_name == "None"
         f32 = dict(dtype=torch.float32, device=dev)
         self.taps = None if self.kernel_none else torch.tensor(recon_taps(obj), **f32)
-        if filter_impl not in ("simt", "tc"):
-            raise ValueError("filter_impl must be 'simt' (float32 FMA) or 'tc' (tensor-core split bf16)")
+        if filter_impl not in ("simt", "tc", "tc3"):
+            raise ValueError("filter_impl must be 'tc3', 'tc' (tensor-core split bf16) or 'simt' (float32 FMA)")
         self.filter_impl = filter_impl
         self.tc = None
-        if filter_impl == "tc" and not self.kernel_none:
-            self.tc = ops.TcFilter(self.dg, self.taps)
+        self._tc_dtype = MCT_F32 if filter_impl == "tc3" else MCT_BF16
+        if filter_impl in ("tc", "tc3") and not self.kernel_none:
+            self.tc = ops.TcFilter(self.dg, self.taps, self._tc_dtype)
         self.gauss_v = None
         if obj.apply_gauss_vertical:
             self.gauss_v = torch.tensor(gaussian_taps(obj.det_elem_count_vertical_actual, obj.det_elem_height,
@@ -87,7 +89,7 @@ class FdkPipeline:
         """Replace the filter taps (float64/float32 array of 2*nu-1 values)."""
         self.taps.copy_(torch.as_tensor(taps, dtype=torch.float32))
         if self.tc is not None:
-            self.tc = ops.TcFilter(self.dg, self.taps)
+            self.tc = ops.TcFilter(self.dg, self.taps, self._tc_dtype)
 
     def backproject(self, filtered, out=None):
         packed = ops.pack(self.dg, filtered, self.dtype, out=self.packed)

@@ -141,18 +141,20 @@ def filter_rows(dg, weighted, taps, out=None):
 
 
 class TcFilter:
-    """Tensor-core split-BF16 row filter for one geometry and one set of taps: owns
-    the tiled operand workspace (A and B^T hi/lo tiles, 1 KiB aligned)."""
+    """Tensor-core row filter for one geometry and one set of taps: owns the tiled
+    operand workspace (A and B^T part tiles, 1 KiB aligned).  dtype MCT_F32: three bf16
+    parts (~1e-6); MCT_BF16: two parts (~1e-5)."""
 
-    def __init__(self, dg, taps):
+    def __init__(self, dg, taps, dtype=MCT_BF16):
         g = dg.geom
         _check(taps, "taps", (2 * g.nu - 1,))
-        n = int(_lib.load().mct_filter_tc_workspace_size(dg.g()))
+        self.dtype = int(dtype)
+        n = int(_lib.load().mct_filter_tc_workspace_size(dg.g(), self.dtype))
         self.dg = dg
         self._buf = torch.empty(n + 1024, dtype=torch.uint8, device=dg.device)
         off = (-self._buf.data_ptr()) % 1024
         self.ws = ctypes.c_void_p(self._buf.data_ptr() + off)
-        _lib.call("mct_filter_tc_prepare", dg.g(), _ptr(taps), self.ws, _stream())
+        _lib.call("mct_filter_tc_prepare", dg.g(), _ptr(taps), self.dtype, self.ws, _stream())
 
     def __call__(self, weighted, out=None):
         g = self.dg.geom
@@ -160,12 +162,12 @@ class TcFilter:
         if out is None:
             out = torch.empty((g.views, g.nv, g.nu), dtype=torch.float32, device=weighted.device)
         _check(out, "out", (g.views, g.nv, g.nu))
-        _lib.call("mct_filter_tc", self.dg.g(), _ptr(weighted), self.ws, _ptr(out), _stream())
+        _lib.call("mct_filter_tc", self.dg.g(), _ptr(weighted), self.dtype, self.ws, _ptr(out), _stream())
         return out
 
     def status(self):
         """Raise if a bounded pipeline wait of an earlier launch timed out (syncs)."""
-        _lib.call("mct_filter_tc_status", self.dg.g(), self.ws, _stream())
+        _lib.call("mct_filter_tc_status", self.dg.g(), self.dtype, self.ws, _stream())
 
 
 def packed_bytes(dg, dtype=MCT_F32):

@@ -266,22 +266,28 @@ def test_run_mgfpj_v1_v2_match_reference(name, tmp_path, cuda):
     assert rel_l2(sgm, z["sgm"]) < TOL
 
 
-@pytest.mark.parametrize("nu,nv,views", [(96, 40, 90), (1024, 4, 40), (300, 7, 33), (64, 2, 129)])
-def test_tc_filter_matches_simt_filter(nu, nv, views, cuda):
-    """tcgen05 split-bf16 Toeplitz product vs the float32 SIMT filter."""
+@pytest.mark.parametrize("parts,tol", [(2, 2e-5), (3, 5e-6)])
+@pytest.mark.parametrize("nu,nv,views", [(96, 40, 90), (1024, 4, 40), (300, 7, 33), (64, 2, 129), (28, 14, 20)])
+def test_tc_filter_matches_simt_filter(nu, nv, views, parts, tol, cuda):
+    """tcgen05 split-bf16 Toeplitz product vs the float32 SIMT filter: two parts
+    (hi + lo) to ~1e-5; three parts (hi + mid + lo) to ~1e-6, the level of the tensor
+    pipe's float32 accumulation (measured 1.3e-6 to 3.6e-6 here)."""
     import torch
     from reconstruction_program_taichi_gb300 import geometry, ops
+    from reconstruction_program_taichi_gb300._lib import MCT_BF16, MCT_F32
+    if parts == 2 and nu == 28:
+        pytest.skip("two parts lose ~1e-4 on this small detector (the ramp's cancellation)")
     o = _cone_obj(nu=nu, nv=nv, views=views)
     dg = geometry.fbp_geometry(o)
     taps = torch.tensor(geometry.recon_taps(o), dtype=torch.float32, device="cuda")
     g = torch.Generator(device="cuda").manual_seed(nu)
     w = torch.rand(dg.sgm_shape, device="cuda", generator=g)
     ref = ops.filter_rows(dg, w, taps)
-    tc = ops.TcFilter(dg, taps)
+    tc = ops.TcFilter(dg, taps, MCT_F32 if parts == 3 else MCT_BF16)
     got = tc(w)
     tc.status()
     err = float(torch.linalg.vector_norm(got - ref) / torch.linalg.vector_norm(ref))
-    assert err < 2e-5, err
+    assert err < tol, err
     # a second call reuses the prepared B tiles
     got2 = tc(w * 2)
     assert float(torch.linalg.vector_norm(got2 - 2 * ref) / torch.linalg.vector_norm(2 * ref)) < 2e-5
