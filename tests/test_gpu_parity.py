@@ -245,15 +245,29 @@ def test_cgls_fused_update_matches_numpy(cuda):
     np.testing.assert_allclose(t[2].cpu().numpy(), d2, rtol=1e-5, atol=1e-5)
 
 
-def test_fp_transposed_copy_is_bit_identical(cuda):
+@pytest.mark.parametrize("kw", [
+    {"Views": 48},
+    {"Views": 8, "ImageRotation": 0},  # views at exact multiples of 45 degrees
+    {"DetectorElementHeight": 4.0, "VoxelHeight": 0.25},  # steep rays
+    {"ImageCenter": [6.0, -4.5], "ImageRotation": 0, "Views": 36},  # rays enter through every face
+    {"ImageDimension": 3, "ImageDimensionZ": 3, "PixelSize": 4.0, "VoxelHeight": 4.0, "Views": 36},  # smallest
+    {"CurvedDetector": True, "ForwardProjectionStepSize": 0.05, "Views": 30},
+    {"HelicalPitch": 0.7, "TotalScanAngle": 720, "Views": 60},
+])
+def test_fp_gather_copies_are_bit_identical(kw, cuda):
+    """The projector on the z-paired gather copies (workspace; the copy orientation
+    follows each view) against the same projector reading the volume directly: the
+    same samples and the same arithmetic, so bit-identical, with and without a mask."""
     import torch
     from reconstruction_program_taichi_gb300 import geometry, ops
-    o = _cone_obj(views=48)
+    o = _cone_obj(**kw)
     dg = geometry.fpj_geometry(o)
     vol = torch.from_numpy(_smooth(np.random.default_rng(8), o.img_dim_z, o.img_dim)).cuda()
-    a = ops.fp(dg, vol, workspace=None)
-    b = ops.fp(dg, vol, workspace=True)
-    assert torch.equal(a, b)
+    mask = (torch.rand(dg.sgm_shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(2)) > 0.1)
+    for m in (None, mask.float()):
+        a = ops.fp(dg, vol, mask=m, workspace=None)
+        b = ops.fp(dg, vol, mask=m, workspace=True)
+        assert torch.equal(a, b)
 
 
 @pytest.mark.parametrize("name", golden_names("fpjv"))
