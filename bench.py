@@ -29,7 +29,10 @@ WORKLOAD = dict(nu=1024, nv=256, views=1080, nx=512, nz=256, du=0.8, dv=0.8, px=
 SMALL = dict(WORKLOAD, nu=256, nv=64, views=270, nx=128, nz=64, du=3.2, dv=3.2, px=1.6, pz=1.6)
 # profiling case for ncu: the full detector and a volume larger than L2 (168 MB), 36 views
 PROF = dict(WORKLOAD, views=36, nz=160)
-WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF}
+# the same with 180 views: enough views per detector-row tile for the projector's L2
+# reuse to resemble the benchmark's (about 3.5 GB on the device)
+PROF180 = dict(PROF, views=180)
+WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF, "prof180": PROF180}
 
 
 def make_config(w):
@@ -746,7 +749,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
-                    help="c2: the benchmark; small: quick checks; prof: short launches for ncu captures")
+                    help="c2: the benchmark; small: quick checks; prof, prof180: short launches for ncu captures")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cgls", action="store_true")

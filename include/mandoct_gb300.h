@@ -193,16 +193,19 @@ int mct_helical_rebin(const mct_helical* h, const float* sgm, const float* z_pos
 /* ---------------------------------------------------------------- forward projection */
 
 /* Bytes of the optional forward-projection workspace (gather copies of the volume:
- * cone beam, two z-paired float32 copies; fan beam, one x/y-transposed copy). */
+ * cone beam, two float32 cell copies of 32 bytes per voxel; fan beam, one
+ * x/y-transposed copy). */
 size_t mct_fp_workspace_size(const mct_geom* g);
 
 /* Ray-driven trilinear forward projection of vol [nz][nx][nx] for all views into
  * sgm [nv][views][nu] (overwritten).  Rays with mask != 1 (mask [nv][views][nu], or
- * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes, 16-byte aligned, or
- * NULL) receives gather copies of vol: for cone beam {V[z], V[z+1]} pairs in [z][y][x]
- * and [z][x][y] order, for fan beam an x/y-transposed copy; views whose detector
- * columns run along y read the transposed order, so a warp's gathers are coalesced.
- * Results are identical with and without the workspace.  Replaces
+ * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes; 32-byte aligned for
+ * cone beam, 16-byte for fan beam; or NULL) receives gather copies of vol: for cone
+ * beam every voxel's 2x2x2 trilinear cell (its z-pairs and x-differences, 32 bytes,
+ * one 256-bit load) in [z][y][x] and [z][x][y] order, for fan beam an x/y-transposed
+ * copy; views whose detector columns run along y read the transposed order, so a
+ * warp's gathers are coalesced.  Results are identical with and without the
+ * workspace.  Replaces
  * Mgfpj_v3.ForwardProjectionBilinear run_mgfpj_v3.py:184-366 and
  * Mgfbp_ir.ForwardProjectionBilinear run_mgfbp_iterative_recon_IRN_CGLS.py:494-676. */
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,

@@ -166,18 +166,29 @@ __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const f
 // One thread per ray (u, v) of view j = blockIdx.y.  vol is [z][y][x]; vol_t, when
 // given, is the same volume as [z][x][y]: views whose detector columns spread along
 // y read vol_t so that the 32 rays of a warp touch consecutive addresses.  With ZP
-// (cone beam, workspace given) the volume is read from z-paired copies zp_x
-// ([z][y][x]) and zp_y ([z][x][y]) whose element (z, y, x) is the float2
-// {V[z][y][x], V[z+1][y][x]}: a cell reload is four 8-byte gathers instead of eight
-// 4-byte ones, and each gather already holds the lower/upper-plane pair that the
-// packed f32x2 interpolation consumes.
-template <typename ZT>
-struct ZPair;
-template <>
-struct ZPair<float2> {
-    static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
-    static __device__ __forceinline__ float2 make(float lo, float hi) { return make_float2(lo, hi); }
+// (cone beam, workspace given) the volume is read from cell copies zp_x ([z][y][x])
+// and zp_y ([z][x][y]) whose element (z, y, x) holds the whole 2x2x2 trilinear cell
+// at voxel (z, y, x) (float32 below, bf16 / float16 further down): a cell reload is
+// one gather.
+
+// float32 cell copy: element (z, y, x) of either orientation holds the 2x2x2 cell whose
+// lowest corner is voxel (z, y, x) as the four z-pairs the interpolation consumes,
+//   {e00, g00, e10, g10} = {V[z..z+1][y][x],  V[z..z+1][y][x+1] - V[z..z+1][y][x],
+//                           V[z..z+1][y+1][x], V[z..z+1][y+1][x+1] - V[z..z+1][y+1][x]},
+// 32 bytes, read with one 256-bit load.  Against four 8-byte z-pair gathers per reload
+// (neighbouring rays about a voxel apart, so each gather of a warp spans ~2.6 L1
+// lines) this touches each line once: L1 wavefronts fell from 86 to 48-64 % of peak,
+// at the price of L1 hits (10 % instead of 89 %: consecutive cells of a ray no longer
+// share lines), and the projector at 512x512x256 / 1080 views went 349 -> 298 ms.
+// The differences are the ones the kernel would compute from the volume.
+struct __align__(32) Cell32 {
+    float v[8];
 };
+__device__ __forceinline__ void ld_cell32(const Cell32* p, float2& e00, float2& g00, float2& e10, float2& g10) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(e00.x), "=f"(e00.y), "=f"(g00.x), "=f"(g00.y), "=f"(e10.x), "=f"(e10.y), "=f"(g10.x), "=f"(g10.y)
+        : "l"(p));
+}
 
 // bf16 cell copy: element (z, y, x) of either orientation holds the whole 2x2x2 cell
 // whose lowest corner is voxel (z, y, x), as four bf16 pairs {lower, upper z-plane}:
@@ -225,7 +236,9 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         auto load_cell = [&](int off) {
             if (off == cell) return;
             cell = off;
-            if constexpr (ZP && std::is_same<ZT, uint4>::value) {
+            if constexpr (ZP && std::is_same<ZT, Cell32>::value) {
+                ld_cell32(V2 + off, e00, g00, e10, g10);
+            } else if constexpr (ZP && std::is_same<ZT, uint4>::value) {
                 const uint4 q = __ldg(V2 + off);
                 e00 = bf16x2_to_float2(q.x);
                 g00 = bf16x2_to_float2(q.y);
@@ -237,14 +250,6 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
                 g00 = h16x2_to_float2(q.y);
                 e10 = h16x2_to_float2(q.z);
                 g10 = h16x2_to_float2(q.w);
-            } else if constexpr (ZP) {
-                const ZT* b2 = V2 + off;
-                e00 = ZPair<ZT>::load(b2);
-                const float2 e01 = ZPair<ZT>::load(b2 + sx);
-                e10 = ZPair<ZT>::load(b2 + sy);
-                const float2 e11 = ZPair<ZT>::load(b2 + sx + sy);
-                g00 = __fadd2_rn(e01, make_float2(-e00.x, -e00.y));
-                g10 = __fadd2_rn(e11, make_float2(-e10.x, -e10.y));
             } else {
                 const float* b = V + off;
                 const float a00 = __ldg(b), a01 = __ldg(b + sx), a10 = __ldg(b + sy), a11 = __ldg(b + sx + sy);
@@ -345,31 +350,6 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
     sgm[oidx] = acc * p.stepvd;
 }
 
-// Z-paired copies: zx[z][y][x] = zy[z][x][y] = {v[z][y][x], v[z+1][y][x]} (0 above
-// the top slice); 32x32 tiles, the transposed copy through shared memory.
-template <typename ZT>
-__global__ void zpair_kernel(int nx, int nz, const float* __restrict__ v, ZT* __restrict__ zx, ZT* __restrict__ zy) {
-    __shared__ ZT tile[32][33];
-    static_assert(std::is_same<ZT, float2>::value, "z-pairs are float32");
-    const int64_t plane = (int64_t)nx * nx;
-    const int z = blockIdx.z;
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-        const int y = y0 + i, x = x0 + threadIdx.x;
-        if (y < nx && x < nx) {
-            const int64_t o = z * plane + (int64_t)y * nx + x;
-            const ZT e = ZPair<ZT>::make(v[o], z + 1 < nz ? v[o + plane] : 0.0f);
-            zx[o] = e;
-            tile[i][threadIdx.x] = e;
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-        const int x = x0 + i, y = y0 + threadIdx.x;
-        if (y < nx && x < nx) zy[z * plane + (int64_t)x * nx + y] = tile[threadIdx.x][i];
-    }
-}
-
 // Largest |v| of the volume as float bits into *maxbits (zeroed by the caller).
 __global__ void vol_absmax_kernel(int64_t n, const float* __restrict__ v, uint32_t* __restrict__ maxbits) {
     uint32_t m = 0;
@@ -407,6 +387,43 @@ __global__ void cell16_kernel(int nx, int nz, const float* __restrict__ v, uint4
             q.y = pk(at(z, y, x + 1) - a0, at(z + 1, y, x + 1) - a1);
             q.z = pk(c0, c1);
             q.w = pk(at(z, y + 1, x + 1) - c0, at(z + 1, y + 1, x + 1) - c1);
+            cx[z * plane + (int64_t)y * nx + x] = q;
+            tile[i][threadIdx.x] = q;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int x = x0 + i, y = y0 + threadIdx.x;
+        if (y < nx && x < nx) cy[z * plane + (int64_t)x * nx + y] = tile[threadIdx.x][i];
+    }
+}
+
+// float32 cell copies (layout at Cell32): cx[z][y][x] and cy[z][x][y] both hold the
+// cell at voxel (z, y, x); corners outside the volume are 0 (no in-volume sample uses
+// them).  32x32 tiles, the transposed copy through shared memory.
+__global__ void cell32_kernel(int nx, int nz, const float* __restrict__ v, Cell32* __restrict__ cx,
+                              Cell32* __restrict__ cy) {
+    __shared__ Cell32 tile[32][33];
+    const int64_t plane = (int64_t)nx * nx;
+    const int z = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    auto at = [&](int zz, int yy, int xx) -> float {
+        return (zz < nz && yy < nx && xx < nx) ? v[zz * plane + (int64_t)yy * nx + xx] : 0.0f;
+    };
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int y = y0 + i, x = x0 + threadIdx.x;
+        if (y < nx && x < nx) {
+            const float a0 = at(z, y, x), a1 = at(z + 1, y, x);
+            const float c0 = at(z, y + 1, x), c1 = at(z + 1, y + 1, x);
+            Cell32 q;
+            q.v[0] = a0;
+            q.v[1] = a1;
+            q.v[2] = at(z, y, x + 1) - a0;
+            q.v[3] = at(z + 1, y, x + 1) - a1;
+            q.v[4] = c0;
+            q.v[5] = c1;
+            q.v[6] = at(z, y + 1, x + 1) - c0;
+            q.v[7] = at(z + 1, y + 1, x + 1) - c1;
             cx[z * plane + (int64_t)y * nx + x] = q;
             tile[i][threadIdx.x] = q;
         }
@@ -692,8 +709,9 @@ extern "C" {
 size_t mct_fp_workspace_size(const mct_geom* g) {
     if (!g || g->nx < 1 || g->nz < 1) return 0;
     const size_t n = (size_t)g->nz * g->nx * g->nx;
-    // cone beam: two z-paired copies (float2); fan beam: one transposed copy
-    return (g->flags & MCT_CONE) ? 2 * n * sizeof(float2) : n * sizeof(float);
+    // cone beam: two float32 cell copies (32 bytes per voxel each); fan beam: one
+    // transposed copy
+    return (g->flags & MCT_CONE) ? 2 * n * sizeof(Cell32) : n * sizeof(float);
 }
 
 size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype) {
@@ -744,12 +762,13 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
                                                             nullptr, reinterpret_cast<const h16x8*>(cx),
                                                             reinterpret_cast<const h16x8*>(cy), mask, sgm, vmax);
     } else if (p.cone && workspace) {
-        float2* zx = static_cast<float2*>(workspace);
-        float2* zy = zx + n;
-        zpair_kernel<float2><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, zx, zy);
-        MCT_TRY(launched("zpair_kernel"));
-        fp_kernel<true, true, float2><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
-                                                             vol, nullptr, zx, zy, mask, sgm, nullptr);
+        MCT_REQUIRE(((uintptr_t)workspace & 31) == 0, "mct_fp: workspace must be 32-byte aligned");
+        Cell32* cx = static_cast<Cell32*>(workspace);
+        Cell32* cy = cx + n;
+        cell32_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy);
+        MCT_TRY(launched("cell32_kernel"));
+        fp_kernel<true, true, Cell32><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
+                                                             vol, nullptr, cx, cy, mask, sgm, nullptr);
     } else {
         float* vt = static_cast<float*>(workspace);
         if (vt) {

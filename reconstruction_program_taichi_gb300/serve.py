@@ -131,6 +131,11 @@ class _FbpSlot:
         return [d if d is not None else self.host_out[i].numpy().copy() for i, d in enumerate(dev_out)]
 
 
+def _fp_workspace_bytes(dg):
+    from . import _lib
+    return int(_lib.load().mct_fp_storage_workspace_size(dg.g(), _lib.MCT_F32))
+
+
 class _CglsSlot:
     """CGLS (reference operator pair, lambda*D^T D with unit weights) for one request."""
 
@@ -144,7 +149,8 @@ class _CglsSlot:
         self.n_iter = n_iter
         self.last_used = time.perf_counter()
         nvol = obj.img_dim * obj.img_dim * obj.img_dim_z
-        self.nbytes = 8 * nvol * 4 + 3 * self.sys.fp_buf.numel() * 4
+        # iterates and operator buffers, the projector's gather copies, sinogram buffers
+        self.nbytes = 4 * nvol * 4 + _fp_workspace_bytes(self.sys.dg) + 3 * self.sys.fp_buf.numel() * 4
 
     def run(self, reqs):
         r = reqs[0]
@@ -250,7 +256,9 @@ class ReconServer:
         nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
         if req.kind == "fbp":  # input, weighted, filtered, packed (4x), tensor-core operand tiles
             return nsgm * 8 + 2 * nvol
-        return 8 * nvol + 3 * nsgm
+        # CGLS: four iterates, the projector's gather copies (cone beam: two 32-byte cells
+        # per voxel), three sinogram buffers
+        return 4 * nvol + (16 if o.cone_beam else 1) * nvol + 3 * nsgm
 
     def _batch_for(self, req):
         """Requests per FBP slot: `batch`, reduced so that one slot takes at most an

@@ -254,10 +254,12 @@ def test_cgls_fused_update_matches_numpy(cuda):
     {"CurvedDetector": True, "ForwardProjectionStepSize": 0.05, "Views": 30},
     {"HelicalPitch": 0.7, "TotalScanAngle": 720, "Views": 60},
 ])
-def test_fp_gather_copies_are_bit_identical(kw, cuda):
-    """The projector on the z-paired gather copies (workspace; the copy orientation
-    follows each view) against the same projector reading the volume directly: the
-    same samples and the same arithmetic, so bit-identical, with and without a mask."""
+def test_fp_gather_copies_match_direct_reads(kw, cuda):
+    """The projector on the float32 cell copies (workspace; the copy orientation
+    follows each view) against the same projector reading the volume directly, with
+    and without a mask: the same samples, so the same zero pattern; the copy path
+    takes interior floors from a rounding constant (positions rounded once around
+    f - 0.5), so sums agree to float rounding."""
     import torch
     from reconstruction_program_taichi_gb300 import geometry, ops
     o = _cone_obj(**kw)
@@ -265,9 +267,10 @@ def test_fp_gather_copies_are_bit_identical(kw, cuda):
     vol = torch.from_numpy(_smooth(np.random.default_rng(8), o.img_dim_z, o.img_dim)).cuda()
     mask = (torch.rand(dg.sgm_shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(2)) > 0.1)
     for m in (None, mask.float()):
-        a = ops.fp(dg, vol, mask=m, workspace=None)
-        b = ops.fp(dg, vol, mask=m, workspace=True)
-        assert torch.equal(a, b)
+        a = ops.fp(dg, vol, mask=m, workspace=None).cpu().numpy()
+        b = ops.fp(dg, vol, mask=m, workspace=True).cpu().numpy()
+        assert np.array_equal(a == 0, b == 0)
+        assert rel_l2(b, a) < 1e-6
 
 
 @pytest.mark.parametrize("name", golden_names("fpjv"))
