@@ -135,10 +135,17 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
 //     sqrt(qx^2 + qy^2 + z^2) / max(|qx|, |qy|) * px
 // (run_mgfbp_iterative_recon_IRN_CGLS.py:417-421) with the square root as d2 * rsqrt(d2).
 // A column that leaves the detector in u in some view is all zero in the reference
-// (SetTruncatedRegionToZero), so its thread stops there.
+// (SetTruncatedRegionToZero), so its thread stops there.  As in the FDK kernel, v and
+// z are affine in the slice index, and the register budget (128 for 16-byte
+// operands, 80 for 8-byte ones) lets all UA_ZC gathers of a view issue before their
+// arithmetic, which hides the gather latency.
 constexpr int UA_ZC = 16;
+template <typename QT>
+constexpr int ua_min_blocks() {
+    return sizeof(QT) == 8 ? 3 : 2;
+}
 template <bool CONE, typename QT, typename PT>
-__global__ void __launch_bounds__(UB_TX* UB_TY)
+__global__ void __launch_bounds__(UB_TX* UB_TY, ua_min_blocks<QT>())
 bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
                           const void* __restrict__ packed, float* __restrict__ vol,
                           const uint32_t* __restrict__ f16_max) {
@@ -193,20 +200,24 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
             if (CONE) {
                 const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq + uc;
                 const float2 ru2 = make_float2(ru, ru);
+                // slice k: z = zA + k zz, v index = vA + k vB
+                const float zA = bz + tb.z;
+                const float vA = (mag * zA - p.v0) * p.kv, vB = (mag * p.zz) * p.kv;
+                const unsigned top = (unsigned)(p.nv - 2);  // rows [0, nv-2] hold a bilinear cell (nv >= 2)
 #pragma unroll
                 for (int k = 0; k < UA_ZC; ++k) {
-                    const float z = fmaf((float)k, p.zz, bz) + tb.z;
-                    const float vi = (mag * z - p.v0) * p.kv;
+                    const float vi = fmaf((float)k, vB, vA);
                     const float vf = floorf(vi);
-                    const bool in = vf >= 0.0f && vf + 1.0f <= (float)(p.nv - 1);  // else: no contribution
-                    const int vr = in ? (int)vf : 0;
+                    const unsigned vu = (unsigned)(int)vf;  // negative rows wrap around
+                    const bool in = vu <= top;              // else: no contribution
                     const float rv = vi - vf;
                     float2 lo, hi;
-                    Quad<QT>::load(base + vr * nq, lo, hi);
+                    Quad<QT>::load(base + min(vu, top) * (unsigned)nq, lo, hi);
                     const float2 s2 = __ffma2_rn(ru2, hi, lo);
+                    const float z = fmaf((float)k, p.zz, zA);
                     const float d2 = fmaf(z, z, r2);
-                    const float w = d2 * rsqrtf(d2) * wpx;
-                    acc[k] += in ? fmaf(rv, s2.y, s2.x) * w : 0.0f;
+                    const float w = in ? d2 * rsqrtf(d2) * wpx : 0.0f;
+                    acc[k] = fmaf(fmaf(rv, s2.y, s2.x), w, acc[k]);
                 }
             } else {
                 const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
