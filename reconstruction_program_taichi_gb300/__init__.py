@@ -13,10 +13,11 @@ from .helical import Mgfbp_helical, run_mgfbp_helical
 from .fpj import FpPipeline, Mgfpj_v3, run_mgfpj_v3
 from .ir import IrSystem, Mgfbp_ir, Mgfbp_ir_piccs, run_mgfbp_ir, run_mgfbp_ir_piccs
 from .admm import Mgfbp_ir_admm, run_mgfbp_ir_admm
+from .stream import ScanStream
 
 __all__ = [
     "ConfigError", "NativeLibraryError", "ReadConfigFile", "load_jsonc", "remove_comments", "save_jsonc",
     "FdkPipeline", "Mgfbp", "run_mgfbp", "Mgfbp_v2", "run_mgfbp_v2", "Mgfbp_helical", "run_mgfbp_helical", "FpPipeline", "Mgfpj_v3", "run_mgfpj_v3",
     "IrSystem", "Mgfbp_ir", "Mgfbp_ir_piccs", "run_mgfbp_ir", "run_mgfbp_ir_piccs", "Mgfbp_ir_admm",
-    "run_mgfbp_ir_admm", "launch_count",
+    "run_mgfbp_ir_admm", "ScanStream", "launch_count",
 ]
