@@ -448,7 +448,7 @@ def c1_bench(dev, stream, barrier, reps=50):
                      "10 ellipses, Poisson 1e5"}
     ph = phantom(C1, dev)
     ref = None
-    for name, storage, impl in (("plain", "f32", "simt"), ("mixed", "bf16", "tc")):
+    for name, storage, impl in (("plain", "f32", "tc3"), ("mixed", "bf16", "tc")):
         pipe = fbp.FdkPipeline(o, device=dev, storage=storage, filter_impl=impl)
         pipe.set_taps(hann_from_ramp(geometry.recon_taps(o)))
         sgm = noisy(ops.project_ellipsoids(pipe.dg, ellipsoids(C1)), C1["photons"], C1["seed"])

@@ -47,6 +47,21 @@ struct BpParams {
     float o_x, o_y, o_z;     // P
 };
 
+// Per-view table of a chunk of nvc views starting at jc: {cos b', sin b', weight, 0}
+// with b' = b - img_rot and weight = delta-beta (run_mgfbp.py:1107-1111) x the
+// redundancy factor x the float16 unscale.
+__device__ __forceinline__ void fill_view_table(const BpParams& p, const float* __restrict__ angles, float4* tab,
+                                                int jc, int nvc, int tid, int nthreads, float unscale) {
+    for (int q = tid; q < nvc; q += nthreads) {
+        const int jg = p.view_begin + jc + q;  // scan index (angles is the whole scan's table)
+        const int vt = p.views_total;
+        float s, c;
+        sincosf(angles[jg] - p.img_rot, &s, &c);
+        float db = (jg == vt - 1) ? fabsf(angles[vt - 1] - angles[0]) / (vt - 1) : fabsf(angles[jg + 1] - angles[jg]);
+        tab[q] = make_float4(c, s, db * p.div * unscale, 0.0f);
+    }
+}
+
 // MODE 0: axial, flat or curved detector, no projection matrix (u hoisted per column)
 // MODE 1: any view mode, no projection matrix (per-voxel u)
 // MODE 2: projection matrix geometry
@@ -77,14 +92,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     for (int jc = 0; jc < p.views; jc += BP_VCHUNK) {
         const int nvc = min(BP_VCHUNK, p.views - jc);
         __syncthreads();
-        for (int q = tid; q < nvc; q += BP_TX * BP_TY) {
-            const int jg = p.view_begin + jc + q;  // scan index (angles is the whole scan's table)
-            const int vt = p.views_total;
-            float s, c;
-            sincosf(angles[jg] - p.img_rot, &s, &c);
-            float db = (jg == vt - 1) ? fabsf(angles[vt - 1] - angles[0]) / (vt - 1) : fabsf(angles[jg + 1] - angles[jg]);
-            tab[q] = make_float4(c, s, db * p.div * unscale, 0.0f);
-        }
+        fill_view_table(p, angles, tab, jc, nvc, tid, BP_TX * BP_TY, unscale);
         __syncthreads();
         if (!active || dead == 0xffffffffu) continue;
 
@@ -211,6 +219,91 @@ __global__ void nan_to_zero_kernel(int64_t n, float* __restrict__ v) {
         if (v[i] != v[i]) v[i] = 0.0f;
 }
 
+// Axial fan beam (one detector row per slice, run_mgfbp.py:1183-1187).  A 2D image
+// has few voxels (256^2 at 720 views: 256 blocks of the kernel above, under two per
+// SM, each thread walking every view), so here the views of a column are split over
+// FB_G threads: block (32 x-voxels, FB_G view groups) for one image row and FB_ZC
+// slices, thread g taking views g, g + FB_G, ...  The group sums are added in a fixed
+// order through shared memory (deterministic), and a column is off the detector if
+// any group saw it off.  Per view the arithmetic is that of the kernel above.
+constexpr int FB_G = 8, FB_ZC = 8;
+static_assert(FB_G == FB_ZC, "each thread finishes one slice");
+template <typename PT>
+__global__ void __launch_bounds__(32 * FB_G)
+fdk_bp_fan_kernel(BpParams p, const float* __restrict__ angles, const void* __restrict__ packed,
+                  float* __restrict__ vol, const uint32_t* __restrict__ f16_max) {
+    __shared__ float4 tab[BP_VCHUNK];
+    __shared__ float part[FB_G][FB_ZC][32];
+    __shared__ int dead_g[FB_G][32];
+    const int tx = threadIdx.x, g = threadIdx.y;
+    const int ix = blockIdx.x * 32 + tx;
+    const int iy = blockIdx.y;
+    const int zb = blockIdx.z * FB_ZC;
+    const int tid = g * 32 + tx;
+    const bool active = ix < p.nx;
+    const int nq = p.nu - 1;
+    const float c0x = p.o_x + ix * p.px_x + iy * p.py_x;
+    const float c0y = p.o_y + ix * p.px_y + iy * p.py_y;
+    float acc[FB_ZC];
+#pragma unroll
+    for (int k = 0; k < FB_ZC; ++k) acc[k] = 0.0f;
+    int dead = 0;
+    const float unscale = IsF16<PT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
+    for (int jc = 0; jc < p.views; jc += BP_VCHUNK) {
+        const int nvc = min(BP_VCHUNK, p.views - jc);
+        __syncthreads();
+        fill_view_table(p, angles, tab, jc, nvc, tid, 32 * FB_G, unscale);
+        __syncthreads();
+        if (!active || dead) continue;
+        for (int q = g; q < nvc; q += FB_G) {
+            const int j = jc + q;
+            const float4 tb = tab[q];
+            const float cb = tb.x, sb = tb.y;
+            const float L = p.sid - c0x * cb - c0y * sb;
+            const float t = -c0x * sb + c0y * cb;
+            const float mag = p.sdd / L;
+            const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
+            const float ui = (u - p.u0) * p.inv_ustep;
+            if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {  // NaN counts as off-detector
+                dead = 1;
+                break;
+            }
+            const float uf = floorf(ui);
+            const float ru = ui - uf;
+            const int uc = (int)uf;
+            const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+            const float w = (p.sid * dw) * tb.z;
+            const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
+#pragma unroll
+            for (int k = 0; k < FB_ZC; ++k) {
+                if (zb + k < p.nz) {
+                    const float2 pr = Pair<PT>::load(base + (int64_t)k * nq);
+                    acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < FB_ZC; ++k) part[g][k][tx] = acc[k];
+    dead_g[g][tx] = dead;
+    __syncthreads();
+    const int k = g;  // this thread finishes slice zb + g of its column
+    if (!active || zb + k >= p.nz) return;
+    float sum = 0.0f;
+    int any_dead = 0;
+#pragma unroll
+    for (int h = 0; h < FB_G; ++h) {
+        sum += part[h][k][tx];
+        any_dead |= dead_g[h][tx];
+    }
+    const bool off_detector = any_dead || sum != sum;
+    float* out = vol + (int64_t)(zb + k) * p.nx * p.nx + (int64_t)iy * p.nx + ix;
+    if (p.accumulate)  // a voxel off the detector in any chunk stays NaN until mct_fdk_bp_finish
+        *out = off_detector ? __int_as_float(0x7fffffff) : *out + sum;
+    else
+        *out = off_detector ? 0.0f : sum;
+}
+
 template <int MODE, bool CONE>
 void launch_bp(const BpParams& p, dim3 grid, dim3 block, cudaStream_t s, const float* angles, const float* pmat,
                const void* packed, int dtype, float* vol, const uint32_t* f16_max) {
@@ -287,7 +380,16 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
     if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
     else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
-    else if (axial_fast) launch_bp<0, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
+    else if (axial_fast) {
+        MCT_REQUIRE(g->nx <= 65535, "mct_fdk_bp: fan beam images are at most 65535 pixels wide");
+        dim3 fgrid((g->nx + 31) / 32, g->nx, (g->nz + FB_ZC - 1) / FB_ZC), fblock(32, FB_G);
+        if (dtype == MCT_BF16)
+            fdk_bp_fan_kernel<uint32_t><<<fgrid, fblock, 0, s>>>(p, t->angles, packed, vol, nullptr);
+        else if (dtype == MCT_F16)
+            fdk_bp_fan_kernel<h16x2><<<fgrid, fblock, 0, s>>>(p, t->angles, packed, vol, fm);
+        else
+            fdk_bp_fan_kernel<float2><<<fgrid, fblock, 0, s>>>(p, t->angles, packed, vol, nullptr);
+    }
     else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     return launched("fdk_bp_kernel");
