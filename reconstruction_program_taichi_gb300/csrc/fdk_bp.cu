@@ -222,61 +222,63 @@ __global__ void nan_to_zero_kernel(int64_t n, float* __restrict__ v) {
 // Axial fan beam (one detector row per slice, run_mgfbp.py:1183-1187).  A 2D image
 // has few voxels (256^2 at 720 views: 256 blocks of the kernel above, under two per
 // SM, each thread walking every view), so here the views of a column are split over
-// FB_G threads: block (32 x-voxels, FB_G view groups) for one image row and FB_ZC
-// slices, thread g taking views g, g + FB_G, ...  The group sums are added in a fixed
-// order through shared memory (deterministic), and a column is off the detector if
-// any group saw it off.  Per view the arithmetic is that of the kernel above.
-constexpr int FB_G = 8, FB_ZC = 8;
-static_assert(FB_G == FB_ZC, "each thread finishes one slice");
-template <typename PT>
+// FB_G threads: block (32 x-voxels, FB_G view groups) for one image row and ZC slices
+// (1 for a single slice, else 8), thread g taking views g, g + FB_G, ...  The group
+// sums are added in a fixed order through shared memory (deterministic), and a column
+// is off the detector if any group saw it off.  A view that sees the column off the
+// detector does not stop the loop (its index is clamped and the column's result is
+// discarded), so independent views can overlap; 1/L is taken once per view.
+constexpr int FB_G = 8;
+template <int ZC, typename PT>
 __global__ void __launch_bounds__(32 * FB_G)
 fdk_bp_fan_kernel(BpParams p, const float* __restrict__ angles, const void* __restrict__ packed,
                   float* __restrict__ vol, const uint32_t* __restrict__ f16_max) {
+    static_assert(ZC <= FB_G, "each of the first ZC view groups finishes one slice");
     __shared__ float4 tab[BP_VCHUNK];
-    __shared__ float part[FB_G][FB_ZC][32];
+    __shared__ float part[FB_G][ZC][32];
     __shared__ int dead_g[FB_G][32];
     const int tx = threadIdx.x, g = threadIdx.y;
     const int ix = blockIdx.x * 32 + tx;
     const int iy = blockIdx.y;
-    const int zb = blockIdx.z * FB_ZC;
+    const int zb = blockIdx.z * ZC;
     const int tid = g * 32 + tx;
     const bool active = ix < p.nx;
     const int nq = p.nu - 1;
     const float c0x = p.o_x + ix * p.px_x + iy * p.py_x;
     const float c0y = p.o_y + ix * p.px_y + iy * p.py_y;
-    float acc[FB_ZC];
+    float acc[ZC];
 #pragma unroll
-    for (int k = 0; k < FB_ZC; ++k) acc[k] = 0.0f;
-    int dead = 0;
+    for (int k = 0; k < ZC; ++k) acc[k] = 0.0f;
+    bool dead = false;
     const float unscale = IsF16<PT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
+    const float umax = (float)(p.nu - 1);
     for (int jc = 0; jc < p.views; jc += BP_VCHUNK) {
         const int nvc = min(BP_VCHUNK, p.views - jc);
         __syncthreads();
         fill_view_table(p, angles, tab, jc, nvc, tid, 32 * FB_G, unscale);
         __syncthreads();
         if (!active || dead) continue;
+#pragma unroll 2
         for (int q = g; q < nvc; q += FB_G) {
             const int j = jc + q;
             const float4 tb = tab[q];
             const float cb = tb.x, sb = tb.y;
             const float L = p.sid - c0x * cb - c0y * sb;
             const float t = -c0x * sb + c0y * cb;
-            const float mag = p.sdd / L;
+            const float r = 1.0f / L;
+            const float mag = p.sdd * r;
             const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
             const float ui = (u - p.u0) * p.inv_ustep;
-            if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {  // NaN counts as off-detector
-                dead = 1;
-                break;
-            }
+            dead |= !(ui >= 0.0f && ui + 1.0f <= umax);  // NaN counts as off-detector
             const float uf = floorf(ui);
             const float ru = ui - uf;
-            const int uc = (int)uf;
-            const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+            const int uc = min(max((int)uf, 0), p.nu - 2);
+            const float dw = p.curved ? 1.0f / (L * L + t * t) : r * r;
             const float w = (p.sid * dw) * tb.z;
             const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
 #pragma unroll
-            for (int k = 0; k < FB_ZC; ++k) {
-                if (zb + k < p.nz) {
+            for (int k = 0; k < ZC; ++k) {
+                if (ZC == 1 || zb + k < p.nz) {
                     const float2 pr = Pair<PT>::load(base + (int64_t)k * nq);
                     acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
                 }
@@ -284,11 +286,11 @@ fdk_bp_fan_kernel(BpParams p, const float* __restrict__ angles, const void* __re
         }
     }
 #pragma unroll
-    for (int k = 0; k < FB_ZC; ++k) part[g][k][tx] = acc[k];
+    for (int k = 0; k < ZC; ++k) part[g][k][tx] = acc[k];
     dead_g[g][tx] = dead;
     __syncthreads();
-    const int k = g;  // this thread finishes slice zb + g of its column
-    if (!active || zb + k >= p.nz) return;
+    const int k = g;  // the first ZC groups finish slice zb + g of their column
+    if (!active || k >= ZC || zb + k >= p.nz) return;
     float sum = 0.0f;
     int any_dead = 0;
 #pragma unroll
@@ -302,6 +304,18 @@ fdk_bp_fan_kernel(BpParams p, const float* __restrict__ angles, const void* __re
         *out = off_detector ? __int_as_float(0x7fffffff) : *out + sum;
     else
         *out = off_detector ? 0.0f : sum;
+}
+
+template <int ZC>
+void launch_bp_fan(const BpParams& p, const mct_geom* g, cudaStream_t s, const float* angles, const void* packed,
+                   int dtype, float* vol, const uint32_t* f16_max) {
+    dim3 grid((g->nx + 31) / 32, g->nx, (g->nz + ZC - 1) / ZC), block(32, FB_G);
+    if (dtype == MCT_BF16)
+        fdk_bp_fan_kernel<ZC, uint32_t><<<grid, block, 0, s>>>(p, angles, packed, vol, nullptr);
+    else if (dtype == MCT_F16)
+        fdk_bp_fan_kernel<ZC, h16x2><<<grid, block, 0, s>>>(p, angles, packed, vol, f16_max);
+    else
+        fdk_bp_fan_kernel<ZC, float2><<<grid, block, 0, s>>>(p, angles, packed, vol, nullptr);
 }
 
 template <int MODE, bool CONE>
@@ -382,13 +396,8 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else if (axial_fast) {
         MCT_REQUIRE(g->nx <= 65535, "mct_fdk_bp: fan beam images are at most 65535 pixels wide");
-        dim3 fgrid((g->nx + 31) / 32, g->nx, (g->nz + FB_ZC - 1) / FB_ZC), fblock(32, FB_G);
-        if (dtype == MCT_BF16)
-            fdk_bp_fan_kernel<uint32_t><<<fgrid, fblock, 0, s>>>(p, t->angles, packed, vol, nullptr);
-        else if (dtype == MCT_F16)
-            fdk_bp_fan_kernel<h16x2><<<fgrid, fblock, 0, s>>>(p, t->angles, packed, vol, fm);
-        else
-            fdk_bp_fan_kernel<float2><<<fgrid, fblock, 0, s>>>(p, t->angles, packed, vol, nullptr);
+        if (g->nz == 1) launch_bp_fan<1>(p, g, s, t->angles, packed, dtype, vol, fm);
+        else launch_bp_fan<8>(p, g, s, t->angles, packed, dtype, vol, fm);
     }
     else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
