@@ -133,6 +133,33 @@ def test_fdk_ops_vs_oracle(kw, cuda):
     assert rel_l2(vol[keep], ref[keep]) < TOL
 
 
+@pytest.mark.parametrize("nv,kw", [(1, {}), (13, {"ImageDimension": 37}), (2, {"CurvedDetector": True,
+                                                                            "TotalScanAngle": 220})])
+def test_fan_beam_fbp_vs_oracle(nv, kw, cuda):
+    """Fan-beam FBP (the view-split backprojector: one slice per thread for a single
+    row, 8-slice chunks otherwise, here a partial one) against the float64 oracle."""
+    import torch
+    from reconstruction_program_taichi_gb300 import fbp, geometry
+    o = _cone_obj(nv=nv, ConeBeam=False, **kw)
+    pipe = fbp.FdkPipeline(o, storage="f32")
+    rng = np.random.default_rng(12)
+    sgm = rng.uniform(0, 1, (o.det_elem_count_vertical_actual, o.view_num, o.det_elem_count_horizontal)).astype(np.float32)
+    vol = pipe.run(torch.from_numpy(sgm).cuda()).cpu().numpy()
+    assert vol.shape[0] == nv
+    u, v, ang = geometry.fbp_arrays(o)
+    w = F.weight_sgm(sgm, u, v, ang, o.source_det_dis, o.curved_dect, o.short_scan, o.total_scan_angle)
+    filt = F.filter_rows(w, geometry.recon_taps(o), o.det_elem_width)
+    ref = F.fdk_bp(filt, ang, u, v, nx=o.img_dim, nz=o.img_dim_z, px=o.img_pix_size, pz=o.img_voxel_height,
+                   cx=o.img_center_x, cy=o.img_center_y, cz=o.img_center_z, sid=o.source_isocenter_dis,
+                   sdd=o.source_det_dis, dv=o.det_elem_height, img_rot=o.img_rot,
+                   total_scan_angle=o.total_scan_angle, short_scan=o.short_scan, cone_beam=False,
+                   curved=o.curved_dect, view_mode=o.recon_view_mode)
+    assert np.array_equal(vol == 0, ref == 0)
+    keep = vol != 0
+    assert keep.mean() > 0.5
+    assert rel_l2(vol[keep], ref[keep]) < TOL
+
+
 @pytest.mark.parametrize("storage,tol", [("bf16", 5e-3), ("f16", 8e-4)])
 @pytest.mark.parametrize("scale", [1.0, 1e6, 1e-6])
 def test_fdk_16bit_storage_error_is_small(storage, tol, scale, cuda):
