@@ -133,6 +133,30 @@ def test_fdk_ops_vs_oracle(kw, cuda):
     assert rel_l2(vol[keep], ref[keep]) < TOL
 
 
+@pytest.mark.parametrize("kw", [{}, {"CurvedDetector": True, "TotalScanAngle": 220},
+                                {"TotalScanAngle": 200, "BeamHardeningCorrectionCoefficients": [0.0, 1.0, 0.05]}])
+def test_weighting_vector_and_scalar_paths_agree(kw, cuda):
+    """The 16-byte weighting kernel (aligned input) and the per-element one (input one
+    float off 16-byte alignment) agree to float rounding (the compiler contracts the
+    distance term into FMAs differently in the two), for both input layouts."""
+    import torch
+    from reconstruction_program_taichi_gb300 import fbp, ops
+    o = _cone_obj(nu=96, nv=20, views=45, **kw)
+    pipe = fbp.FdkPipeline(o)
+    dg = pipe.dg
+    nv, nb, nu = dg.sgm_shape
+    rng = np.random.default_rng(14)
+    data = torch.from_numpy(rng.uniform(0, 2, nv * nb * nu).astype(np.float32)).cuda()
+    aligned = data.clone()
+    shifted = torch.empty(data.numel() + 1, device="cuda")[1:]  # 4 bytes past a 16-byte boundary
+    shifted.copy_(data)
+    assert aligned.data_ptr() % 16 == 0 and shifted.data_ptr() % 16 == 4
+    for row_stride, view_stride in ((nb * nu, nu), (nu, nv * nu)):  # [rows][views][cols], post-log [views][rows][cols]
+        a = ops.weight(dg, aligned, row_stride, view_stride, pipe.bh)
+        b = ops.weight(dg, shifted, row_stride, view_stride, pipe.bh)
+        assert float(((a - b).abs() / b.abs().clamp_min(1e-30)).max()) < 1e-6
+
+
 @pytest.mark.parametrize("nv,kw", [(1, {}), (13, {"ImageDimension": 37}), (2, {"CurvedDetector": True,
                                                                             "TotalScanAngle": 220})])
 def test_fan_beam_fbp_vs_oracle(nv, kw, cuda):
