@@ -391,7 +391,7 @@ def run_gpu(args, w):
         cgls = irn_bench(dev, stream, barrier)
         piccs = piccs_bench(dev, stream, barrier)
     if not args.no_serve and w is WORKLOAD and world == 1:
-        del pipe, fpg, sgm, fp_out, dev_sgm, host_sgm, host_vol, host_fp
+        del pipe, fpg, sgm, fp_out, scans, host_sgm, host_vol, host_fp
         torch.cuda.empty_cache()
         served = serve_bench(dev)
 
