@@ -753,10 +753,18 @@ def main():
     ap.add_argument("--no-cgls", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--only", default=None, choices=["cgls"],
+                    help="cgls: only the IRN-CGLS-TV section (a short run for ncu captures of its kernels)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w)
+    elif args.only == "cgls":
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        out = irn_bench(dev, torch.cuda.current_stream(dev), torch.cuda.synchronize)
+        print(json.dumps({"irn_cgls_tv": out}))
     else:
         run_gpu(args, w)
 
