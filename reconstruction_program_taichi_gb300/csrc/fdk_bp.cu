@@ -104,7 +104,8 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                 // u is shared by the whole column
                 const float L = p.sid - c0x * cb - c0y * sb;
                 const float t = -c0x * sb + c0y * cb;
-                const float mag = p.sdd / L;
+                const float rL = 1.0f / L;  // one reciprocal for the magnification and the flat distance weight
+                const float mag = p.sdd * rL;
                 const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
                 const float ui = (u - p.u0) * p.inv_ustep;
                 if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {  // NaN counts as off-detector
@@ -114,7 +115,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                 const float uf = floorf(ui);
                 const float ru = ui - uf;
                 const int uc = (int)uf;
-                const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+                const float dw = p.curved ? 1.0f / (L * L + t * t) : rL * rL;
                 const float w = (p.sid * dw) * tb.z;
                 if (CONE) {
                     const float vA = (mag * c0z - p.v0) * p.kv;
@@ -160,12 +161,13 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     const float z = fmaf((float)k, p.pz_z, c0z);
                     const float L = p.sid - x * cb - y * sb;
                     const float t = -x * sb + y * cb;
-                    float mag, ui;
+                    float mag, ui, rL = 0.0f;
                     if (MODE == 2) {
                         mag = 1.0f / (P8 * x + P9 * y + P10 * z + P11);
                         ui = (P0 * x + P1 * y + P2 * z + P3) * mag;
                     } else {
-                        mag = p.sdd / L;
+                        rL = 1.0f / L;  // one reciprocal for the magnification and the flat distance weight
+                        mag = p.sdd * rL;
                         const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
                         ui = (u - p.u0) * p.inv_ustep;
                     }
@@ -176,7 +178,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     const float uf = floorf(ui);
                     const float ru = ui - uf;
                     const int uc = (int)uf;
-                    const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+                    const float dw = p.curved ? 1.0f / (L * L + t * t) : (MODE == 2 ? 1.0f / (L * L) : rL * rL);
                     const float w = (p.sid * dw) * tb.z;
                     if (CONE) {
                         const float vi = (MODE == 2) ? (P4 * x + P5 * y + P6 * z + P7) * mag : (mag * z - p.v0) * p.kv;
