@@ -184,7 +184,9 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
             const float L = p.sid - x * cb - y * sb;
             const float qx = x - tb.w, qy = y - tab_s[q];
             const float aqx = fabsf(qx), aqy = fabsf(qy);
-            const float mag = p.sdd / L;
+            const float mq = aqx > aqy ? aqx : aqy;
+            const float rr = 1.0f / (L * mq);  // one reciprocal for sdd / L and px / max(|qx|, |qy|)
+            const float mag = p.sdd * mq * rr;
             const float t = -x * sb + y * cb;
             const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
             const float ui = (u - p.u0) * p.inv_ustep;
@@ -196,7 +198,7 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
             const float ru = ui - uf;
             const int uc = (int)uf;
             const float r2 = qx * qx + qy * qy;
-            const float wpx = p.px / (aqx > aqy ? aqx : aqy);
+            const float wpx = p.px * L * rr;
             if (CONE) {
                 const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq + uc;
                 const float2 ru2 = make_float2(ru, ru);
