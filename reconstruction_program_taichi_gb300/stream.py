@@ -50,9 +50,16 @@ class ScanStream:
         until the returned event has completed."""
         if (host_proj is None) != (self.proj is None):
             raise ValueError("host_proj is required exactly when the stream has a forward-projection geometry")
+        shapes = {"host_sgm": self.sgm[0].shape, "host_vol": self.vol[0].shape,
+                  "host_proj": self.proj[0].shape if self.proj is not None else None}
         for t, name in ((host_sgm, "host_sgm"), (host_vol, "host_vol"), (host_proj, "host_proj")):
-            if t is not None and (t.is_cuda or not t.is_pinned()):
+            if t is None:
+                continue
+            if t.is_cuda or not t.is_pinned():
                 raise ValueError(f"{name} must be a pinned host tensor")
+            if t.dtype != torch.float32 or tuple(t.shape) != tuple(shapes[name]):
+                raise ValueError(f"{name} must be float32 of shape {tuple(shapes[name])}, got {t.dtype} "
+                                 f"{tuple(t.shape)}")
         s = self.submitted % 2
         reuse = self.submitted >= 2
         self.submitted += 1

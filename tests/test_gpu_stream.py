@@ -49,3 +49,5 @@ def test_scan_stream_rejects_pageable_buffers(cuda):
     with pytest.raises(ValueError, match="host_proj"):
         st.submit(sgm.pin_memory(), torch.empty(pipe.dg.vol_shape, pin_memory=True),
                   torch.empty((1,), pin_memory=True))
+    with pytest.raises(ValueError, match="shape"):
+        st.submit(sgm.pin_memory(), torch.empty((1, 2, 3), pin_memory=True))
