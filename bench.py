@@ -387,9 +387,11 @@ def run_gpu(args, w):
     cgls = piccs = c1 = served = None
     if w is WORKLOAD and not args.no_mixed:
         c1 = c1_bench(dev, stream, barrier)
+    widened = None
     if not args.no_cgls and w is WORKLOAD:
         cgls = irn_bench(dev, stream, barrier)
         piccs = piccs_bench(dev, stream, barrier)
+        widened = widen_bench(dev, stream, barrier)
     if not args.no_serve and w is WORKLOAD and world == 1:
         del pipe, fpg, sgm, fp_out, scans, host_sgm, host_vol, host_fp
         torch.cuda.empty_cache()
@@ -421,7 +423,7 @@ def run_gpu(args, w):
             "fp_samples_per_s": round(n_samples / (st[3] / 1e3), 1), "fp_in_volume_samples": n_samples,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clk.summary(), "mixed": mixed, "irn_cgls_tv": cgls, "irn_cgls_piccs": piccs,
-            "fbp_2d_fan": c1, "serving": served,
+            "fbp_2d_fan": c1, "serving": served, "widened": widened,
         }
         print(json.dumps(line))
     if world > 1:
@@ -578,6 +580,84 @@ def piccs_bench(dev, stream, barrier):
     for k in ("bfloat16", "float16"):
         out[k]["speedup"] = round(f["s_total"] / out[k]["s_total"], 3)
         out[k]["rmse_ratio"] = round(out[k]["rmse_vs_phantom"] / f["rmse_vs_phantom"], 5)
+    return out
+
+
+def widen_bench(dev, stream, barrier):
+    """The widened drop-ins on the benchmark geometry, timed with CUDA events on
+    synthetic data (their cost does not depend on the data): the view-streaming FBP of
+    the benchmark sinogram held in host memory (Mgfbp_v2, chunks of views copied while
+    earlier chunks compute), the helical FBP by rebinning (Mgfbp_helical, three
+    rounds at pitch 1 on a 1024 x 64 detector) and ADMM-TV (5 x 10, the C3 size)."""
+    import tempfile
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    from reconstruction_program_taichi_gb300.admm import Mgfbp_ir_admm
+    from reconstruction_program_taichi_gb300.fbp import Mgfbp_v2
+    from reconstruction_program_taichi_gb300.helical import Mgfbp_helical
+    rng = np.random.default_rng(5)
+    out = {}
+
+    def timed(fn):
+        fn()  # warm-up
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        barrier()
+        return r, e0.elapsed_time(e1)
+
+    w = WORKLOAD
+    v2 = Mgfbp_v2(make_config(w), device=dev, verbose=False, views_per_chunk=120)
+    v2._raw = rng.uniform(0, 1, (w["nv"], w["views"], w["nu"])).astype(np.float32)
+    v2._view_stride = w["nu"]
+    pipe = v2.pipeline
+    pipe.set_taps(hann_from_ramp(geometry.recon_taps(v2)))
+    _, ms = timed(lambda: v2._stream_file(pipe))
+    nvox = w["nx"] * w["nx"] * w["nz"]
+    out["fbp_view_streaming"] = {
+        "config": "FDK 512x512x256 from a host sinogram (1.13 GB) in chunks of 120 views, copies inside the timing",
+        "ms": round(ms, 3), "gups": round(nvox * w["views"] / (ms / 1e3) / 1e9, 2)}
+    del v2, pipe
+    torch.cuda.empty_cache()
+
+    hcfg = make_config(dict(w, nv=64, views=2160))
+    hcfg.update(TotalScanAngle=1080, HelicalPitch=1.0)
+    hel = Mgfbp_helical(hcfg, device=dev, verbose=False)
+    sgm = torch.from_numpy(rng.uniform(0, 1, (64, 2160, w["nu"])).astype(np.float32)).to(dev)
+    vol, ms = timed(lambda: hel.reconstruct(sgm, save_rebinned=False))
+    nz = vol.shape[0]
+    out["helical_fbp"] = {
+        "config": "helical, 1024x64 det @0.8mm, 3 rounds x 720 views, pitch 1.0, 512x512 slices @0.4mm",
+        "slices": nz, "views_per_slice": hel.view_count, "ms": round(ms, 3), "ms_per_slice": round(ms / nz, 4),
+        "gups": round(w["nx"] * w["nx"] * nz * hel.view_count / (ms / 1e3) / 1e9, 2)}
+    del hel, sgm, vol
+    torch.cuda.empty_cache()
+
+    with tempfile.TemporaryDirectory() as d:
+        prior = os.path.join(d, "prior.raw")
+        np.zeros((C3["nz"], C3["nx"], C3["nx"]), np.float32).tofile(prior)
+        cfg = make_config(C3)
+        cfg.update(Lambda=1e-3, BetaTV=1e-6, NumberOfIRNIterations=5, NumberOfIterations=10, Alpha=0.5,
+                   PriorImageFile=prior)
+        adm = Mgfbp_ir_admm(cfg, device=dev, verbose=False)
+    sy = adm.system
+    sgm3 = noisy(ops.project_ellipsoids(sy.dg, ellipsoids(C3)), C3["photons"], C3["seed"])
+    x0 = torch.zeros(sy.dg.vol_shape, dtype=torch.float32, device=dev)
+    calls = []
+
+    def admm():
+        c0 = sy.ptp_calls
+        x = adm.solve_admm(sgm3, x0)
+        calls.append(sy.ptp_calls - c0)
+        return x
+
+    _, ms = timed(admm)
+    out["admm_tv"] = {"config": "ADMM-TV 5 x 10 CG, 512x512x64 @0.4mm, 360 views, 1024x64 det, rho 0.1",
+                      "s_total": round(ms / 1e3, 3), "ptp": calls[-1], "s_per_ptp": round(ms / 1e3 / calls[-1], 5)}
+    del adm, sy, sgm3, x0
+    torch.cuda.empty_cache()
     return out
 
 

@@ -119,8 +119,10 @@ class Mgfbp_helical(Mgfbp):  # noqa: N801 - reference name
             t = t.permute(1, 0, 2).contiguous()
         return t
 
-    def reconstruct(self, sgm):
-        """All slices of one helical sinogram sgm [rows][views][cols] (device)."""
+    def reconstruct(self, sgm, save_rebinned=True):
+        """All slices of one helical sinogram sgm [rows][views][cols] (device).
+        save_rebinned writes the rebinned stack to InputDir/temp/sgm_rebin.raw, as the
+        reference's driver does (imaddRaw)."""
         dev = sgm.device
         nz, vc, nu, n = len(self.array_z_pos), self.view_count, self.det_elem_count_horizontal, self.img_dim
         # 1. rebinning of every slice
@@ -131,7 +133,8 @@ class Mgfbp_helical(Mgfbp):  # noqa: N801 - reference name
         stack = torch.empty((nz, vc, nu), dtype=torch.float32, device=dev)
         _lib.call("mct_helical_rebin", ctypes.byref(h), ops._ptr(sgm), ops._ptr(z_pos), ops._ptr(stack),
                   ops._stream())
-        stack.cpu().numpy().tofile(os.path.join(self.input_dir, "temp", "sgm_rebin.raw"))  # as imaddRaw leaves it
+        if save_rebinned:  # as imaddRaw leaves it
+            stack.cpu().numpy().tofile(os.path.join(self.input_dir, "temp", "sgm_rebin.raw"))
         # 2. weighting + row filter over the stack (slices as rows)
         stack_obj = self.fan_object(nz)
         pipe = FdkPipeline(stack_obj, device=dev, storage="f32")
