@@ -658,7 +658,56 @@ def widen_bench(dev, stream, barrier):
                       "s_total": round(ms / 1e3, 3), "ptp": calls[-1], "s_per_ptp": round(ms / 1e3 / calls[-1], 5)}
     del adm, sy, sgm3, x0
     torch.cuda.empty_cache()
+
+    # FDK with the run_mgfbp options, benchmark sizes, one sinogram on the device
+    from reconstruction_program_taichi_gb300 import config as mcfg
+    from reconstruction_program_taichi_gb300.fbp import FdkPipeline
+
+    class _Obj:
+        verbose = False
+
+    opts = {"curved": {"CurvedDetector": True}, "short_scan_220deg": {"TotalScanAngle": 220},
+            "coronal": {"ReconViewMode": "coronal"}, "pmatrix": None}
+    res = {}
+    sgm = torch.from_numpy(rng.uniform(0, 1, (w["nv"], w["views"], w["nu"])).astype(np.float32)).to(dev)
+    with tempfile.TemporaryDirectory() as d:
+        for name, extra in opts.items():
+            cfg = make_config(w)
+            if extra is None:
+                path = os.path.join(d, "pmatrix.jsonc")
+                with open(path, "w") as f:
+                    json.dump({"Value": [float(x) for x in circular_pmatrices(w)]}, f)
+                cfg["PMatrixFile"] = path
+            else:
+                cfg.update(extra)
+            o = _Obj()
+            mcfg.parse_fbp(o, cfg)
+            pipe = FdkPipeline(o, device=dev)
+            _, ms = timed(lambda: pipe.run(sgm))
+            res[name] = {"ms": round(ms, 3), "gups": round(nvox * w["views"] / (ms / 1e3) / 1e9, 2)}
+            del pipe
+            torch.cuda.empty_cache()
+    out["fdk_options"] = dict(config="FDK 512x512x256, 1080 views, 1024x256 det, device-resident sinogram", **res)
+    del sgm
+    torch.cuda.empty_cache()
     return out
+
+
+def circular_pmatrices(w):
+    """3x4 projection matrices of the benchmark's circular scan, P_j = [e_u e_v d]^-1
+    [I | -s]: source s at angle 2 pi j / views on the circle of radius SID, flat
+    detector at SDD with pixel vectors e_u, e_v, centred.  Flattened, 12 per view."""
+    out = []
+    for j in range(w["views"]):
+        b = 2 * np.pi * j / w["views"]
+        c, s_ = np.cos(b), np.sin(b)
+        src = np.array([w["sid"] * c, w["sid"] * s_, 0.0])
+        e_u = w["du"] * np.array([s_, -c, 0.0])
+        e_v = w["dv"] * np.array([0.0, 0.0, -1.0])
+        origin = src - w["sdd"] * np.array([c, s_, 0.0]) - (w["nu"] - 1) / 2 * e_u - (w["nv"] - 1) / 2 * e_v
+        m = np.linalg.inv(np.stack([e_u, e_v, origin - src], axis=1))
+        out.append(np.concatenate([m, (-m @ src)[:, None]], axis=1).reshape(-1))
+    return np.concatenate(out)
 
 
 def serve_bench(dev, n_req=256, seed=7, mean_gap_ms=150.0):
