@@ -64,7 +64,8 @@ __device__ __forceinline__ void fill_view_table(const BpParams& p, const float* 
 
 // MODE 0: axial, flat or curved detector, no projection matrix (u hoisted per column)
 // MODE 1: any view mode, no projection matrix (per-voxel u)
-// MODE 2: projection matrix geometry
+// MODE 2: projection matrix geometry, any view mode (per-voxel matrix products)
+// MODE 3: projection matrix geometry, axial view mode (per-column matrix rows)
 template <int MODE, bool CONE, typename QT, typename PT>
 __global__ void __launch_bounds__(BP_TX* BP_TY, bp_min_blocks<MODE, QT>())
 fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
@@ -143,6 +144,74 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                             const float2 pr = Pair<PT>::load(base + (int64_t)k * nq);
                             acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
                         }
+                    }
+                }
+            } else if (MODE == 3) {
+                // Axial view mode with projection matrices: x and y are fixed per column, so
+                // the matrix rows are affine in the slice index and the distance weight does
+                // not depend on z.  An untilted trajectory has no z term in the u and depth
+                // rows (P2 = P10 = 0 up to rounding left by the matrix processing): when
+                // 16 |B| < 2^-26 |A| for both, fmaf(k, B, A) rounds to A for every slice, so
+                // u and the magnification are the column's (as in MODE 0) and taking them
+                // once gives exactly the per-slice result.
+                const float* P = pmat + 12 * (p.view_begin + j);
+                const float P0 = __ldg(P + 0), P1 = __ldg(P + 1), P2 = __ldg(P + 2), P3 = __ldg(P + 3);
+                const float P4 = __ldg(P + 4), P5 = __ldg(P + 5), P6 = __ldg(P + 6), P7 = __ldg(P + 7);
+                const float P8 = __ldg(P + 8), P9 = __ldg(P + 9), P10 = __ldg(P + 10), P11 = __ldg(P + 11);
+                const float dz = p.pz_z;
+                const float Au = P0 * c0x + P1 * c0y + P2 * c0z + P3, Bu = P2 * dz;
+                const float Av = P4 * c0x + P5 * c0y + P6 * c0z + P7, Bv = P6 * dz;
+                const float Aw = P8 * c0x + P9 * c0y + P10 * c0z + P11, Bw = P10 * dz;
+                const float L = p.sid - c0x * cb - c0y * sb;
+                const float t = -c0x * sb + c0y * cb;
+                const float dw = p.curved ? 1.0f / (L * L + t * t) : 1.0f / (L * L);
+                const float w = (p.sid * dw) * tb.z;
+                const unsigned nan_row = (unsigned)(p.nv - 1);  // rows outside [0, nv-2] read the NaN row
+                const QT* view = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq;
+                const float tiny = 0x1p-26f / (float)BP_ZC;
+                if (fabsf(Bu) <= tiny * fabsf(Au) && fabsf(Bw) <= tiny * fabsf(Aw)) {
+                    const float mag = 1.0f / Aw;
+                    const float ui = Au * mag;
+                    if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {  // NaN counts as off-detector
+                        dead = 0xffffffffu;
+                        break;
+                    }
+                    const float uf = floorf(ui);
+                    const float ru = ui - uf;
+                    const QT* base = view + (int)uf;
+                    const float2 ru2 = make_float2(ru, ru);
+#pragma unroll
+                    for (int k = 0; k < BP_ZC; ++k) {
+                        const float vi = fmaf((float)k, Bv, Av) * mag;  // as in the per-slice branch
+                        const float vf = floorf(vi);
+                        const unsigned vr = min((unsigned)(int)vf, nan_row);
+                        const float rv = vi - vf;
+                        float2 lo, hi;
+                        Quad<QT>::load(base + vr * (unsigned)nq, lo, hi);
+                        const float2 s2 = __ffma2_rn(ru2, hi, lo);
+                        acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < BP_ZC; ++k) {
+                        if ((dead >> k) & 1u) continue;
+                        const float fk = (float)k;
+                        const float mag = 1.0f / fmaf(fk, Bw, Aw);
+                        const float ui = fmaf(fk, Bu, Au) * mag;
+                        if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {
+                            dead |= 1u << k;
+                            continue;
+                        }
+                        const float uf = floorf(ui);
+                        const float ru = ui - uf;
+                        const float vi = fmaf(fk, Bv, Av) * mag;
+                        const float vf = floorf(vi);
+                        const unsigned vr = min((unsigned)(int)vf, nan_row);
+                        const float rv = vi - vf;
+                        float2 lo, hi;
+                        Quad<QT>::load(view + vr * (unsigned)nq + (int)uf, lo, hi);
+                        const float2 s2 = __ffma2_rn(make_float2(ru, ru), hi, lo);
+                        acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
                     }
                 }
             } else {
@@ -394,7 +463,8 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     cudaStream_t s = as_stream(stream);
     const bool axial_fast = g->view_mode == 1 && !pm;
     const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
-    if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
+    if (pm && g->view_mode == 1) launch_bp<3, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
+    else if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
     else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else if (axial_fast) {
         MCT_REQUIRE(g->nx <= 65535, "mct_fdk_bp: fan beam images are at most 65535 pixels wide");
