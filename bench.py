@@ -322,7 +322,9 @@ def run_gpu(args, w):
     # mixed precision: tensor-core split-bf16 filter, bf16 backprojection operand, bf16
     # forward-projection cells; the whole step, then FDK-only variants
     mixed = None
-    if args.storage == "f32" and not args.no_mixed:
+    # the mixed-precision, 2D, iterative and widened sections run in single-GPU runs
+    # (they do not enter the metric; with several ranks they would only repeat per rank)
+    if args.storage == "f32" and not args.no_mixed and world == 1:
         ref_vol = pipe.run(sgm).clone()
         ref_fp = ops.fp(fpg, ref_vol).clone()
         plain_ms = float(st[0] + st[1] + st[2])
@@ -385,10 +387,10 @@ def run_gpu(args, w):
             del pm
 
     cgls = piccs = c1 = served = None
-    if w is WORKLOAD and not args.no_mixed:
+    if w is WORKLOAD and not args.no_mixed and world == 1:
         c1 = c1_bench(dev, stream, barrier)
     widened = None
-    if not args.no_cgls and w is WORKLOAD:
+    if not args.no_cgls and w is WORKLOAD and world == 1:
         cgls = irn_bench(dev, stream, barrier)
         piccs = piccs_bench(dev, stream, barrier)
         widened = widen_bench(dev, stream, barrier)
