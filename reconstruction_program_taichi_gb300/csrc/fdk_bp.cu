@@ -222,14 +222,17 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     P4 = __ldg(P + 4); P5 = __ldg(P + 5); P6 = __ldg(P + 6); P7 = __ldg(P + 7);
                     P8 = __ldg(P + 8); P9 = __ldg(P + 9); P10 = __ldg(P + 10); P11 = __ldg(P + 11);
                 }
+                // the voxel moves by (pz_x, pz_y, pz_z) per slice, so L and t are affine in k
+                const float L0 = p.sid - c0x * cb - c0y * sb, dL = -(p.pz_x * cb + p.pz_y * sb);
+                const float t0 = -c0x * sb + c0y * cb, dt = -p.pz_x * sb + p.pz_y * cb;
 #pragma unroll
                 for (int k = 0; k < BP_ZC; ++k) {
                     if (zb + k >= p.nz || (dead >> k) & 1u) continue;
                     const float x = fmaf((float)k, p.pz_x, c0x);
                     const float y = fmaf((float)k, p.pz_y, c0y);
                     const float z = fmaf((float)k, p.pz_z, c0z);
-                    const float L = p.sid - x * cb - y * sb;
-                    const float t = -x * sb + y * cb;
+                    const float L = fmaf((float)k, dL, L0);
+                    const float t = fmaf((float)k, dt, t0);
                     float mag, ui, rL = 0.0f;
                     if (MODE == 2) {
                         mag = 1.0f / (P8 * x + P9 * y + P10 * z + P11);
