@@ -658,6 +658,17 @@ def widen_bench(dev, stream, barrier):
     _, ms = timed(admm)
     out["admm_tv"] = {"config": "ADMM-TV 5 x 10 CG, 512x512x64 @0.4mm, 360 views, 1024x64 det, rho 0.1",
                       "s_total": round(ms / 1e3, 3), "ptp": calls[-1], "s_per_ptp": round(ms / 1e3 / calls[-1], 5)}
+    # the autograd pair: the projector and its exact adjoint on the same geometry; the
+    # adjoint scatters through the cell-space buffer (default) or straight into the volume
+    xs = torch.rand(sy.dg.vol_shape, device=dev)
+    ys = torch.rand(sy.dg.sgm_shape, device=dev)
+    _, ms_fp = timed(lambda: ops.fp(sy.dg, xs))
+    _, ms_ad = timed(lambda: ops.fp_adjoint(sy.dg, ys))
+    _, ms_ad_direct = timed(lambda: ops.fp_adjoint(sy.dg, ys, workspace=None))
+    out["fp_adjoint_pair"] = {"config": "512x512x64 @0.4mm, 360 views, 1024x64 det, no mask",
+                              "fp_ms": round(ms_fp, 3), "adjoint_ms": round(ms_ad, 3),
+                              "adjoint_direct_scatter_ms": round(ms_ad_direct, 3)}
+    del xs, ys
     del adm, sy, sgm3, x0
     torch.cuda.empty_cache()
 

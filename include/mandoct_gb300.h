@@ -231,6 +231,19 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
 int mct_fp_adjoint(const mct_geom* g, const mct_tables* t, const float* sgm, const float* mask,
                    float* vol, void* stream);
 
+/* Bytes of the mct_fp_adjoint_cells workspace: 32 per voxel in cone beam (the 8
+ * corner sums of each trilinear cell), 16 in fan beam (4 per slice cell). */
+size_t mct_fp_adjoint_workspace_size(const mct_geom* g);
+
+/* mct_fp_adjoint (vol += P^T sgm) with the scatter done in cell space: each ray
+ * flushes a cell's corner sums with one (fan) or two (cone) 16-byte vector
+ * reductions into workspace (mct_fp_adjoint_workspace_size bytes, 16-byte aligned,
+ * cleared on the stream by this call), then one pass adds to each voxel the entries of
+ * the cells that contain it.  Same operator as mct_fp_adjoint up to the order of the
+ * float32 additions.  No counterpart in the reference. */
+int mct_fp_adjoint_cells(const mct_geom* g, const mct_tables* t, const float* sgm, const float* mask,
+                         float* vol, void* workspace, void* stream);
+
 /* *count (device uint64) = number of trilinear samples of mct_fp whose stencil lies
  * inside the volume (rays with mask != 1 excluded): the forward projector's
  * algorithmic work.  No counterpart in the reference. */

@@ -92,6 +92,8 @@ SIGNATURES = {
     "mct_fp_storage_workspace_size": (ctypes.c_size_t, [_G, _i32]),
     "mct_fp_storage": (ctypes.c_int, [_G, _T, _P, _P, _P, _P, _i32, _P]),
     "mct_fp_adjoint": (ctypes.c_int, [_G, _T, _P, _P, _P, _P]),
+    "mct_fp_adjoint_workspace_size": (ctypes.c_size_t, [_G]),
+    "mct_fp_adjoint_cells": (ctypes.c_int, [_G, _T, _P, _P, _P, _P, _P]),
     "mct_effective_map": (ctypes.c_int, [_G, _T, _P, _P]),
     "mct_fp_count_samples": (ctypes.c_int, [_G, _T, _P, _P, _P]),
     "mct_bin_noise": (ctypes.c_int, [_G, _P, _i32, _f32, _u64, _P, _P]),

@@ -452,8 +452,20 @@ __global__ void transpose_xy_kernel(int nx, int nz, const float* __restrict__ v,
     }
 }
 
+// 16-byte vector reduction (sm_90 and later): four float adds at one aligned address,
+// one L2 atomic request instead of four.
+__device__ __forceinline__ void red_add_v4(float* q, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(q), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
 // Exact transpose of fp_kernel: every in-volume sample scatters its trilinear weights
-// times the ray value into the volume.
+// times the ray value into the volume.  CELLS: the corner sums go to a cell-space
+// buffer instead (per cell of the 2x2x2 stencil its 8 corner sums, z-low 4 then
+// z-high 4, each group ordered (x,y) (x+1,y) (x,y+1) (x+1,y+1); fan beam: the 4 of the
+// slice), one or two 16-byte reductions per flush; adjoint_gather_kernel then sums
+// each voxel's corner entries from the cells that contain it.
+template <bool CELLS>
 __global__ void __launch_bounds__(256)
 fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
                   const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
@@ -477,6 +489,13 @@ fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __r
     float s00 = 0.f, s01 = 0.f, s10 = 0.f, s11 = 0.f, t00 = 0.f, t01 = 0.f, t10 = 0.f, t11 = 0.f;
     auto flush = [&]() {
         if (cell < 0) return;
+        if (CELLS) {
+            float* c = vol + (int64_t)cell * (p.cone ? 8 : 4);
+            red_add_v4(c, s00, s01, s10, s11);
+            if (p.cone) red_add_v4(c + 4, t00, t01, t10, t11);
+            s00 = s01 = s10 = s11 = t00 = t01 = t10 = t11 = 0.f;
+            return;
+        }
         float* b = vol + cell;
         atomicAdd(b, s00);
         atomicAdd(b + 1, s01);
@@ -530,6 +549,35 @@ fp_adjoint_kernel(FpParams p, const float* __restrict__ angles, const float* __r
         }
     }
     flush();
+}
+
+// vol[z][y][x] += the corner entries of the (up to) 8 cells that contain voxel
+// (z, y, x), in a fixed order.  C = 8 (cone beam) or 4 (fan beam: one slice per cell).
+template <int C>
+__global__ void __launch_bounds__(256)
+adjoint_gather_kernel(int nx, int nz, const float* __restrict__ cells, float* __restrict__ vol) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= nx || y >= nx || z >= nz) return;
+    const int64_t plane = (int64_t)nx * nx;
+    const int64_t v = z * plane + (int64_t)y * nx + x;
+    float acc = 0.0f;
+#pragma unroll
+    for (int dz = 0; dz < C / 4; ++dz) {
+        if (z - dz < 0) continue;
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            if (y - dy < 0) continue;
+#pragma unroll
+            for (int dx = 0; dx < 2; ++dx) {
+                if (x - dx < 0) continue;
+                const int64_t c = v - dz * plane - (int64_t)dy * nx - dx;
+                acc += __ldg(cells + c * C + dz * 4 + dy * 2 + dx);
+            }
+        }
+    }
+    vol[v] += acc;
 }
 
 // Effective ray map, run_mgfbp_iterative_recon_IRN_CGLS.py:749-833.
@@ -799,9 +847,39 @@ int mct_fp_adjoint(const mct_geom* g, const mct_tables* t, const float* sgm, con
     MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp_adjoint: NULL buffer");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp_adjoint: projection-matrix tables missing");
     dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
-    fp_adjoint_kernel<<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
-                                                             sgm, mask, vol);
+    fp_adjoint_kernel<false><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a,
+                                                                    t->pmat_xs, sgm, mask, vol);
     return launched("fp_adjoint_kernel");
+}
+
+size_t mct_fp_adjoint_workspace_size(const mct_geom* g) {
+    if (!g || g->nx < 1 || g->nz < 1) return 0;
+    return (size_t)g->nz * g->nx * g->nx * ((g->flags & MCT_CONE) ? 32 : 16);
+}
+
+int mct_fp_adjoint_cells(const mct_geom* g, const mct_tables* t, const float* sgm, const float* mask, float* vol,
+                         void* workspace, void* stream) {
+    FpParams p;
+    MCT_TRY(make_params(g, p, "mct_fp_adjoint_cells"));
+    MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm && workspace, "mct_fp_adjoint_cells: NULL buffer");
+    MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp_adjoint_cells: projection-matrix tables missing");
+    MCT_REQUIRE(((uintptr_t)workspace & 15) == 0, "mct_fp_adjoint_cells: workspace must be 16-byte aligned");
+    MCT_REQUIRE(g->nx <= 65535 * 8 && g->nz <= 65535, "mct_fp_adjoint_cells: at most 524280 x 524280 x 65535 voxels");
+    cudaStream_t s = as_stream(stream);
+    float* cells = static_cast<float*>(workspace);
+    const int C = p.cone ? 8 : 4;
+    MCT_REQUIRE(cudaMemsetAsync(cells, 0, mct_fp_adjoint_workspace_size(g), s) == cudaSuccess,
+                "mct_fp_adjoint_cells: clearing the workspace failed");
+    dim3 block(32, 8), grid((g->nu + 31) / 32, g->views, (g->nv + 7) / 8);
+    fp_adjoint_kernel<true><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, sgm,
+                                                   mask, cells);
+    MCT_TRY(launched("fp_adjoint_kernel"));
+    dim3 gb(32, 8), gg((g->nx + 31) / 32, (g->nx + 7) / 8, g->nz);
+    if (C == 8)
+        adjoint_gather_kernel<8><<<gg, gb, 0, s>>>(g->nx, g->nz, cells, vol);
+    else
+        adjoint_gather_kernel<4><<<gg, gb, 0, s>>>(g->nx, g->nz, cells, vol);
+    return launched("adjoint_gather_kernel");
 }
 
 int mct_fp_count_samples(const mct_geom* g, const mct_tables* t, const float* mask, uint64_t* count, void* stream) {

@@ -249,7 +249,20 @@ def fp(dg, vol, mask=None, out=None, workspace=True, dtype=MCT_F32):
     return out
 
 
-def fp_adjoint(dg, sgm, mask=None, out=None, accumulate=False):
+def fp_adjoint_workspace(dg):
+    """Per-geometry cell-space buffer of fp_adjoint() (cached)."""
+    ws = dg.__dict__.get("_adj_ws")
+    if ws is None:
+        n = int(_lib.load().mct_fp_adjoint_workspace_size(dg.g()))
+        ws = torch.empty(max(n // 4, 4), dtype=torch.float32, device=dg.device)
+        dg.__dict__["_adj_ws"] = ws
+    return ws
+
+
+def fp_adjoint(dg, sgm, mask=None, out=None, accumulate=False, workspace=True):
+    """P^T sgm, the exact transpose of fp().  workspace=True scatters through the
+    geometry's cached cell-space buffer (mct_fp_adjoint_cells); None scatters the 8
+    corner weights straight into the volume (mct_fp_adjoint)."""
     _check(sgm, "sgm", dg.sgm_shape)
     if mask is not None:
         _check(mask, "mask", dg.sgm_shape)
@@ -258,7 +271,11 @@ def fp_adjoint(dg, sgm, mask=None, out=None, accumulate=False):
     elif not accumulate:
         out.zero_()
     _check(out, "out", dg.vol_shape)
-    _lib.call("mct_fp_adjoint", dg.g(), dg.t(), _ptr(sgm), _ptr(mask), _ptr(out), _stream())
+    ws = fp_adjoint_workspace(dg) if workspace is True else workspace
+    if ws is None:
+        _lib.call("mct_fp_adjoint", dg.g(), dg.t(), _ptr(sgm), _ptr(mask), _ptr(out), _stream())
+    else:
+        _lib.call("mct_fp_adjoint_cells", dg.g(), dg.t(), _ptr(sgm), _ptr(mask), _ptr(out), _ptr(ws), _stream())
     return out
 
 

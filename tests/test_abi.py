@@ -74,6 +74,9 @@ def test_entry_points_reject_bad_arguments_before_any_launch():
         # float32 cone-beam cell copies are read with 32-byte loads
         ("mct_fp", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, ctypes.c_void_p(4112), None),
          "32-byte"),
+        # the cell-space adjoint reduces 16 bytes at a time
+        ("mct_fp_adjoint_cells", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE,
+                                  ctypes.c_void_p(4104), None), "16-byte"),
         # 16-bit forward projection needs a workspace
         ("mct_fp_storage", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, None, 1, None),
          "workspace"),
@@ -115,3 +118,5 @@ def test_packed_and_workspace_sizes():
     assert lib.mct_fp_workspace_size(ctypes.byref(g)) == 2 * 32 * 32 * 8 * 32
     assert lib.mct_fp_storage_workspace_size(ctypes.byref(g), 0) == 2 * 32 * 32 * 8 * 32
     assert lib.mct_fp_workspace_size(ctypes.byref(fan)) == 32 * 32 * 16 * 4
+    assert lib.mct_fp_adjoint_workspace_size(ctypes.byref(g)) == 32 * 32 * 8 * 32
+    assert lib.mct_fp_adjoint_workspace_size(ctypes.byref(fan)) == 32 * 32 * 16 * 16
