@@ -480,14 +480,17 @@ def test_packed_unmatched_bp_matches_plain(cone, cuda):
     assert float((a - b).abs().max()) < 1e-5 * float(a.abs().max())
 
 
-def test_fp_bf16_storage_error_is_small(cuda):
+@pytest.mark.parametrize("views,nv", [(60, 40), (30, 13)])
+def test_fp_bf16_storage_error_is_small(views, nv, cuda):
     """bf16 cell copies: only stored values are rounded (the base corner to 2^-9
     relative, the other corners through rounded differences); the projection error
-    stays far below that, and which rays are zero is unchanged."""
+    stays far below that, and which rays are zero is unchanged.  The 16-bit projector
+    runs 4 views x 2 rows per block: 30 views and 13 rows leave a partial view group
+    and a lone last row, whose rays must all be written."""
     import torch
     from reconstruction_program_taichi_gb300 import geometry, ops
     from reconstruction_program_taichi_gb300._lib import MCT_BF16, MCT_F16
-    o = _cone_obj(views=60)
+    o = _cone_obj(views=views, nv=nv)
     dg = geometry.fpj_geometry(o)
     vol = torch.from_numpy(_smooth(np.random.default_rng(9), o.img_dim_z, o.img_dim)).cuda()
     a = ops.fp(dg, vol)
