@@ -658,18 +658,8 @@ def widen_bench(dev, stream, barrier):
     _, ms = timed(admm)
     out["admm_tv"] = {"config": "ADMM-TV 5 x 10 CG, 512x512x64 @0.4mm, 360 views, 1024x64 det, rho 0.1",
                       "s_total": round(ms / 1e3, 3), "ptp": calls[-1], "s_per_ptp": round(ms / 1e3 / calls[-1], 5)}
-    # the autograd pair: the projector and its exact adjoint on the same geometry; the
-    # adjoint scatters through the cell-space buffer (default) or straight into the volume
-    xs = torch.rand(sy.dg.vol_shape, device=dev)
-    ys = torch.rand(sy.dg.sgm_shape, device=dev)
-    _, ms_fp = timed(lambda: ops.fp(sy.dg, xs))
-    _, ms_ad = timed(lambda: ops.fp_adjoint(sy.dg, ys))
-    _, ms_ad_direct = timed(lambda: ops.fp_adjoint(sy.dg, ys, workspace=None))
-    out["fp_adjoint_pair"] = {"config": "512x512x64 @0.4mm, 360 views, 1024x64 det, no mask",
-                              "fp_ms": round(ms_fp, 3), "adjoint_ms": round(ms_ad, 3),
-                              "adjoint_direct_scatter_ms": round(ms_ad_direct, 3)}
-    del xs, ys
     del adm, sy, sgm3, x0
+    out["fp_adjoint_pair"] = adjoint_pair_bench(dev, stream, barrier)
     torch.cuda.empty_cache()
 
     # FDK with the run_mgfbp options, benchmark sizes, one sinogram on the device
@@ -704,6 +694,33 @@ def widen_bench(dev, stream, barrier):
     del sgm
     torch.cuda.empty_cache()
     return out
+
+
+def adjoint_pair_bench(dev, stream, barrier):
+    """The autograd pair at 512x512x64, 360 views: the projector and its exact adjoint,
+    which scatters through the cell-space buffer (default) or straight into the volume."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    dg = geometry.fpj_geometry(parse(C3), device=dev)
+    g = torch.Generator(device=dev).manual_seed(C3["seed"])
+    xs = torch.rand(dg.vol_shape, device=dev, generator=g)
+    ys = torch.rand(dg.sgm_shape, device=dev, generator=g)
+
+    def timed(fn):
+        fn()  # warm-up
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        barrier()
+        return e0.elapsed_time(e1)
+
+    ms_ad = timed(lambda: ops.fp_adjoint(dg, ys))
+    ms_ad_direct = timed(lambda: ops.fp_adjoint(dg, ys, workspace=None))
+    ms_fp = timed(lambda: ops.fp(dg, xs))
+    return {"config": "512x512x64 @0.4mm, 360 views, 1024x64 det, no mask", "fp_ms": round(ms_fp, 3),
+            "adjoint_ms": round(ms_ad, 3), "adjoint_direct_scatter_ms": round(ms_ad_direct, 3)}
 
 
 def circular_pmatrices(w):
@@ -895,8 +912,9 @@ def main():
     ap.add_argument("--no-cgls", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--only", default=None, choices=["cgls"],
-                    help="cgls: only the IRN-CGLS-TV section (a short run for ncu captures of its kernels)")
+    ap.add_argument("--only", default=None, choices=["cgls", "adjoint"],
+                    help="cgls: only the IRN-CGLS-TV section; adjoint: only the projector / exact-adjoint "
+                         "pair (short runs for ncu captures of their kernels)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -907,6 +925,12 @@ def main():
         torch.cuda.set_device(dev)
         out = irn_bench(dev, torch.cuda.current_stream(dev), torch.cuda.synchronize)
         print(json.dumps({"irn_cgls_tv": out}))
+    elif args.only == "adjoint":
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        out = adjoint_pair_bench(dev, torch.cuda.current_stream(dev), torch.cuda.synchronize)
+        print(json.dumps({"fp_adjoint_pair": out}))
     else:
         run_gpu(args, w)
 
