@@ -204,8 +204,21 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     return *reinterpret_cast<uint32_t*>(&b);
 }
 
+// Resident blocks per SM that the register allocation of fp_kernel targets.  The
+// float32 cone-beam path waits on L2 and needs its warps: 5 blocks (48 registers) take
+// 297 ms at 512x512x256 / 1080 views, 4 blocks 321 ms, 3 blocks (71 registers) 400 ms;
+// the fan-beam path keeps 40 registers (6 blocks).  The 16-bit paths are issue-bound
+// and gain from registers: 1 (80 registers, 3 blocks of 256) gives bf16 237.4 ms
+// against 254.9 with 5 blocks, float16 274.4 against 291.7.
+template <bool CONE, typename ZT>
+struct FpMinBlocks {
+    static constexpr int value = (std::is_same<ZT, uint4>::value || std::is_same<ZT, h16x8>::value) ? 1
+                                 : CONE                                                             ? 5
+                                                                                                    : 6;
+};
+
 template <bool CONE, bool ZP, typename ZT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, FpMinBlocks<CONE, ZT>::value)
 fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict__ u_arr,
           const float* __restrict__ v_arr, const float* __restrict__ czv, const float* __restrict__ pa,
           const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
