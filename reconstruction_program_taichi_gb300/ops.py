@@ -219,7 +219,8 @@ def fdk_bp(dg, packed, dtype=MCT_F32, out=None):
 
 def fp_workspace(dg, dtype=MCT_F32):
     """Per-geometry workspace of fp() (the gather copies of the volume), cached per
-    storage type."""
+    storage type.  It belongs to the geometry object: calls that share one geometry
+    must be ordered on one stream, or pass workspaces of their own."""
     cache = dg.__dict__.setdefault("_fp_ws", {})
     ws = cache.get(int(dtype))
     if ws is None:
@@ -250,7 +251,8 @@ def fp(dg, vol, mask=None, out=None, workspace=True, dtype=MCT_F32):
 
 
 def fp_adjoint_workspace(dg):
-    """Per-geometry cell-space buffer of fp_adjoint() (cached)."""
+    """Per-geometry cell-space buffer of fp_adjoint() (cached; like fp_workspace() it
+    belongs to the geometry object, so calls sharing a geometry stay on one stream)."""
     ws = dg.__dict__.get("_adj_ws")
     if ws is None:
         n = int(_lib.load().mct_fp_adjoint_workspace_size(dg.g()))
