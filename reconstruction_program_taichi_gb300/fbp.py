@@ -17,6 +17,7 @@ from . import ops
 from ._lib import MCT_BF16, MCT_F16, MCT_F32
 from .config import ConfigError, ReadConfigFile, parse_fbp
 from .geometry import fbp_geometry, gaussian_taps, recon_taps
+from .file_pipeline import run_over_files
 from .io import imwriteRaw, imwriteTiff, read_sinogram_file, read_sinogram_raw_layout
 
 STORAGE = {"f32": MCT_F32, "float32": MCT_F32, "bf16": MCT_BF16, "bfloat16": MCT_BF16, "f16": MCT_F16,
@@ -129,19 +130,21 @@ class Mgfbp:
                               "in the config!")
         pipe = self.pipeline
         self.file_processed_count = 0
-        for file in os.listdir(self.input_dir):
-            if re.match(self.input_files_pattern, file):
-                if self.ReadSinogram(file):
-                    self.file_processed_count += 1
-                    self._log("Reconstructing %s ..." % self.input_path)
-                    dev = torch.from_numpy(self._raw).to(pipe.device, non_blocking=False)
-                    filtered = pipe.filter(dev, self._row_stride, self._view_stride)
-                    if self.save_filtered_sinogram:
-                        imwriteTiff(filtered.cpu().numpy(), self.output_dir + "/sgm_filtered_" + self.output_file)
-                    vol = pipe.backproject(filtered)
-                    self.img_recon = vol.cpu().numpy()
-                    self._log("Saving to %s !" % self.output_path)
-                    self.SaveReconImg()
+
+        def compute(d):
+            d.file_processed_count += 1
+            d._log("Reconstructing %s ..." % d.input_path)
+            dev = torch.from_numpy(d._raw).to(pipe.device, non_blocking=False)
+            filtered = pipe.filter(dev, d._row_stride, d._view_stride)
+            if d.save_filtered_sinogram:
+                imwriteTiff(filtered.cpu().numpy(), d.output_dir + "/sgm_filtered_" + d.output_file)
+            vol = pipe.backproject(filtered)
+            d.img_recon = vol.cpu().numpy()
+            d._log("Saving to %s !" % d.output_path)
+
+        # the next file is read and the previous one written while this one runs
+        files = [f for f in os.listdir(self.input_dir) if re.match(self.input_files_pattern, f)]
+        run_over_files(self, files, lambda d, f: d.ReadSinogram(f), compute, lambda d: d.SaveReconImg())
         return self.img_recon
 
     def output_name(self, file):

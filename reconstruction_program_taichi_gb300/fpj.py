@@ -13,6 +13,7 @@ import torch
 from . import ops
 from .config import ConfigError, ReadConfigFile, parse_fbp, parse_fpj, parse_fpj_v1, parse_fpj_v3
 from .geometry import fpj_geometry, fpj_variant_geometry
+from .file_pipeline import run_over_files
 from .io import imwriteRaw
 
 
@@ -108,18 +109,20 @@ class Mgfpj_v3:  # noqa: N801 - reference name
         """Forward project every matching volume (run_mgfpj_v3.py:82-127)."""
         pipe = self.pipeline
         self.file_processed_count = 0
-        for file in os.listdir(self.input_dir):
-            if re.match(self.input_files_pattern, file):
-                if self.ReadImage(file):
-                    if self.verbose:
-                        print("\nForward projecting %s ..." % self.input_path)
-                    self.file_processed_count += 1
-                    vol = torch.from_numpy(self.img_image).to(pipe.dg.device)
-                    sgm = pipe.project(vol, seed=self.noise_seed + self.file_processed_count)
-                    self.img_sgm = sgm.cpu().numpy()
-                    if self.verbose:
-                        print("\nSaving to %s !" % self.output_path)
-                    self.SaveSinogram()
+
+        def compute(d):
+            if d.verbose:
+                print("\nForward projecting %s ..." % d.input_path)
+            d.file_processed_count += 1
+            vol = torch.from_numpy(d.img_image).to(pipe.dg.device)
+            sgm = pipe.project(vol, seed=d.noise_seed + d.file_processed_count)
+            d.img_sgm = sgm.cpu().numpy()
+            if d.verbose:
+                print("\nSaving to %s !" % d.output_path)
+
+        # the next volume is read and the previous sinogram written while this one runs
+        files = [f for f in os.listdir(self.input_dir) if re.match(self.input_files_pattern, f)]
+        run_over_files(self, files, lambda d, f: d.ReadImage(f), compute, lambda d: d.SaveSinogram())
         return self.img_sgm
 
     def SaveSinogram(self):  # noqa: N802 - reference name
