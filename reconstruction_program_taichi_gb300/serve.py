@@ -19,20 +19,27 @@ Model
     spent, idle slots of other classes are evicted, least recently used first.
   * Inputs may be host arrays or CUDA tensors already resident on the device; the
     result comes back in the same form (a new device tensor for device inputs, so
-    resident data never crosses the host link).
+    resident data never crosses the host link).  Inputs may also be file paths, read
+    with the reference's conventions for the request's config on the server's I/O
+    threads from the moment of submission; a request is admitted only once its
+    inputs are in memory, so disk reads overlap the GPU work of other requests.  With
+    `out_path` the result is also written there on an I/O thread after its slot has
+    been released; the future resolves once the file is written.
   * Results do not depend on the mix: every kernel is deterministic and a slot's
     graph always runs the same kernels on the same buffer layout.
 """
+import os
 import queue
 import threading
 import time
-from concurrent.futures import Future
+from concurrent.futures import Future, ThreadPoolExecutor
 
 import numpy as np
 import torch
 
 from . import ops
 from .fbp import FdkPipeline
+from .io import imwriteRaw, read_sinogram_file
 
 _SENTINEL = object()
 
@@ -48,6 +55,29 @@ def _geom_key(obj, kind, extra=()):
     return (kind,) + g + tuple(extra)
 
 
+def _is_path(a):
+    return isinstance(a, (str, os.PathLike))
+
+
+def _input_error(r):
+    """The exception of a failed input read of request r, else None."""
+    for a in (r.sgm, r.x0):
+        if isinstance(a, Future) and a.done() and a.exception() is not None:
+            return a.exception()
+    return None
+
+
+def _inputs_ready(r):
+    return all(not isinstance(a, Future) or a.done() for a in (r.sgm, r.x0))
+
+
+def _resolve_inputs(r):
+    if isinstance(r.sgm, Future):
+        r.sgm = r.sgm.result()
+    if isinstance(r.x0, Future):
+        r.x0 = r.x0.result()
+
+
 def _to_device(a, device):
     """A host array or a tensor as a float32 tensor on device (no copy when it already is)."""
     if isinstance(a, torch.Tensor):
@@ -57,10 +87,11 @@ def _to_device(a, device):
 
 class _Request:
     __slots__ = ("kind", "obj", "sgm", "x0", "n_iter", "storage", "key", "future", "t_arrive", "t_start",
-                 "t_done", "units", "on_device")
+                 "t_done", "units", "on_device", "out_path")
 
-    def __init__(self, kind, obj, sgm, x0=None, n_iter=0, storage="f32"):
+    def __init__(self, kind, obj, sgm, x0=None, n_iter=0, storage="f32", out_path=None):
         self.kind, self.obj, self.sgm, self.x0, self.n_iter, self.storage = kind, obj, sgm, x0, n_iter, storage
+        self.out_path = out_path
         extra = (storage, n_iter) if kind == "cgls" else (storage,)
         self.key = _geom_key(obj, kind, extra)
         self.future = Future()
@@ -192,19 +223,27 @@ class ReconServer:
         self.closed = False
         self.errors = []
         self._workers = []
+        self._io = ThreadPoolExecutor(2, thread_name_prefix="mct-serve-io")
         self._thread = threading.Thread(target=self._schedule, daemon=True)
         self._thread.start()
 
     # ------------------------------------------------------------ API
-    def submit_fbp(self, obj, sgm, storage="f32"):
-        """FBP/FDK of a sinogram [rows, views, cols] (host array or CUDA tensor) for the
-        parsed config obj; the future's result is a host array or a new CUDA tensor."""
-        return self._submit(_Request("fbp", obj, sgm, storage=storage))
+    def submit_fbp(self, obj, sgm, storage="f32", out_path=None):
+        """FBP/FDK of a sinogram [rows, views, cols] (host array, CUDA tensor, or the path
+        of an input file in the config's InputFileForm and detector row range) for the
+        parsed config obj; the future's result is a host array or a new CUDA tensor.
+        out_path: also write the result there (raw float32)."""
+        sgm = self._load(sgm, lambda p: read_sinogram_file(obj, p))
+        return self._submit(_Request("fbp", obj, sgm, storage=storage, out_path=out_path))
 
-    def submit_cgls(self, obj, sgm, x0, n_iter):
-        """n_iter CGLS iterations (Tikhonov-TV with unit weights) from x0 (host arrays
-        or CUDA tensors, as for submit_fbp)."""
-        return self._submit(_Request("cgls", obj, sgm, x0=x0, n_iter=n_iter))
+    def submit_cgls(self, obj, sgm, x0, n_iter, out_path=None):
+        """n_iter CGLS iterations (Tikhonov-TV with unit weights) from x0 (host arrays,
+        CUDA tensors or file paths as for submit_fbp; a volume file is raw float32
+        [z, y, x])."""
+        sgm = self._load(sgm, lambda p: read_sinogram_file(obj, p))
+        x0 = self._load(x0, lambda p: np.fromfile(p, dtype=np.float32).reshape(obj.img_dim_z, obj.img_dim,
+                                                                             obj.img_dim))
+        return self._submit(_Request("cgls", obj, sgm, x0=x0, n_iter=n_iter, out_path=out_path))
 
     def close(self, wait=True):
         with self.cv:
@@ -214,6 +253,7 @@ class ReconServer:
             self._thread.join()
             for t in self._workers:
                 t.join()
+        self._io.shutdown(wait=wait)  # pending result writes finish first when waiting
 
     def stats(self):
         """Latency (arrival to result), its queueing and service parts, throughput."""
@@ -235,6 +275,27 @@ class ReconServer:
                 "evictions": self.evictions, "hbm_used_gb": self.used / 1e9}
 
     # ------------------------------------------------------------ internals
+    def _load(self, a, reader):
+        """A path becomes a future of its contents, read on an I/O thread; the scheduler
+        is woken when the read ends."""
+        if not _is_path(a):
+            return a
+        fut = self._io.submit(reader, os.fspath(a))
+        fut.add_done_callback(self._wake)
+        return fut
+
+    def _wake(self, _fut=None):
+        with self.cv:
+            self.cv.notify_all()
+
+    def _write_result(self, r, out):
+        try:
+            imwriteRaw(out.cpu().numpy() if isinstance(out, torch.Tensor) else out, os.fspath(r.out_path),
+                       dtype=np.float32)
+            r.future.set_result(out)
+        except Exception as e:  # noqa: BLE001 - handed to the caller through the future
+            r.future.set_exception(e)
+
     def _submit(self, req):
         with self.cv:
             if self.closed:
@@ -286,6 +347,13 @@ class ReconServer:
         """Start the oldest pending request's class if a slot is free or can be
         created within the budget; returns True if something started."""
         for i, head in enumerate(self.pending):
+            err = _input_error(head)
+            if err is not None:  # its input file could not be read: fail this request only
+                head.future.set_exception(err)
+                self.pending.pop(i)
+                return True
+            if not _inputs_ready(head):
+                continue
             key = head.key
             free = self.free_slots.setdefault(key, [])
             slot = free.pop() if free else None
@@ -309,7 +377,8 @@ class ReconServer:
                     return True
                 self.used += slot.nbytes
                 self.all_slots[key] = self.all_slots.get(key, 0) + 1
-            group = [r for r in self.pending if r.key == key][:slot.batch]
+            group = [r for r in self.pending if r.key == key and _inputs_ready(r) and _input_error(r) is None]
+            group = group[:slot.batch]
             for r in group:
                 self.pending.remove(r)
                 r.t_start = time.perf_counter()
@@ -339,6 +408,8 @@ class ReconServer:
         outs, err = None, None
         try:
             torch.cuda.set_device(self.device)
+            for r in group:
+                _resolve_inputs(r)
             outs = slot.run(group)
             now = time.perf_counter()
             for r in group:
@@ -355,6 +426,12 @@ class ReconServer:
             self.cv.notify_all()
         for i, r in enumerate(group):
             if outs is not None:
-                r.future.set_result(outs[i])
+                if r.out_path is not None:
+                    try:
+                        self._io.submit(self._write_result, r, outs[i])
+                    except RuntimeError:  # I/O threads already shut down (close without waiting)
+                        self._write_result(r, outs[i])
+                else:
+                    r.future.set_result(outs[i])
             elif not r.future.done():
                 r.future.set_exception(err)

@@ -95,3 +95,41 @@ def test_idle_slots_are_evicted_under_budget_pressure(cuda):
     assert st["evictions"] >= 3
     for i, out in enumerate(outs):
         assert np.array_equal(out, ref[i % 2])
+
+
+def test_file_inputs_and_outputs(tmp_path, cuda):
+    """Paths as inputs (read on the server's I/O threads, admitted once in memory) and
+    out_path (written after the slot is released): same results as array inputs; a
+    missing input file fails its own request only."""
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(5)
+    o = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60)
+    cg = _cgls_obj(n=24, nz=8, nu=48, nv=12, views=30, DetectorElementHeight=1.0)
+    sg = [rng.uniform(0, 1, (24, 60, 72)).astype(np.float32) for _ in range(3)]
+    sgm_cg = rng.uniform(0, 0.5, (12, 30, 48)).astype(np.float32)
+    x0 = rng.uniform(0, 0.01, (8, 24, 24)).astype(np.float32)
+    paths = []
+    for i, s in enumerate(sg):
+        paths.append(tmp_path / f"sgm_{i}.raw")
+        s.tofile(paths[-1])
+    sgm_cg.tofile(tmp_path / "cg_sgm.raw")
+    x0.tofile(tmp_path / "cg_x0.raw")
+
+    srv = ReconServer(batch=2)
+    want = [srv.submit_fbp(o, s).result(timeout=120) for s in sg]
+    want_cg = srv.submit_cgls(cg, sgm_cg, x0, 3).result(timeout=120)
+    futs = [srv.submit_fbp(o, p, out_path=tmp_path / f"rec_{i}.raw") for i, p in enumerate(paths)]
+    bad = srv.submit_fbp(o, tmp_path / "missing.raw")
+    fut_cg = srv.submit_cgls(cg, str(tmp_path / "cg_sgm.raw"), tmp_path / "cg_x0.raw", 3,
+                             out_path=tmp_path / "cg_out.raw")
+    got = [f.result(timeout=120) for f in futs]
+    got_cg = fut_cg.result(timeout=120)
+    with pytest.raises(FileNotFoundError):
+        bad.result(timeout=60)
+    srv.close()
+    for i in range(3):
+        assert np.array_equal(got[i], want[i])
+        assert np.array_equal(np.fromfile(tmp_path / f"rec_{i}.raw", dtype=np.float32).reshape(want[i].shape),
+                              want[i])
+    assert np.allclose(got_cg, want_cg, rtol=1e-6, atol=1e-7)
+    assert np.array_equal(np.fromfile(tmp_path / "cg_out.raw", dtype=np.float32).reshape(got_cg.shape), got_cg)
