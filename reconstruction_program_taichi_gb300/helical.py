@@ -29,6 +29,7 @@ from . import _lib, ops
 from ._lib import MCT_F32, Helical, Tables
 from .config import PI, ConfigError, ReadConfigFile
 from .fbp import Mgfbp, FdkPipeline
+from .file_pipeline import run_over_files
 from .geometry import fbp_geometry, gaussian_taps
 from .io import imwriteTiff
 
@@ -100,14 +101,16 @@ class Mgfbp_helical(Mgfbp):  # noqa: N801 - reference name
             raise ConfigError("ERROR: helical rebinning needs the full detector (no vertical recon range)!")
         self.file_processed_count = 0
         os.makedirs(os.path.join(self.input_dir, "temp"), exist_ok=True)
-        for file in os.listdir(self.input_dir):
-            if re.match(self.input_files_pattern, file):
-                if self.ReadSinogram(file):
-                    self.file_processed_count += 1
-                    self._log("\nReconstructing %s ..." % self.input_path)
-                    self.img_recon = self.reconstruct(self._device_sinogram()).cpu().numpy()
-                    self._log("\nSaving to %s !" % self.output_path)
-                    self.SaveReconImg()
+
+        def compute(d):
+            d.file_processed_count += 1
+            d._log("\nReconstructing %s ..." % d.input_path)
+            d.img_recon = d.reconstruct(d._device_sinogram()).cpu().numpy()
+            d._log("\nSaving to %s !" % d.output_path)
+
+        # the next file is read and the previous one written while this one runs
+        files = [f for f in os.listdir(self.input_dir) if re.match(self.input_files_pattern, f)]
+        run_over_files(self, files, lambda d, f: d.ReadSinogram(f), compute, lambda d: d.SaveReconImg())
         return self.img_recon
 
     def _device_sinogram(self):
