@@ -61,13 +61,16 @@ def _ray_dirs(u_arr, v_arr, rows, sid, sdd, curved, zpv, view_idx):
 
 def march(vol, view_idx, angles, u_arr, v_arr, *, nx, nz, px, pz, cx, cy, cz_view, sid, sdd,
           step, cone_beam, curved=False, zpv=0.0, rows=None, K=None, mask=None,
-          pmat_A=None, pmat_xs=None, mode="fp"):
+          pmat_A=None, pmat_xs=None, mode="fp", ray_values=None, out=None):
     """One view of the ray-driven projector over rows x cols rays.
 
-    mode 'fp'  : trilinear Riemann sum (run_mgfpj_v3.py:283-363); rays with
-                 mask == 0 give 0 (IRN_CGLS.py:567).
-    mode 'emap': effective-map value (IRN_CGLS.py:750, 824-833).
-    Returns [rows, cols].
+    mode 'fp'     : trilinear Riemann sum (run_mgfpj_v3.py:283-363); rays with
+                    mask == 0 give 0 (IRN_CGLS.py:567).  Returns [rows, cols].
+    mode 'emap'   : effective-map value (IRN_CGLS.py:750, 824-833).  Returns [rows, cols].
+    mode 'adjoint': the exact transpose of 'fp' (no reference counterpart): every sample
+                    that 'fp' sums adds ray_values[row, col] x its trilinear weights x
+                    the step length to the volume `out` [nz, nx, nx] (float64, in place;
+                    rays with mask != 1 add nothing).  Returns out.
     """
     nu = len(u_arr)
     rows = len(v_arr) if rows is None else rows
@@ -93,6 +96,10 @@ def march(vol, view_idx, angles, u_arr, v_arr, *, nx, nz, px, pz, cx, cy, cz_vie
     acc = np.zeros((rows, nu), dtype=np.float64)
     emap = np.ones((rows, nu), dtype=np.float64)
     V = None if vol is None else np.asarray(vol, dtype=np.float64)
+    if mode == "adjoint":
+        Y = np.asarray(ray_values, dtype=np.float64)[:rows]
+        if mask is not None:
+            Y = np.where(np.asarray(mask)[:rows] == 1, Y, 0.0)
     rowz = np.broadcast_to(np.arange(rows)[:, None], (rows, nu))
     for k in range(K):
         lk = k * step * vd + l_min
@@ -125,6 +132,23 @@ def march(vol, view_idx, angles, u_arr, v_arr, *, nx, nz, px, pz, cx, cy, cz_vie
         yw = (yr - (yi * (-px) + y0)) / (-px)
         xa = np.clip(xi, 0, nx - 2).astype(np.int64)
         ya = np.clip(yi, 0, nx - 2).astype(np.int64)
+        if mode == "adjoint":
+            if cone_beam:
+                zi = np.floor((zr - z0) / pz)
+                okz = ok & (zi >= 0) & (zi + 1 < nz)
+                za = np.clip(zi, 0, nz - 2).astype(np.int64)
+                zw = (zr - (zi * pz + z0)) / pz
+            else:
+                okz, za, zw = ok, rowz, np.zeros_like(xw)
+            w = np.where(okz, Y * step * vd, 0.0)
+            for dz in ((0, 1) if cone_beam else (0,)):
+                wz = zw if dz else 1.0 - zw
+                for dy in (0, 1):
+                    wy = yw if dy else 1.0 - yw
+                    for dx in (0, 1):
+                        wx = xw if dx else 1.0 - xw
+                        np.add.at(out, (za + dz, ya + dy, xa + dx), w * wz * wy * wx)
+            continue
         if cone_beam:
             zi = np.floor((zr - z0) / pz)
             okz = ok & (zi >= 0) & (zi + 1 < nz)
@@ -143,6 +167,8 @@ def march(vol, view_idx, angles, u_arr, v_arr, *, nx, nz, px, pz, cx, cy, cz_vie
             acc += np.where(ok, val * step * vd, 0.0)
     if mode == "emap":
         return emap
+    if mode == "adjoint":
+        return out
     if mask is not None:
         acc = np.where(np.asarray(mask)[:rows] == 1, acc, 0.0)
     return acc
