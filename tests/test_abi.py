@@ -74,9 +74,11 @@ def test_entry_points_reject_bad_arguments_before_any_launch():
         # float32 cone-beam cell copies are read with 32-byte loads
         ("mct_fp", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, ctypes.c_void_p(4112), None),
          "32-byte"),
-        # the cell-space adjoint reduces 16 bytes at a time
+        # the cell-space adjoint reduces 16 bytes at a time, into a workspace it needs
         ("mct_fp_adjoint_cells", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE,
                                   ctypes.c_void_p(4104), None), "16-byte"),
+        ("mct_fp_adjoint_cells", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, None, None),
+         "NULL buffer"),
         # 16-bit forward projection needs a workspace
         ("mct_fp_storage", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, None, 1, None),
          "workspace"),
