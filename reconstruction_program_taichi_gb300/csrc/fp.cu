@@ -169,29 +169,26 @@ __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const f
 // One thread per ray (u, v) of view j = blockIdx.y.  vol is [z][y][x]; vol_t, when
 // given, is the same volume as [z][x][y]: views whose detector columns spread along
 // y read vol_t so that the 32 rays of a warp touch consecutive addresses.  With ZP
-// (cone beam, workspace given) the volume is read from cell copies zp_x ([z][y][x])
-// and zp_y ([z][x][y]) whose element (z, y, x) holds the whole 2x2x2 trilinear cell
-// at voxel (z, y, x) (float32 below, bf16 / float16 further down): a cell reload is
-// one gather.
+// (cone beam, workspace given) the volume is read from copies zp_x ([z][y][x]) and
+// zp_y ([z][x][y]): float32 quads (two adjacent 16-byte elements per cell reload) or
+// 16-bit cells (the whole 2x2x2 trilinear cell in one 16-byte element), below.
 
-// float32 cell copy: element (z, y, x) of either orientation holds the 2x2x2 cell whose
-// lowest corner is voxel (z, y, x) as the four z-pairs the interpolation consumes,
-//   {e00, g00, e10, g10} = {V[z..z+1][y][x],  V[z..z+1][y][x+1] - V[z..z+1][y][x],
-//                           V[z..z+1][y+1][x], V[z..z+1][y+1][x+1] - V[z..z+1][y+1][x]},
-// 32 bytes, read with one 256-bit load.  Against four 8-byte z-pair gathers per reload
-// (neighbouring rays about a voxel apart, so each gather of a warp spans ~2.6 L1
-// lines) this touches each line once: L1 wavefronts fell from 86 to 48-64 % of peak,
-// at the price of L1 hits (10 % instead of 89 %: consecutive cells of a ray no longer
-// share lines), and the projector at 512x512x256 / 1080 views went 349 -> 298 ms.
-// The differences are the ones the kernel would compute from the volume.
-struct __align__(32) Cell32 {
-    float v[8];
+// float32 quad copy, indexed in a (slow s, fast f) frame: (s, f) = (y, x) for views whose
+// detector columns spread along x (copy cx, [z][y][x]) and (x, y) for the others (copy
+// cy, [z][x][y]), so that the 32 rays of a warp read neighbouring elements.  Element
+// (z, s, f) holds the z-pairs of the voxel and of its neighbour along s,
+//   {V(z, s, f), V(z+1, s, f), V(z, s+1, f), V(z+1, s+1, f)}    (16 bytes),
+// and the neighbour along f is the next element: a cell reload is two adjacent 16-byte
+// loads, and the f-differences are taken in registers (the same float32 subtraction a
+// direct read would do).  Against a 32-byte element holding the whole cell (differences
+// included) this halves the copies (32 instead of 64 bytes per voxel for both
+// orientations), so twice the cells fit L1 and L2; with blocks of 8 consecutive views,
+// whose rays cross nearly the same cells at the same step, the projector at
+// 512x512x256 / 1080 views went 297.6 -> 267.3 ms (the 32-byte cells: 304-312 ms with
+// 2-8 views per block, 297.6 with 8 rows of one view).
+struct __align__(16) Quad16 {
+    float v[4];
 };
-__device__ __forceinline__ void ld_cell32(const Cell32* p, float2& e00, float2& g00, float2& e10, float2& g10) {
-    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(e00.x), "=f"(e00.y), "=f"(g00.x), "=f"(g00.y), "=f"(e10.x), "=f"(e10.y), "=f"(g10.x), "=f"(g10.y)
-        : "l"(p));
-}
 
 // bf16 cell copy: element (z, y, x) of either orientation holds the whole 2x2x2 cell
 // whose lowest corner is voxel (z, y, x), as four bf16 pairs {lower, upper z-plane}:
@@ -205,9 +202,10 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 }
 
 // Resident blocks per SM that the register allocation of fp_kernel targets.  The
-// float32 cone-beam path waits on L2 and needs its warps: 5 blocks (48 registers) take
-// 297 ms at 512x512x256 / 1080 views, 4 blocks 321 ms, 3 blocks (71 registers) 400 ms;
-// the fan-beam path keeps 40 registers (6 blocks).  The 16-bit paths are issue-bound
+// float32 cone-beam path waits on L2 and needs its warps: with quad copies and 8 views
+// per block, 5 blocks (48 registers) take 267.3 ms at 512x512x256 / 1080 views, 4
+// blocks 273.8 ms, 6 blocks (40 registers, spilling) 317.1 ms; the fan-beam path keeps
+// 40 registers (6 blocks).  The 16-bit paths are issue-bound
 // and gain from registers: 1 (80 registers, 3 blocks of 256) gives bf16 237.4 ms
 // against 254.9 with 5 blocks, float16 274.4 against 291.7.
 template <bool CONE, typename ZT>
@@ -236,13 +234,25 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
     }
     const int nx = p.nx;
     const bool tr = (ZP || vol_t != nullptr) && spread_along_y(p, j, angles, pa);
+    // quad copies are addressed in their (slow, fast) frame: the ray's x and y swap for
+    // the transposed copy, so the fast axis is always "x" below (both axes span
+    // [0, nx - 1), so the clipping and inside tests are unchanged)
+    constexpr bool kQuad = ZP && std::is_same<ZT, Quad16>::value;
     const float* __restrict__ V = tr ? vol_t : vol;
     const ZT* __restrict__ V2 = tr ? zp_y : zp_x;
-    const int sx = tr ? nx : 1, sy = tr ? 1 : nx;
+    const int sx = (tr && !kQuad) ? nx : 1, sy = (tr && !kQuad) ? 1 : nx;
     const int plane = nx * nx;  // volumes below 2^31 voxels (checked on the host)
     Ray r;
     float acc = 0.0f;
     if (setup_ray(p, iu, iv, j, angles, u_arr, v_arr, czv, pa, pxs, true, r)) {
+        if (kQuad && tr) {
+            float t = r.fx0;
+            r.fx0 = r.fy0;
+            r.fy0 = t;
+            t = r.dfx;
+            r.dfx = r.dfy;
+            r.dfy = t;
+        }
         const float xmax = (float)(nx - 1), zmax = (float)(p.nz - 1);
         // Consecutive samples are 0.2 voxel diagonals apart, so most fall in the same
         // 2x2x2 cell as the previous one: the cell stays in registers (as corner values
@@ -253,8 +263,13 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         auto load_cell = [&](int off) {
             if (off == cell) return;
             cell = off;
-            if constexpr (ZP && std::is_same<ZT, Cell32>::value) {
-                ld_cell32(V2 + off, e00, g00, e10, g10);
+            if constexpr (kQuad) {
+                const float4 q0 = __ldg(reinterpret_cast<const float4*>(V2 + off));
+                const float4 q1 = __ldg(reinterpret_cast<const float4*>(V2 + off + 1));
+                e00 = make_float2(q0.x, q0.y);
+                e10 = make_float2(q0.z, q0.w);
+                g00 = __fadd2_rn(make_float2(q1.x, q1.y), make_float2(-q0.x, -q0.y));
+                g10 = __fadd2_rn(make_float2(q1.z, q1.w), make_float2(-q0.z, -q0.w));
             } else if constexpr (ZP && std::is_same<ZT, uint4>::value) {
                 const uint4 q = __ldg(V2 + off);
                 e00 = bf16x2_to_float2(q.x);
@@ -322,10 +337,10 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
             if (check) acc += ok ? val : 0.0f;
             else acc += val;
         };
-        // Interior samples (at least 1e-3 voxel inside on every axis).  With 16-bit
-        // cells the floors come from the 1.5 * 2^23 rounding constant, on the FMA pipe
-        // instead of the conversion unit (which then limits the kernel); the float32
-        // path is bound by L1 wavefronts, where the plain floors measure faster.
+        // Interior samples (at least 1e-3 voxel inside on every axis).  With copies
+        // the floors come from the 1.5 * 2^23 rounding constant, on the FMA pipe
+        // instead of the conversion unit (which otherwise limits the 16-bit kernels
+        // and costs the float32 one 5 ms at 512x512x256 / 1080 views).
         // Round-to-nearest of f - 0.5 is floor(f), or floor(f) - 1 at an exact integer
         // f, where the interpolant has the same value from either cell (weight 1 in the
         // lower one); both cells lie inside the volume.  The element offset is summed in
@@ -415,12 +430,14 @@ __global__ void cell16_kernel(int nx, int nz, const float* __restrict__ v, uint4
     }
 }
 
-// float32 cell copies (layout at Cell32): cx[z][y][x] and cy[z][x][y] both hold the
-// cell at voxel (z, y, x); corners outside the volume are 0 (no in-volume sample uses
-// them).  32x32 tiles, the transposed copy through shared memory.
-__global__ void cell32_kernel(int nx, int nz, const float* __restrict__ v, Cell32* __restrict__ cx,
-                              Cell32* __restrict__ cy) {
-    __shared__ Cell32 tile[32][33];
+// float32 quad copies (layout at Quad16): cx[z][y][x] = {V[z][y][x], V[z+1][y][x],
+// V[z][y+1][x], V[z+1][y+1][x]} (fast axis x) and cy[z][x][y] = {V[z][y][x],
+// V[z+1][y][x], V[z][y][x+1], V[z+1][y][x+1]} (fast axis y); corners outside the volume
+// are 0 (no in-volume sample uses them).  32x32 tiles, the transposed copy through
+// shared memory.
+__global__ void quad32_kernel(int nx, int nz, const float* __restrict__ v, float4* __restrict__ cx,
+                              float4* __restrict__ cy) {
+    __shared__ float4 tile[32][33];
     const int64_t plane = (int64_t)nx * nx;
     const int z = blockIdx.z;
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
@@ -431,18 +448,8 @@ __global__ void cell32_kernel(int nx, int nz, const float* __restrict__ v, Cell3
         const int y = y0 + i, x = x0 + threadIdx.x;
         if (y < nx && x < nx) {
             const float a0 = at(z, y, x), a1 = at(z + 1, y, x);
-            const float c0 = at(z, y + 1, x), c1 = at(z + 1, y + 1, x);
-            Cell32 q;
-            q.v[0] = a0;
-            q.v[1] = a1;
-            q.v[2] = at(z, y, x + 1) - a0;
-            q.v[3] = at(z + 1, y, x + 1) - a1;
-            q.v[4] = c0;
-            q.v[5] = c1;
-            q.v[6] = at(z, y + 1, x + 1) - c0;
-            q.v[7] = at(z + 1, y + 1, x + 1) - c1;
-            cx[z * plane + (int64_t)y * nx + x] = q;
-            tile[i][threadIdx.x] = q;
+            cx[z * plane + (int64_t)y * nx + x] = make_float4(a0, a1, at(z, y + 1, x), at(z + 1, y + 1, x));
+            tile[i][threadIdx.x] = make_float4(a0, a1, at(z, y, x + 1), at(z + 1, y, x + 1));
         }
     }
     __syncthreads();
@@ -774,9 +781,9 @@ extern "C" {
 size_t mct_fp_workspace_size(const mct_geom* g) {
     if (!g || g->nx < 1 || g->nz < 1) return 0;
     const size_t n = (size_t)g->nz * g->nx * g->nx;
-    // cone beam: two float32 cell copies (32 bytes per voxel each); fan beam: one
+    // cone beam: two float32 quad copies (16 bytes per voxel each); fan beam: one
     // transposed copy
-    return (g->flags & MCT_CONE) ? 2 * n * sizeof(Cell32) : n * sizeof(float);
+    return (g->flags & MCT_CONE) ? 2 * n * sizeof(Quad16) : n * sizeof(float);
 }
 
 size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype) {
@@ -799,11 +806,22 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
                 "mct_fp: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
     MCT_REQUIRE(dtype == MCT_F32 || (p.cone && workspace), "mct_fp: 16-bit storage needs cone beam and a workspace");
     cudaStream_t s = as_stream(stream);
+    if (g->nx < 2 || (p.cone && g->nz < 2)) {
+        // no trilinear stencil fits inside the volume: every ray sums nothing, as in the
+        // reference (its inside test fails for every sample)
+        cudaError_t e = cudaMemsetAsync(sgm, 0, (size_t)sgm_elems(*g) * sizeof(float), s);
+        if (e != cudaSuccess) {
+            set_error("mct_fp: %s", cudaGetErrorString(e));
+            return MCT_E_CUDA;
+        }
+        return MCT_OK;
+    }
     dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
-    // Blocks of 8 detector rows of one view for float32 cells; 4 views x 2 rows for
-    // 16-bit cells (bf16 at 512x512x256 / 1080 views: 254.8 ms against 261.4; float32:
-    // 297.5 ms against 304-312 with 2, 4 or 8 views per block).
-    p.vshift = (p.cone && workspace && dtype != MCT_F32) ? 2 : 0;
+    // Blocks of 8 consecutive views x 1 detector row for float32 quad copies (at
+    // 512x512x256 / 1080 views: 267.3 ms; 4 views x 2 rows 276.9, 2 x 4 293.8, 1 x 8
+    // 306.5); 4 views x 2 rows for 16-bit cells (bf16 254.8 ms against 261.4 with 1 x 8);
+    // 8 rows of one view without copies.
+    p.vshift = (p.cone && workspace) ? (dtype == MCT_F32 ? 3 : 2) : 0;
     const int vb = 1 << p.vshift, rb = 8 >> p.vshift;
     dim3 block(32, 8), grid((g->nu + 31) / 32, (g->views + vb - 1) / vb, (g->nv + rb - 1) / rb);
     const size_t n = (size_t)g->nz * g->nx * g->nx;
@@ -832,12 +850,11 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
                                                             nullptr, reinterpret_cast<const h16x8*>(cx),
                                                             reinterpret_cast<const h16x8*>(cy), mask, sgm, vmax);
     } else if (p.cone && workspace) {
-        MCT_REQUIRE(((uintptr_t)workspace & 31) == 0, "mct_fp: workspace must be 32-byte aligned");
-        Cell32* cx = static_cast<Cell32*>(workspace);
-        Cell32* cy = cx + n;
-        cell32_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy);
-        MCT_TRY(launched("cell32_kernel"));
-        fp_kernel<true, true, Cell32><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
+        Quad16* cx = static_cast<Quad16*>(workspace);
+        Quad16* cy = cx + n;
+        quad32_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, reinterpret_cast<float4*>(cx), reinterpret_cast<float4*>(cy));
+        MCT_TRY(launched("quad32_kernel"));
+        fp_kernel<true, true, Quad16><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
                                                              vol, nullptr, cx, cy, mask, sgm, nullptr);
     } else {
         float* vt = static_cast<float*>(workspace);

@@ -71,9 +71,9 @@ def test_entry_points_reject_bad_arguments_before_any_launch():
                     None, FAKE, None, None), "view-chunked"),
         # packed operand must be 16-byte aligned
         ("mct_pack", (ctypes.byref(_valid_geom()), FAKE, ctypes.c_void_p(4100), 0, None), "aligned"),
-        # float32 cone-beam cell copies are read with 32-byte loads
-        ("mct_fp", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, ctypes.c_void_p(4112), None),
-         "32-byte"),
+        # the cone-beam gather copies are read with 16-byte loads
+        ("mct_fp", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE, ctypes.c_void_p(4104), None),
+         "16-byte"),
         # the cell-space adjoint reduces 16 bytes at a time, into a workspace it needs
         ("mct_fp_adjoint_cells", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, None, FAKE,
                                   ctypes.c_void_p(4104), None), "16-byte"),
@@ -104,7 +104,7 @@ def test_entry_points_reject_bad_arguments_before_any_launch():
 def test_packed_and_workspace_sizes():
     """Sizes the host allocates from: coefficient operand nv rows (incl. the NaN row)
     x (nu-1) columns per view, 16 B float32 / 8 B 16-bit (+16 for the float16 scale);
-    FP cells 64 B per voxel in float32, 32 B in 16 bits (both orientations); the fan
+    FP copies 32 B per voxel in float32 (quads) and in 16 bits (cells), both orientations; the fan
     beam's transposed copy 4 B per voxel."""
     lib = _lib.load()
     g = _valid_geom()
@@ -117,8 +117,8 @@ def test_packed_and_workspace_sizes():
     assert lib.mct_fp_storage_workspace_size(ctypes.byref(g), 1) == 2 * 32 * 32 * 8 * 16
     assert lib.mct_fp_storage_workspace_size(ctypes.byref(g), 2) == 2 * 32 * 32 * 8 * 16 + 16
     assert lib.mct_fp_storage_workspace_size(ctypes.byref(fan), 1) == 0
-    assert lib.mct_fp_workspace_size(ctypes.byref(g)) == 2 * 32 * 32 * 8 * 32
-    assert lib.mct_fp_storage_workspace_size(ctypes.byref(g), 0) == 2 * 32 * 32 * 8 * 32
+    assert lib.mct_fp_workspace_size(ctypes.byref(g)) == 2 * 32 * 32 * 8 * 16
+    assert lib.mct_fp_storage_workspace_size(ctypes.byref(g), 0) == 2 * 32 * 32 * 8 * 16
     assert lib.mct_fp_workspace_size(ctypes.byref(fan)) == 32 * 32 * 16 * 4
     assert lib.mct_fp_adjoint_workspace_size(ctypes.byref(g)) == 32 * 32 * 8 * 32
     assert lib.mct_fp_adjoint_workspace_size(ctypes.byref(fan)) == 32 * 32 * 16 * 16
