@@ -6,14 +6,19 @@ No counterpart in the reference (it reconstructs one config at a time).
 Model
   * A request is an FBP/FDK reconstruction or an N-iteration CGLS solve of one
     sinogram for one geometry (a parsed config).
-  * Requests of the same geometry and kind share a *slot class*.  A slot owns
-    device buffers for up to `batch` requests, a CUDA stream, and a CUDA graph of
-    the whole batch captured once (weight -> filter -> pack -> backproject for each
-    sinogram, or the full CGLS loop), so a batch executes as one graph launch.
+  * Requests of the same kind, storage precision (and CGLS iteration count) whose
+    parsed configs agree in every attribute that can change the result (a digest of
+    the whole parsed config, file names aside) share a *slot class*.  A slot owns
+    device buffers for up to `batch` requests, a CUDA stream, and CUDA graphs captured
+    once per occupancy (weight -> filter -> pack -> backproject for each sinogram, or
+    the full CGLS loop for each request), so a batch of k requests executes as one
+    graph launch that runs exactly k reconstructions.
   * Admission is continuous: a scheduler thread takes pending requests in arrival
     order, groups those whose slot class matches (up to `batch`), and starts them on
     a free slot; new slots are created while the HBM budget allows, and a slot is
-    reused as soon as its previous batch finishes.  Batches on different slots run
+    reused as soon as its previous batch finishes.  A new slot is built by the worker
+    thread of its first batch, outside the scheduler's lock (one slot at a time, since a
+    graph capture cannot overlap another thread's).  Batches on different slots run
     concurrently on their own streams.
   * Slots are kept for reuse; when a request needs a new slot and the budget is
     spent, idle slots of other classes are evicted, least recently used first.
@@ -29,7 +34,6 @@ Model
     graph always runs the same kernels on the same buffer layout.
 """
 import os
-import queue
 import threading
 import time
 from concurrent.futures import Future, ThreadPoolExecutor
@@ -41,18 +45,59 @@ from . import ops
 from .fbp import FdkPipeline
 from .io import imwriteRaw, read_sinogram_file
 
-_SENTINEL = object()
+# Parsed-config attributes that only name files or control logging: they do not
+# change what a slot computes, so requests that differ only in them share a slot.
+_IO_ONLY = frozenset({
+    "config_dict", "input_dir", "output_dir", "input_files_pattern", "output_file_prefix",
+    "output_file_replace", "output_file_format", "input_file_form", "save_filtered_sinogram",
+    "verbose", "input_path", "output_path", "output_file", "img_sgm", "img_recon", "img_x",
+    "file_processed_count", "num_iter_runned", "loss", "prior_image_file", "img_prior",
+})
+
+
+def _digest_value(h, v):
+    if isinstance(v, np.ndarray):
+        a = np.ascontiguousarray(v)
+        h.update(f"nd{a.dtype.str}{a.shape}".encode())
+        h.update(a.tobytes())
+    elif isinstance(v, (list, tuple)):
+        h.update(f"seq{len(v)}[".encode())
+        for x in v:
+            _digest_value(h, x)
+        h.update(b"]")
+    elif isinstance(v, dict):
+        h.update(f"map{len(v)}{{".encode())
+        for k in sorted(v, key=repr):
+            h.update(repr(k).encode())
+            _digest_value(h, v[k])
+        h.update(b"}")
+    else:  # scalars (float repr is exact), strings, None
+        h.update(f"{type(v).__name__}:{v!r};".encode())
+
+
+def config_digest(obj):
+    """Digest of every parsed-config attribute that can change a reconstruction:
+    every attribute of the parsed object except the file-naming and logging ones
+    (_IO_ONLY) and private caches; arrays (angles, projection matrices, beam-hardening
+    coefficients, per-view centres) by their bytes.  Two configs with the same digest
+    produce the same result from the same sinogram."""
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(vars(obj)):
+        if k.startswith("_") or k in _IO_ONLY:
+            continue
+        v = getattr(obj, k)
+        if callable(v):
+            continue
+        h.update(k.encode() + b"=")
+        _digest_value(h, v)
+    return h.hexdigest()
 
 
 def _geom_key(obj, kind, extra=()):
-    g = (obj.det_elem_count_horizontal, obj.det_elem_count_vertical_actual, obj.view_num, obj.img_dim,
-         obj.img_dim_z, float(obj.det_elem_width), float(obj.det_elem_height), float(obj.img_pix_size),
-         float(obj.img_voxel_height), float(obj.source_isocenter_dis), float(obj.source_det_dis),
-         float(obj.total_scan_angle), float(obj.img_rot), bool(obj.cone_beam), bool(obj.curved_dect),
-         str(obj.kernel_name), float(obj.kernel_param), float(obj.det_offset_horizontal),
-         float(getattr(obj, "det_offset_vertical", 0.0)), float(obj.img_center_x), float(obj.img_center_y),
-         float(obj.img_center_z), int(obj.recon_view_mode))
-    return (kind,) + g + tuple(extra)
+    """Slot class of a request: its kind, the digest of its parsed config and the
+    per-request options (storage, iteration count)."""
+    return (kind, config_digest(obj)) + tuple(extra)
 
 
 def _is_path(a):
@@ -102,44 +147,58 @@ class _Request:
         self.on_device = isinstance(sgm, torch.Tensor) and sgm.is_cuda
 
 
+_IR_STORAGE = {"f32": "float32", "bf16": "bfloat16", "f16": "float16"}
+
+
+def _graph_capture(stream, body, pool):
+    """Warm body() on stream (first-call set-up and cached buffers outside the
+    capture), then capture it into a CUDA graph drawing on the shared memory pool."""
+    with torch.cuda.stream(stream):
+        body()
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    # thread-local capture: other slots keep running on their own threads and streams
+    with torch.cuda.graph(g, pool=pool, stream=stream, capture_error_mode="thread_local"):
+        body()
+    return g
+
+
 class _FbpSlot:
-    """Static buffers and one captured graph for `batch` FBP reconstructions."""
+    """Static buffers for `batch` FBP reconstructions of one slot class and one
+    captured graph per occupancy: a batch of k requests replays the graph of its first
+    k members only, so no member recomputes a stale input.  The graphs share one memory
+    pool (a slot runs one batch at a time).  The mixed-precision path (16-bit storage)
+    uses the two-part tensor-core filter and 16-bit backprojection coefficients."""
 
     def __init__(self, obj, batch, storage, device, use_graph):
         self.device = device
         self.stream = torch.cuda.Stream(device=device)
         self.batch = batch
+        impl = "tc3" if storage == "f32" else "tc"
         with torch.cuda.stream(self.stream):
-            self.pipes = [FdkPipeline(obj, device=device, storage=storage) for _ in range(batch)]
+            self.pipes = [FdkPipeline(obj, device=device, storage=storage, filter_impl=impl) for _ in range(batch)]
             shape = self.pipes[0].dg.sgm_shape
             self.inp = [torch.zeros(shape, dtype=torch.float32, device=device) for _ in range(batch)]
             self.out = [torch.zeros(self.pipes[0].dg.vol_shape, dtype=torch.float32, device=device)
                         for _ in range(batch)]
         self.host_out = [torch.empty(self.pipes[0].dg.vol_shape, dtype=torch.float32, pin_memory=True)
                          for _ in range(batch)]
-        self.graph = None
+        self.graphs = {}
         self.last_used = time.perf_counter()
         self.nbytes = sum(p.weighted.numel() * 4 + p.filtered.numel() * 4 + p.packed.numel() + p.vol.numel() * 4
                           + (p.tc._buf.numel() if p.tc is not None else 0)
                           for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
-            self._capture()
+            pool = torch.cuda.graph_pool_handle()
+            for k in range(1, batch + 1):
+                self.graphs[k] = _graph_capture(self.stream, lambda k=k: self._body(k), pool)
 
-    def _body(self):
-        for p, i, o in zip(self.pipes, self.inp, self.out):
+    def _body(self, k):
+        for p, i, o in zip(self.pipes[:k], self.inp[:k], self.out[:k]):
             p.run(i, out=o)
 
-    def _capture(self):
-        with torch.cuda.stream(self.stream):
-            self._body()  # warm (first-call set-up outside the capture)
-        self.stream.synchronize()
-        g = torch.cuda.CUDAGraph()
-        # thread-local capture: other slots keep running on their own threads/streams
-        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-            self._body()
-        self.graph = g
-
     def run(self, reqs):
+        k = len(reqs)
         dev_out = []
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
@@ -147,10 +206,10 @@ class _FbpSlot:
                     self.inp[i].copy_(r.sgm)
                 else:
                     self.inp[i].copy_(torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)))
-            if self.graph is not None:
-                self.graph.replay()
+            if k in self.graphs:
+                self.graphs[k].replay()
             else:
-                self._body()
+                self._body(k)
             for i, r in enumerate(reqs):
                 if r.on_device:
                     dev_out.append(self.out[i].clone())
@@ -162,41 +221,70 @@ class _FbpSlot:
         return [d if d is not None else self.host_out[i].numpy().copy() for i, d in enumerate(dev_out)]
 
 
-def _fp_workspace_bytes(dg):
+def _fp_workspace_bytes(dg, dtype):
     from . import _lib
-    return int(_lib.load().mct_fp_storage_workspace_size(dg.g(), _lib.MCT_F32))
+    return int(_lib.load().mct_fp_storage_workspace_size(dg.g(), int(dtype)))
 
 
 class _CglsSlot:
-    """CGLS (reference operator pair, lambda*D^T D with unit weights) for one request."""
+    """n_iter CGLS iterations (reference operator pair, lambda * D^T D with unit
+    weights, as submit_cgls describes) for up to `batch` requests of one slot class.
+    The members share one IrSystem (geometry tables, effective ray map, projector
+    workspace, packed operand), which is safe because they run one after another on
+    the slot's stream; each member has static input and output buffers.  One graph is
+    captured per occupancy, so a batch of k requests is one graph launch of k solves."""
 
-    def __init__(self, obj, n_iter, device):
+    def __init__(self, obj, n_iter, storage, batch, device, use_graph):
         from .ir import IrSystem
+        self.device = device
         self.stream = torch.cuda.Stream(device=device)
-        self.batch = 1
-        with torch.cuda.stream(self.stream):
-            self.sys = IrSystem(obj, device)
+        self.batch = batch
         self.obj = obj
         self.n_iter = n_iter
+        self.lr = obj.coef_lambda * obj.pixel_count_ratio
+        with torch.cuda.stream(self.stream):
+            self.sys = IrSystem(obj, device, storage=_IR_STORAGE.get(storage, storage))
+            dg = self.sys.dg
+            f32 = dict(dtype=torch.float32, device=device)
+            self.sgm = [torch.zeros(dg.sgm_shape, **f32) for _ in range(batch)]
+            self.x0 = [torch.zeros(dg.vol_shape, **f32) for _ in range(batch)]
+            self.out = [torch.zeros(dg.vol_shape, **f32) for _ in range(batch)]
+            self.wr = torch.ones(dg.vol_shape, **f32)
         self.last_used = time.perf_counter()
-        nvol = obj.img_dim * obj.img_dim * obj.img_dim_z
-        # iterates and operator buffers, the projector's gather copies, sinogram buffers
-        self.nbytes = 4 * nvol * 4 + _fp_workspace_bytes(self.sys.dg) + 3 * self.sys.fp_buf.numel() * 4
+        nvol = 4 * obj.img_dim * obj.img_dim * obj.img_dim_z
+        nsgm = 4 * self.sys.fp_buf.numel()
+        # per member: sinogram, seed, result; shared: unit weights, map, projector
+        # buffer and workspace, packed operands (float32 and storage type), and the
+        # temporaries of one solve (masked sinogram, P^T b, d, r, x, q)
+        self.nbytes = (batch * (nsgm + 2 * nvol) + nvol + 2 * nsgm + _fp_workspace_bytes(dg, self.sys.fp_dtype)
+                       + 2 * 4 * nsgm + nsgm + 5 * nvol)
+        self.graphs = {}
+        if use_graph:
+            pool = torch.cuda.graph_pool_handle()
+            for k in range(1, batch + 1):
+                self.graphs[k] = _graph_capture(self.stream, lambda k=k: self._body(k), pool)
+
+    def _body(self, k):
+        sy = self.sys
+        for i in range(k):
+            sy.bpb = sy.bp_b(self.sgm[i])
+            x = sy.cgls(self.x0[i], [], [(self.lr, self.wr)], self.n_iter)
+            self.out[i].copy_(x)
 
     def run(self, reqs):
-        r = reqs[0]
-        obj = self.obj
+        k = len(reqs)
         with torch.cuda.stream(self.stream):
-            sgm = _to_device(r.sgm, self.sys.device)
-            x0 = _to_device(r.x0, self.sys.device)
-            self.sys.bpb = self.sys.bp_b(sgm)
-            wr = torch.ones_like(x0)
-            lr = obj.coef_lambda * obj.pixel_count_ratio
-            x = self.sys.cgls(x0, [], [(lr, wr)], self.n_iter)
-            out = x if r.on_device else x.cpu().numpy()
+            for i, r in enumerate(reqs):
+                self.sgm[i].copy_(_to_device(r.sgm, self.device))
+                self.x0[i].copy_(_to_device(r.x0, self.device))
+            if k in self.graphs:
+                self.graphs[k].replay()
+            else:
+                self._body(k)
+            outs = [self.out[i].clone() if r.on_device else self.out[i].cpu().numpy() for i, r in enumerate(reqs)]
         self.stream.synchronize()
         self.last_used = time.perf_counter()
-        return [out]
+        return outs
 
 
 class ReconServer:
@@ -216,13 +304,17 @@ class ReconServer:
         self.pending = []
         self.cv = threading.Condition()
         self.free_slots = {}    # key -> [slot]
-        self.all_slots = {}     # key -> count
+        self.all_slots = {}     # key -> count (built and being built)
         self.evictions = 0
         self.busy = 0
         self.done = []
         self.closed = False
         self.errors = []
         self._workers = []
+        # slot construction (buffers, warm-up, graph capture) runs on the workers,
+        # outside self.cv, one slot at a time: a capture begins with a device-wide
+        # synchronize, which is illegal while another thread is capturing
+        self._build_lock = threading.Lock()
         self._io = ThreadPoolExecutor(2, thread_name_prefix="mct-serve-io")
         self._thread = threading.Thread(target=self._schedule, daemon=True)
         self._thread.start()
@@ -232,18 +324,21 @@ class ReconServer:
         """FBP/FDK of a sinogram [rows, views, cols] (host array, CUDA tensor, or the path
         of an input file in the config's InputFileForm and detector row range) for the
         parsed config obj; the future's result is a host array or a new CUDA tensor.
-        out_path: also write the result there (raw float32)."""
+        storage: 'f32' (plain) or 'bf16' / 'f16' (mixed precision: two-part tensor-core
+        filter, 16-bit backprojection operand).  out_path: also write the result there
+        (raw float32)."""
         sgm = self._load(sgm, lambda p: read_sinogram_file(obj, p))
         return self._submit(_Request("fbp", obj, sgm, storage=storage, out_path=out_path))
 
-    def submit_cgls(self, obj, sgm, x0, n_iter, out_path=None):
+    def submit_cgls(self, obj, sgm, x0, n_iter, storage="f32", out_path=None):
         """n_iter CGLS iterations (Tikhonov-TV with unit weights) from x0 (host arrays,
         CUDA tensors or file paths as for submit_fbp; a volume file is raw float32
-        [z, y, x])."""
+        [z, y, x]).  storage: 'f32', or 'bf16' / 'f16' for 16-bit projector gathers
+        inside the iterations (the data term stays float32)."""
         sgm = self._load(sgm, lambda p: read_sinogram_file(obj, p))
         x0 = self._load(x0, lambda p: np.fromfile(p, dtype=np.float32).reshape(obj.img_dim_z, obj.img_dim,
                                                                              obj.img_dim))
-        return self._submit(_Request("cgls", obj, sgm, x0=x0, n_iter=n_iter, out_path=out_path))
+        return self._submit(_Request("cgls", obj, sgm, x0=x0, n_iter=n_iter, storage=storage, out_path=out_path))
 
     def close(self, wait=True):
         with self.cv:
@@ -306,9 +401,10 @@ class ReconServer:
 
     def _make_slot(self, req):
         torch.cuda.set_device(self.device)
-        if req.kind == "fbp":
-            return _FbpSlot(req.obj, self._batch_for(req), req.storage, self.device, self.use_graphs)
-        return _CglsSlot(req.obj, req.n_iter, self.device)
+        with self._build_lock:
+            if req.kind == "fbp":
+                return _FbpSlot(req.obj, self._batch_for(req), req.storage, self.device, self.use_graphs)
+            return _CglsSlot(req.obj, req.n_iter, req.storage, self._batch_for(req), self.device, self.use_graphs)
 
     @staticmethod
     def _per_request_bytes(req):
@@ -317,20 +413,32 @@ class ReconServer:
         nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
         if req.kind == "fbp":  # input, weighted, filtered, packed (4x), tensor-core operand tiles
             return nsgm * 8 + 2 * nvol
-        # CGLS: four iterates, the projector's gather copies (cone beam: two 32-byte cells
-        # per voxel), three sinogram buffers
-        return 4 * nvol + (16 if o.cone_beam else 1) * nvol + 3 * nsgm
+        # CGLS member: sinogram, seed, result
+        return nsgm + 2 * nvol
+
+    @staticmethod
+    def _shared_bytes(req):
+        """Bytes a slot holds whatever its batch (CGLS: the shared IrSystem and the
+        temporaries of one solve; FBP: none)."""
+        if req.kind == "fbp":
+            return 0
+        o = req.obj
+        nvol = o.img_dim * o.img_dim * o.img_dim_z * 4
+        nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
+        # unit weights, map, projector buffer, gather copies (cone beam, float32 quad
+        # copies: 8 floats per voxel), packed operands (2 x 4 per element), temporaries
+        return nvol + 2 * nsgm + (8 if o.cone_beam else 1) * nvol + 8 * nsgm + nsgm + 5 * nvol
 
     def _batch_for(self, req):
-        """Requests per FBP slot: `batch`, reduced so that one slot takes at most an
-        eighth of the budget (large geometries get small slots, so that several classes
-        stay resident)."""
-        if req.kind != "fbp":
-            return 1
-        return max(1, min(self.batch, int(self.budget / 8 // max(self._per_request_bytes(req), 1))))
+        """Requests per slot: `batch`, reduced so that one slot takes at most an eighth
+        of the budget (large geometries get small slots, so that several classes stay
+        resident)."""
+        per = max(self._per_request_bytes(req), 1)
+        room = self.budget / 8 - self._shared_bytes(req)
+        return max(1, min(self.batch, int(room // per)))
 
     def _estimate(self, req):
-        return self._batch_for(req) * self._per_request_bytes(req)
+        return self._shared_bytes(req) + self._batch_for(req) * self._per_request_bytes(req)
 
     def _schedule(self):
         while True:
@@ -344,8 +452,10 @@ class ReconServer:
                     self.cv.wait(timeout=0.05)
 
     def _try_start(self):
-        """Start the oldest pending request's class if a slot is free or can be
-        created within the budget; returns True if something started."""
+        """Start the oldest pending request's class on a free slot, or reserve the
+        budget for a new slot and hand its construction to the batch's worker (the
+        slot is built outside the lock); returns True if something started.  Called
+        with the lock held."""
         for i, head in enumerate(self.pending):
             err = _input_error(head)
             if err is not None:  # its input file could not be read: fail this request only
@@ -357,6 +467,7 @@ class ReconServer:
             key = head.key
             free = self.free_slots.setdefault(key, [])
             slot = free.pop() if free else None
+            reserved = 0
             if slot is None:
                 if self.all_slots.get(key, 0) >= self.max_slots:
                     continue
@@ -369,21 +480,17 @@ class ReconServer:
                         self.pending.pop(i)
                         return True
                     continue
-                try:
-                    slot = self._make_slot(head)
-                except Exception as e:  # allocation or build failure: fail this request only
-                    head.future.set_exception(e)
-                    self.pending.pop(i)
-                    return True
-                self.used += slot.nbytes
+                reserved = need
+                self.used += need
                 self.all_slots[key] = self.all_slots.get(key, 0) + 1
+            cap = slot.batch if slot is not None else self._batch_for(head)
             group = [r for r in self.pending if r.key == key and _inputs_ready(r) and _input_error(r) is None]
-            group = group[:slot.batch]
+            group = group[:cap]
             for r in group:
                 self.pending.remove(r)
                 r.t_start = time.perf_counter()
             self.busy += 1
-            t = threading.Thread(target=self._run, args=(slot, key, group), daemon=True)
+            t = threading.Thread(target=self._run, args=(slot, key, group, reserved), daemon=True)
             self._workers.append(t)
             t.start()
             return True
@@ -404,10 +511,25 @@ class ReconServer:
             self.evictions += 1
             del s
 
-    def _run(self, slot, key, group):
+    def _run(self, slot, key, group, reserved):
+        """Worker of one batch: builds the slot first when the scheduler reserved the
+        budget for a new one (outside the lock, so finishing batches are not held up),
+        then runs the batch and returns the slot."""
         outs, err = None, None
         try:
             torch.cuda.set_device(self.device)
+            if slot is None:
+                try:
+                    slot = self._make_slot(group[0])
+                finally:
+                    with self.cv:
+                        if slot is None:  # construction failed: release the reservation
+                            self.used -= reserved
+                            self.all_slots[key] -= 1
+                            if self.all_slots[key] == 0:
+                                del self.all_slots[key]
+                        else:  # account the slot's own size instead of the estimate
+                            self.used += slot.nbytes - reserved
             for r in group:
                 _resolve_inputs(r)
             outs = slot.run(group)
@@ -422,7 +544,8 @@ class ReconServer:
             if outs is not None:
                 self.done.extend(group)
             self.busy -= 1
-            self.free_slots.setdefault(key, []).append(slot)
+            if slot is not None:
+                self.free_slots.setdefault(key, []).append(slot)
             self.cv.notify_all()
         for i, r in enumerate(group):
             if outs is not None:

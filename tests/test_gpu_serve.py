@@ -133,3 +133,95 @@ def test_file_inputs_and_outputs(tmp_path, cuda):
                               want[i])
     assert np.allclose(got_cg, want_cg, rtol=1e-6, atol=1e-7)
     assert np.array_equal(np.fromfile(tmp_path / "cg_out.raw", dtype=np.float32).reshape(got_cg.shape), got_cg)
+
+
+def test_batched_cgls_requests_match_alone(cuda):
+    """Several CGLS requests of one class run as one batch (one graph launch of k
+    solves on a slot that shares the projector workspace between members): each result
+    equals the request run alone."""
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(31)
+    cg = _cgls_obj(n=24, nz=8, nu=48, nv=12, views=30, DetectorElementHeight=1.0)
+    sg = [rng.uniform(0, 0.5, (12, 30, 48)).astype(np.float32) for _ in range(3)]
+    x0 = [rng.uniform(0, 0.01, (8, 24, 24)).astype(np.float32) for _ in range(3)]
+    srv = ReconServer(batch=1, max_slots_per_class=1)
+    alone = [srv.submit_cgls(cg, s, x, 4).result(timeout=120) for s, x in zip(sg, x0)]
+    srv.close()
+    srv = ReconServer(batch=4, max_slots_per_class=1)
+    srv.submit_cgls(cg, sg[0], x0[0], 4).result(timeout=120)  # builds the slot (its 4 graphs)
+    futs = [srv.submit_cgls(cg, s, x, 4) for s, x in zip(sg, x0)]
+    got = [f.result(timeout=120) for f in futs]
+    st = srv.stats()
+    srv.close()
+    assert st["slots"]["cgls"] == 1
+    for a, b in zip(alone, got):
+        assert np.allclose(a, b, rtol=1e-6, atol=1e-7)
+
+
+def test_partial_batch_runs_only_its_members(cuda):
+    """A batch of k requests on a slot of `batch` members replays the graph of its
+    first k members: the other members' outputs are not recomputed."""
+    import torch
+    from reconstruction_program_taichi_gb300.serve import _FbpSlot, _Request
+    o = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60)
+    slot = _FbpSlot(o, 3, "f32", torch.device("cuda"), use_graph=True)
+    assert sorted(slot.graphs) == [1, 2, 3]
+    rng = np.random.default_rng(33)
+    s = rng.uniform(0, 1, (24, 60, 72)).astype(np.float32)
+    for t in slot.out[1:]:
+        t.fill_(7.0)
+    out = slot.run([_Request("fbp", o, s)])
+    torch.cuda.synchronize()
+    assert all(bool((t == 7.0).all()) for t in slot.out[1:])
+    full = slot.run([_Request("fbp", o, s)] * 3)
+    assert all(np.array_equal(out[0], f) for f in full)
+
+
+def test_configs_that_differ_only_in_the_scan_range_are_not_batched(cuda):
+    """A short scan (Parker weights, other angles and redundancy factor) and a full scan
+    of otherwise equal configs go to different slots: in a mix each result equals its
+    own config's result alone."""
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(34)
+    full, short = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60), _cone_obj(n=40, nz=16, nu=72, nv=24, views=60,
+                                                                          TotalScanAngle=220)
+    s = rng.uniform(0, 1, (24, 60, 72)).astype(np.float32)
+    srv = ReconServer(batch=1, max_slots_per_class=1)
+    want = [srv.submit_fbp(o, s).result(timeout=120) for o in (full, short)]
+    srv.close()
+    assert not np.array_equal(want[0], want[1])
+    srv = ReconServer(batch=4, max_slots_per_class=1)
+    futs = [srv.submit_fbp(o, s) for o in (full, short, full, short)]
+    got = [f.result(timeout=120) for f in futs]
+    st = srv.stats()
+    srv.close()
+    assert st["classes"] == 2
+    for i, g in enumerate(got):
+        assert np.array_equal(g, want[i % 2])
+
+
+def test_mixed_precision_requests(cuda):
+    """storage='bf16' serves the mixed path (two-part tensor-core filter, bf16
+    backprojection coefficients; bf16 projector cells in CGLS): the same result as the
+    pipeline run directly, close to the plain result, in its own slot class."""
+    import torch
+    from reconstruction_program_taichi_gb300.fbp import FdkPipeline
+    from reconstruction_program_taichi_gb300.serve import ReconServer
+    rng = np.random.default_rng(35)
+    o = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60)
+    s = rng.uniform(0, 1, (24, 60, 72)).astype(np.float32)
+    cg = _cgls_obj(n=24, nz=8, nu=48, nv=12, views=30, DetectorElementHeight=1.0)
+    sc = rng.uniform(0, 0.5, (12, 30, 48)).astype(np.float32)
+    x0 = np.zeros((8, 24, 24), np.float32)
+    srv = ReconServer(batch=2, max_slots_per_class=1)
+    plain, mixed = srv.submit_fbp(o, s).result(timeout=120), srv.submit_fbp(o, s, storage="bf16").result(timeout=120)
+    cg_plain = srv.submit_cgls(cg, sc, x0, 3).result(timeout=120)
+    cg_mixed = srv.submit_cgls(cg, sc, x0, 3, storage="bf16").result(timeout=120)
+    st = srv.stats()
+    srv.close()
+    assert st["classes"] == 4
+    direct = FdkPipeline(o, storage="bf16", filter_impl="tc").run(torch.from_numpy(s).cuda()).cpu().numpy()
+    assert np.array_equal(mixed, direct)
+    assert np.array_equal(plain == 0, mixed == 0)
+    assert np.linalg.norm(mixed - plain) / np.linalg.norm(plain) < 5e-3
+    assert np.linalg.norm(cg_mixed - cg_plain) / np.linalg.norm(cg_plain) < 2e-2

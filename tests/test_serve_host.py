@@ -108,3 +108,110 @@ def test_admission_waits_for_a_slow_read(server, tmp_path, monkeypatch):
     assert not slow.done()
     gate.set()
     assert np.allclose(slow.result(timeout=30), 48.0)
+
+
+def _parsed(**kw):
+    from reconstruction_program_taichi_gb300 import config
+
+    class O:
+        verbose = False
+
+    cfg = {"InputDir": "/tmp/a", "OutputDir": "/tmp/b", "InputFiles": "sgm_.*", "OutputFilePrefix": "",
+           "OutputFileReplace": ["sgm", "rec"], "DetectorElementCountHorizontal": 64, "DetectorElementWidth": 0.8,
+           "DetectorOffsetHorizontal": 0.0, "DetectorElementCountVertical": 16, "DetectorElementHeight": 0.8,
+           "Views": 90, "TotalScanAngle": 360, "SourceIsocenterDistance": 300, "SourceDetectorDistance": 550,
+           "ImageDimension": 32, "PixelSize": 0.5, "ImageDimensionZ": 8, "VoxelHeight": 0.5, "ConeBeam": True,
+           "HammingFilter": 1, "ForwardProjectionStepSize": 0.3, "Lambda": 1e-3}
+    cfg.update(kw)
+    cfg = {k: v for k, v in cfg.items() if v is not None}  # None removes a key
+    o = O()
+    config.parse_fbp(o, cfg)
+    config.parse_fpj(o, cfg)
+    config.parse_fpj_v3(o, cfg)
+    config.parse_ir(o, cfg)
+    return o
+
+
+@pytest.mark.parametrize("kw", [
+    {"TotalScanAngle": 220},                                   # short scan (Parker weights)
+    {"Lambda": 2e-3},                                          # CGLS regularisation
+    {"BeamHardeningCorrectionCoefficients": [0.0, 1.0, 0.1]},  # BH polynomial
+    {"ImageRotation": 1.0},
+    {"HammingFilter": 0.5},
+    {"DetectorOffsetVertical": 0.2},
+    {"CurvedDetector": True},
+    {"ForwardProjectionStepSize": 0.2},
+    {"ImageCenterZ": 0.3},
+    {"DetectorElementVerticalGaussFilterSize": 1.5},
+    {"GaussianApodizedRamp": 1.2, "HammingFilter": None},
+])
+def test_slot_key_separates_configs_that_change_the_result(kw):
+    """Requests are batched on one slot (whose pipeline is built from the first
+    request's config) only when their parsed configs agree in everything that can
+    change the result."""
+    base, other = _parsed(), _parsed(**kw)
+    for kind in ("fbp", "cgls"):
+        a = serve._Request(kind, base, None, n_iter=3)
+        b = serve._Request(kind, other, None, n_iter=3)
+        assert a.key != b.key, kw
+
+
+def test_slot_key_ignores_file_names():
+    a = _parsed()
+    b = _parsed(InputDir="/elsewhere", OutputDir="/out2", InputFiles="scan_.*", OutputFilePrefix="p_",
+                OutputFileReplace=["scan", "img"])
+    assert serve._Request("fbp", a, None).key == serve._Request("fbp", b, None).key
+    assert serve._Request("fbp", a, None).key != serve._Request("fbp", a, None, storage="bf16").key
+    assert serve._Request("cgls", a, None, n_iter=3).key != serve._Request("cgls", a, None, n_iter=4).key
+
+
+def test_slot_construction_does_not_block_other_batches(monkeypatch):
+    """A new slot is built by its batch's worker outside the scheduler's lock: while
+    one class's slot is still being built, requests of a class with a free slot run
+    and their futures resolve."""
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: True)
+    monkeypatch.setattr(torch.cuda, "set_device", lambda d: None)
+    gate = threading.Event()
+    slow_obj = _Obj(n=9)
+
+    def make(self, req):
+        if req.obj is slow_obj:
+            assert gate.wait(20)
+        return _FakeSlot(req.obj)
+
+    monkeypatch.setattr(serve.ReconServer, "_make_slot", make)
+    _FakeSlot.runs = []
+    srv = serve.ReconServer(device="cuda:0", hbm_budget_gb=1.0, batch=2)
+    try:
+        o = _Obj()
+        assert np.allclose(srv.submit_fbp(o, np.ones((4, 6, 10), np.float32)).result(timeout=30), 24.0)
+        slow = srv.submit_fbp(slow_obj, np.ones((4, 6, 10), np.float32))
+        time.sleep(0.1)  # the slow class's worker is now inside the slot construction
+        fast = srv.submit_fbp(o, np.full((4, 6, 10), 3.0, np.float32))
+        assert np.allclose(fast.result(timeout=10), 72.0)
+        assert not slow.done()
+        gate.set()
+        assert np.allclose(slow.result(timeout=30), 24.0)
+        assert srv.stats()["slots"]["fbp"] == 2
+    finally:
+        gate.set()
+        srv.close()
+
+
+def test_failed_slot_construction_releases_its_reservation(monkeypatch):
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: True)
+    monkeypatch.setattr(torch.cuda, "set_device", lambda d: None)
+
+    def make(self, req):
+        raise RuntimeError("out of device memory")
+
+    monkeypatch.setattr(serve.ReconServer, "_make_slot", make)
+    srv = serve.ReconServer(device="cuda:0", hbm_budget_gb=1.0, batch=2)
+    try:
+        f = srv.submit_fbp(_Obj(), np.ones((4, 6, 10), np.float32))
+        with pytest.raises(RuntimeError, match="out of device memory"):
+            f.result(timeout=30)
+        time.sleep(0.05)
+        assert srv.used == 0 and srv.all_slots == {}
+    finally:
+        srv.close()
