@@ -4,8 +4,9 @@
  * The reference (MandoCT-Taichi) has no native ABI: its hot path is Taichi kernels
  * that are methods of Python classes.  Each entry point below replaces one of those
  * kernels (cited per function as file:line in the reference).  The Python drop-in
- * (package reconstruction_program_taichi_gb300) binds this library with ctypes;
- * INTEGRATION.md shows the binding.
+ * (package reconstruction_program_taichi_gb300) binds this library with ctypes: each
+ * function is looked up by name, given the argument types listed in its
+ * declaration here, and called with raw device pointers taken from torch tensors.
  *
  * Conventions
  *   - Every pointer to bulk data is a DEVICE pointer owned by the caller.
@@ -193,19 +194,20 @@ int mct_helical_rebin(const mct_helical* h, const float* sgm, const float* z_pos
 /* ---------------------------------------------------------------- forward projection */
 
 /* Bytes of the optional forward-projection workspace (gather copies of the volume:
- * cone beam, two float32 cell copies of 32 bytes per voxel; fan beam, one
+ * cone beam, two float32 quad copies of 16 bytes per voxel; fan beam, one
  * x/y-transposed copy). */
 size_t mct_fp_workspace_size(const mct_geom* g);
 
 /* Ray-driven trilinear forward projection of vol [nz][nx][nx] for all views into
  * sgm [nv][views][nu] (overwritten).  Rays with mask != 1 (mask [nv][views][nu], or
- * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes; 32-byte aligned for
- * cone beam, 16-byte for fan beam; or NULL) receives gather copies of vol: for cone
- * beam every voxel's 2x2x2 trilinear cell (its z-pairs and x-differences, 32 bytes,
- * one 256-bit load) in [z][y][x] and [z][x][y] order, for fan beam an x/y-transposed
- * copy; views whose detector columns run along y read the transposed order, so a
- * warp's gathers are coalesced.  Results are identical with and without the
- * workspace.  Replaces
+ * NULL for none) give 0.  workspace (mct_fp_workspace_size bytes, 16-byte aligned, or
+ * NULL) receives gather copies of vol: for cone beam, per voxel the z-pairs of the
+ * voxel and of its neighbour along the copy's slow axis (16 bytes; a trilinear cell is
+ * two adjacent elements) in [z][y][x] and [z][x][y] order, for fan beam an
+ * x/y-transposed copy; views whose detector columns run along y read the transposed
+ * order, so a warp's gathers are coalesced.  Results agree with and without the
+ * workspace to float32 rounding (the same samples, so the same zero pattern).
+ * Replaces
  * Mgfpj_v3.ForwardProjectionBilinear run_mgfpj_v3.py:184-366 and
  * Mgfbp_ir.ForwardProjectionBilinear run_mgfbp_iterative_recon_IRN_CGLS.py:494-676. */
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
@@ -303,6 +305,14 @@ int mct_tv_weights(const mct_geom* g, const float* x, float beta, float* wr, voi
  * run_mgfbp_iterative_recon_IRN_CGLS.py:267-286. */
 int mct_dtwd(const mct_geom* g, const float* x, const float* wr, float s, const float* out_in,
              float a, float* out, void* stream);
+
+/* mct_dtwd fused with the CG step's inner product: out = a*out_in + s * D^T W D x and
+ * *dot = sum x[i]*out[i] in float64 (device scalar, overwritten), in one pass over the
+ * volume (out may be out_in).  Replaces the last Dt_W_D of the operator and the
+ * np.sum(d * q) of TikhonovSol run_mgfbp_iterative_recon_IRN_CGLS.py:200-203.
+ * partials: device scratch of mct_reduce_scratch_size() bytes. */
+int mct_dtwd_dot(const mct_geom* g, const float* x, const float* wr, float s, const float* out_in,
+                 float a, float* out, double* partials, double* dot, void* stream);
 
 /* sum sqrt(|D x|^2 + beta) accumulated in float64 into *result (device, overwritten).
  * Replaces Mgfbp_ir.TVPenaltyVal run_mgfbp_iterative_recon_IRN_CGLS.py:245-254.

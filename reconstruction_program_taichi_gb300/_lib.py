@@ -100,6 +100,7 @@ SIGNATURES = {
     "mct_bp_ref_unmatched": (ctypes.c_int, [_G, _T, _P, _P, _P]),
     "mct_tv_weights": (ctypes.c_int, [_G, _P, _f32, _P, _P]),
     "mct_dtwd": (ctypes.c_int, [_G, _P, _P, _f32, _P, _f32, _P, _P]),
+    "mct_dtwd_dot": (ctypes.c_int, [_G, _P, _P, _f32, _P, _f32, _P, _P, _P, _P]),
     "mct_admm_shrink": (ctypes.c_int, [_G, _P, _f32, _f32, _P, _P, _P, _P, _P]),
     "mct_admm_rhs": (ctypes.c_int, [_G, _P, _P, _P, _P, _P, _f32, _P, _P]),
     "mct_tv_penalty": (ctypes.c_int, [_G, _P, _f32, _P, _P, _P]),

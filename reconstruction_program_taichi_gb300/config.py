@@ -418,7 +418,9 @@ def parse_fpj_v3(self, cfg):
     """Mgfpj_v3.__init__ extras (per-view angle / z-centre files), run_mgfpj_v3.py:129-172."""
     if "ScanAngleFile" in cfg:
         v = _read_value_file(cfg["ScanAngleFile"], "ScanAngleFile", self.view_num)
-        self.array_angle = np.array(v, dtype=np.float32).astype(np.float64) / 180.0 * PI + self.img_rot
+        # float32 arithmetic, as the reference's array (run_mgfpj_v3.py:142)
+        self.array_angle = (np.array(v, dtype=np.float32) / np.float32(180.0) * np.float32(PI)
+                            + np.float32(self.img_rot)).astype(np.float64)
         self.bool_uneven_scan_angle = True
     else:
         self.bool_uneven_scan_angle = False
@@ -473,6 +475,14 @@ def parse_ir(self, cfg):
     if sp not in ("float32", "bfloat16", "float16"):
         _err("StoragePrecision can only be float32, bfloat16 or float16!")
     self.storage_precision = sp
+    # storage of the measured sinogram in the data term P^T b (an addition): "float32"
+    # (default; rounding b to bf16 adds errors of the size of the photon noise, which
+    # the iterations fit), "float16" (fp16 with a power-of-two scale, 2^-11 relative)
+    # or "bfloat16"
+    dp = cfg.get("SinogramPrecision", "float32")
+    if dp not in ("float32", "bfloat16", "float16"):
+        _err("SinogramPrecision can only be float32, bfloat16 or float16!")
+    self.sinogram_precision = dp
 
 
 def parse_piccs(self, cfg):

@@ -311,11 +311,18 @@ __global__ void admm_rhs_kernel(int nx, int nz, const float* __restrict__ bpb, c
     }
 }
 
+__device__ __forceinline__ double block_sum(double v);
+
 // out = a*out_in + s * (D^T W D x), run_mgfbp_iterative_recon_IRN_CGLS.py:267-286.
-__global__ void dtwd_kernel(int nx, int nz, const float* __restrict__ x, const float* __restrict__ wr, float s,
-                            const float* __restrict__ out_in, float a, float* __restrict__ out) {
+// DOT: also the per-block float64 partial sums of x[i] * out[i] (the CG step's <d, q>
+// while q is being written; out may alias out_in).
+template <bool DOT>
+__global__ void __launch_bounds__(256)
+dtwd_kernel(int nx, int nz, const float* __restrict__ x, const float* __restrict__ wr, float s,
+            const float* out_in, float a, float* out, double* __restrict__ partials) {
     const int64_t n = (int64_t)nz * nx * nx;
     const int64_t plane = (int64_t)nx * nx;
+    double dsum = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % nx);
         const int iy = (int)((i / nx) % nx);
@@ -340,6 +347,11 @@ __global__ void dtwd_kernel(int nx, int nz, const float* __restrict__ x, const f
         float v = s * r;
         if (a != 0.0f) v += a * out_in[i];
         out[i] = v;
+        if (DOT) dsum += (double)c * (double)v;
+    }
+    if (DOT) {
+        dsum = block_sum(dsum);
+        if (threadIdx.x == 0) partials[blockIdx.x] = dsum;
     }
 }
 
@@ -548,8 +560,22 @@ int mct_dtwd(const mct_geom* g, const float* x, const float* wr, float s, const 
              void* stream) {
     MCT_REQUIRE(g && x && wr && out && out != x && out != wr && g->nx >= 1 && g->nz >= 1, "mct_dtwd: bad arguments");
     MCT_REQUIRE(a == 0.0f || out_in, "mct_dtwd: out_in is NULL");
-    dtwd_kernel<<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, x, wr, s, out_in, a, out);
+    dtwd_kernel<false><<<ew_grid(vol_elems(*g)), 256, 0, as_stream(stream)>>>(g->nx, g->nz, x, wr, s, out_in, a, out,
+                                                                             nullptr);
     return launched("dtwd_kernel");
+}
+
+int mct_dtwd_dot(const mct_geom* g, const float* x, const float* wr, float s, const float* out_in, float a, float* out,
+                 double* partials, double* dot, void* stream) {
+    MCT_REQUIRE(g && x && wr && out && partials && dot && out != x && out != wr && g->nx >= 1 && g->nz >= 1,
+                "mct_dtwd_dot: bad arguments");
+    MCT_REQUIRE(a == 0.0f || out_in, "mct_dtwd_dot: out_in is NULL");
+    static_assert(RED_THREADS == 256, "dtwd_kernel<true> reduces over blocks of 256 threads");
+    cudaStream_t st = as_stream(stream);
+    dtwd_kernel<true><<<RED_BLOCKS, RED_THREADS, 0, st>>>(g->nx, g->nz, x, wr, s, out_in, a, out, partials);
+    MCT_TRY(launched("dtwd_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, st>>>(partials, RED_BLOCKS, dot);
+    return launched("finish_sum_kernel");
 }
 
 size_t mct_reduce_scratch_size(void) { return (size_t)RED_BLOCKS * sizeof(double); }

@@ -5,8 +5,9 @@ Mirrors run_mgfbp_iterative_recon_IRN_CGLS.py:14-370 and
 run_mgfbp_iterative_recon_IRN_CGLS_piccs.py:13-161 with everything resident on the
 GPU: the reference moves the whole volume between host and device for every
 P^T P and runs the CG vector algebra in NumPy; here each CG iteration is one FP
-launch, one BP launch, the fused TV stencil, two float64 inner products and two
-fused vector updates, with alpha and beta kept on the device.
+launch, one BP launch, the TV stencil fused with the float64 inner product <d, q>,
+and two fused vector updates (the first also yields |r|^2 for the next iteration),
+with alpha and beta kept on the device.
 
 Operators: by default the reference's pair (masked trilinear FP and the
 voxel-driven per-view backprojector with distance_factor*pixel_size weights);
@@ -46,6 +47,7 @@ class IrSystem:
         # reference backprojector; the exact adjoint scatters float32 either way
         self.dtype = kinds[storage]
         self.fp_dtype = self.dtype if self.dg.geom.flags & ops.MCT_CONE else ops.MCT_F32
+        self.data_dtype = kinds[getattr(obj, "sinogram_precision", "float32")]
         self.mask = ops.effective_map(self.dg)
         f32 = dict(dtype=torch.float32, device=self.device)
         self.fp_buf = torch.empty(self.dg.sgm_shape, **f32)
@@ -81,10 +83,11 @@ class IrSystem:
 
     def bp_b(self, sgm):
         """P^T (b * mask) (run_mgfbp_iterative_recon_IRN_CGLS.py:319-336).  The measured
-        data is packed at float32 whatever the storage precision: rounding b to bf16
-        adds noise of the order of the photon noise, which the iterations would fit;
-        only the operator applications inside CG use the reduced storage."""
-        return self.bp(sgm * self.mask, dtype=ops.MCT_F32)
+        data is stored (packed) at the sinogram precision, float32 unless the config
+        asks for 16 bits: rounding b to bf16 adds noise of the order of the photon
+        noise, which the iterations would fit; float16 with its power-of-two scale
+        rounds to 2^-11 of the largest value's binade."""
+        return self.bp(sgm * self.mask, dtype=self.data_dtype)
 
     def dtwd_acc(self, x, wr, s, acc):
         """acc += s * D^T W D x (in place)."""
@@ -110,14 +113,22 @@ class IrSystem:
         r = d.clone()
         x = x_seed.clone()
         q = torch.empty_like(x)
+        rr, rr_new = self._rr, self._rr_new
+        ops.dot(r, r, out=rr)
         for _ in range(n_iter):
             self.ptp(d, out=q)
-            for s, w in op_terms:
+            # the last TV term is added in the same pass as <d, q>
+            for s, w in op_terms[:-1]:
                 self.dtwd_acc(d, w, s, q)
-            ops.dot(r, r, out=self._rr)
-            ops.dot(d, q, out=self._dq)
-            ops.cgls_update(self._rr, self._dq, x, r, d, q, self._rr_new)
-            ops.cgls_direction(self._rr, self._rr_new, r, d)
+            if op_terms:
+                ops.dtwd_dot(self.dg, d, op_terms[-1][1], op_terms[-1][0], q, self._dq)
+            else:
+                ops.dot(d, q, out=self._dq)
+            # x += alpha d, r -= alpha q and rr_new = |r|^2 in one pass; |r|^2 of this
+            # iteration is the next iteration's rr (no separate pass over r)
+            ops.cgls_update(rr, self._dq, x, r, d, q, rr_new)
+            ops.cgls_direction(rr, rr_new, r, d)
+            rr, rr_new = rr_new, rr
         return x
 
     def loss_tv(self, x, sgm, lam, beta, extra=None):

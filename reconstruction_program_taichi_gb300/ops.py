@@ -347,6 +347,17 @@ def dtwd(dg, x, wr, s=1.0, out_in=None, a=0.0, out=None):
     return out
 
 
+def dtwd_dot(dg, x, wr, s, acc, dot_out):
+    """acc += s * D^T W D x (in place) and dot_out = <x, acc> (float64 device scalar),
+    in one pass."""
+    _check(x, "x", dg.vol_shape)
+    _check(wr, "wr", dg.vol_shape)
+    _check(acc, "acc", dg.vol_shape)
+    _lib.call("mct_dtwd_dot", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(acc), 1.0, _ptr(acc),
+              _ptr(reduce_scratch(x.device)), _ptr(dot_out), _stream())
+    return dot_out
+
+
 _scratch = {}
 
 
