@@ -260,8 +260,37 @@ class _MathCompat:
         return g
 
 
+# per-view side files (run_mgfpj_v3.py:131-172): ScanAngleFile (degrees; Mgfbp_ir keeps
+# them, Mgfpj_v3's InitializeArrays overwrites them) and ImageCenterZFile (per-view image
+# centre z, used by both projectors and the IR backprojector)
+SIDE_FPJ_CASES = {
+    "fpj_cone_sidefiles": _upd(BASE_FPJ, __ScanAngles=[0.0, 27.0, 61.5, 88.0, 121.0, 149.5, 183.0, 210.0, 241.5,
+                                                       268.0, 302.0, 330.5],
+                               __CenterZ=[0.2 + 0.15 * j for j in range(12)]),
+}
+SIDE_IR_CASES = {
+    "ir_tv_sidefiles": _upd(BASE_IR, __ScanAngles=[3.0, 40.0, 71.0, 105.0, 139.0, 178.0, 212.0, 250.0, 288.0, 323.0],
+                            __CenterZ=[0.4 - 0.2 * j for j in range(10)]),
+}
+
+
 def _clean(cfg):
     return {k: v for k, v in cfg.items() if v is not None}
+
+
+def _side_files(cfg, out):
+    """Write the case's per-view side files into the working folder, point the config
+    at them and keep their values in the fixture."""
+    if "__ScanAngles" in cfg:
+        vals = cfg.pop("__ScanAngles")
+        json.dump({"Value": vals}, open("scan_angle.jsonc", "w"))
+        cfg["ScanAngleFile"] = os.path.abspath("scan_angle.jsonc")
+        out["side_scan_angles"] = np.asarray(vals, np.float64)
+    if "__CenterZ" in cfg:
+        vals = cfg.pop("__CenterZ")
+        json.dump({"Value": vals}, open("center_z.jsonc", "w"))
+        cfg["ImageCenterZFile"] = os.path.abspath("center_z.jsonc")
+        out["side_center_z"] = np.asarray(vals, np.float64)
 
 
 @contextlib.contextmanager
@@ -330,13 +359,15 @@ def run_fpj_case(name, cfg, R3, rng):
         if not cfg.get("ConeBeam", False):
             vol = _smooth_volume(rng, cfg["DetectorElementCountVertical"], cfg["ImageDimension"])
         vol.tofile("img/img_a.raw")
+        side = {}
+        _side_files(cfg, side)
         json.dump(cfg, open("config.jsonc", "w"))
         conf = R3.ReadConfigFile("config.jsonc")
         fpj = R3.Mgfpj_v3(conf)
         sgm = fpj.MainFunction()
         return dict(config=json.dumps(cfg), input_vol=vol, sgm=np.asarray(sgm, np.float64),
                     u=_arr(fpj.array_u_taichi), v=_arr(fpj.array_v_taichi),
-                    angles=_arr(fpj.array_angle_taichi), cz=_arr(fpj.array_img_center_z_taichi).ravel())
+                    angles=_arr(fpj.array_angle_taichi), cz=_arr(fpj.array_img_center_z_taichi).ravel(), **side)
 
 
 def run_fpj_variant_case(name, cfg, module, rng):
@@ -374,6 +405,7 @@ def run_ir_case(name, cfg, RI, RP, R, rng):
             prior.tofile("prior.raw")
             cfg["PriorImageFile"] = d + "/prior.raw"
             out["prior"] = prior
+        _side_files(cfg, out)
         json.dump(cfg, open("config.jsonc", "w"))
         conf = R.ReadConfigFile("config.jsonc")
         if "Alpha" in cfg:
@@ -430,7 +462,8 @@ def main():
         + [(k, v, "ir") for k, v in IR_CASES.items()] + [(k, v, "v1") for k, v in FPJ_V1_CASES.items()] \
         + [(k, v, "v2") for k, v in FPJ_V2_CASES.items()] + [(k, v, "pm") for k, v in PM_CASES.items()] \
         + [(k, v, "fbpv2") for k, v in FBPV2_CASES.items()] + [(k, v, "helical") for k, v in HELICAL_CASES.items()] \
-        + [(k, v, "admm") for k, v in ADMM_CASES.items()]
+        + [(k, v, "admm") for k, v in ADMM_CASES.items()] + [(k, v, "fpj") for k, v in SIDE_FPJ_CASES.items()] \
+        + [(k, v, "ir") for k, v in SIDE_IR_CASES.items()]
     for i, (name, cfg, kind) in enumerate(jobs):
         if only and name not in only:
             continue

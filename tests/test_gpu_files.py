@@ -61,3 +61,23 @@ def test_run_mgfpj_v3_over_a_folder_matches_single_file_runs(tmp_path, cuda):
                               np.fromfile(d1 / f"sgm_{t}.raw", dtype=np.float32)), t
     last = _last_listed(d_in, "img").replace("img", "sgm")
     assert np.array_equal(ret.ravel(), np.fromfile(d_out / last, dtype=np.float32))
+
+
+def test_tiff_output_format(tmp_path, cuda):
+    """OutputFileFormat 'tif' (run_mgfbp.py:1199-1203, 1306-1309): the output file is
+    named *.tif and holds the returned volume, one page per slice; SaveFilteredSinogram
+    writes the filtered sinogram as a TIFF with one page per view, [views, rows, cols]
+    (the reference transposes its [rows, views, cols] array before writing, :1293-1298)."""
+    from test_tiff import read_tiff
+    from reconstruction_program_taichi_gb300 import run_mgfbp
+    z = load_golden("fdk_cone")
+    cfg = dict(z["config"], OutputFileFormat="tif", SaveFilteredSinogram=True)
+    path, d_in, d_out = _folder_case(tmp_path, "tif", cfg, {"a": z["input_sgm"]}, "sgm", "rec")
+    vol = run_mgfbp(path, verbose=False)
+    assert sorted(os.listdir(d_out)) == ["rec_a.tif", "sgm_filtered_rec_a.tif"]
+    back = read_tiff(d_out / "rec_a.tif")
+    assert back.shape == vol.shape and np.array_equal(back, vol)
+    filt = read_tiff(d_out / "sgm_filtered_rec_a.tif")
+    want = z["filtered"].transpose(1, 0, 2)
+    assert filt.shape == want.shape
+    assert np.linalg.norm(filt - want) / np.linalg.norm(want) < 1e-4
