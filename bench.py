@@ -277,21 +277,56 @@ def run_gpu(args, w):
     units = 2.0 * nvox * w["views"] * world
     value = units / (ms / 1e3) / 1e9
 
-    # roofline of the dominant kernel (bp or fp), algorithmic bytes per launch
+    # rooflines of the two gather kernels.  "achieved" counts the compulsory bytes of a
+    # launch (its operand read once, its output written once) against the measured HBM
+    # copy bandwidth; "dram" the DRAM bytes ncu measured per launch (a committed
+    # profile, workload and scaling stated there) over this run's launch time; "on_chip"
+    # the binding on-chip unit from the same profile; "gather" the bytes the kernel's
+    # loads deliver (served by L1 and L2), the per-update figure of the operator.
     hbm, _, peak_kind = peaks()
     n_samples = ops.fp_count_samples(fpg)
-    bp_bytes = nvox * w["views"] * (16 if pipe.dtype == ops.MCT_F32 else 8) + nvox * 4
-    fp_bytes = n_samples * (32 if fp_dtype == ops.MCT_F32 else 16) + fpg.geom.nv * fpg.geom.views * fpg.geom.nu * 4
+    prof = {}
+    pj = os.path.join(ROOT, "profiles", "roofline_inputs.json")
+    if os.path.exists(pj):
+        prof = json.load(open(pj))
+    nvox = w["nx"] * w["nx"] * w["nz"]
+    g_fdk = pipe.dg.geom
+    cells = g_fdk.views * g_fdk.nv * (g_fdk.nu - 1)  # (nv - 1) cell rows + one NaN row per view
+    bp_elem = 16 if pipe.dtype == ops.MCT_F32 else 8
+    fp_rays = fpg.geom.nv * fpg.geom.views * fpg.geom.nu
+    kern = {
+        "fp_kernel": dict(ms=float(st[3]), compulsory=nvox * 32 + fp_rays * 4,
+                          gather=n_samples * (32 if fp_dtype == ops.MCT_F32 else 16),
+                          what="copies of the volume (32 B per voxel, both orientations) read once, the "
+                               "projection written once; gathers: one 32-byte (16-bit: 16-byte) cell per "
+                               "in-volume sample"),
+        "fdk_bp_kernel": dict(ms=float(st[2]), compulsory=cells * bp_elem + nvox * 4,
+                              gather=nvox * w["views"] * bp_elem,
+                              what="packed operand (16 B float32 / 8 B 16-bit per detector cell) read once, the "
+                                   "volume written once; gathers: one coefficient cell per voxel x view update"),
+    }
+
+    def kernel_roofline(name):
+        k = kern[name]
+        sec = k["ms"] / 1e3
+        ach = k["compulsory"] / sec / 1e9
+        out = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+               "frac": round(ach / hbm, 4), "traffic": None, "peak_source": peak_kind,
+               "algorithmic_bytes": int(k["compulsory"]), "algorithmic": k["what"],
+               "gather": {"bytes_per_launch": int(k["gather"]), "tb_per_s": round(k["gather"] / sec / 1e12, 2)}}
+        pk = prof.get(name, {})
+        if pk.get("dram_bytes_per_launch") and args.storage == "f32" and w is WORKLOAD:
+            t = float(pk["dram_bytes_per_launch"])
+            out["traffic"] = int(t)
+            out["dram"] = {"gb_per_s": round(t / sec / 1e9, 1), "frac": round(t / sec / 1e9 / hbm, 4),
+                           "source": pk.get("source")}
+        if pk.get("on_chip"):
+            out["on_chip"] = pk["on_chip"]
+        return out
+
     dom = "fp_kernel" if st[3] >= st[2] else "fdk_bp_kernel"
-    dom_ms, dom_bytes = (st[3], fp_bytes) if dom == "fp_kernel" else (st[2], bp_bytes)
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    traffic = None
-    tj = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if os.path.exists(tj) and args.storage == "f32" and w is WORKLOAD:
-        traffic = json.load(open(tj)).get(dom)
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes": int(dom_bytes)}
+    roofline = kernel_roofline(dom)
+    roofline_other = kernel_roofline("fdk_bp_kernel" if dom == "fp_kernel" else "fp_kernel")
 
     # end to end through the public API: pinned host sinogram in, volume + projections
     # out, every step's copies inside the timed region; consecutive steps run through
@@ -319,14 +354,28 @@ def run_gpu(args, w):
            "h2d_bytes_per_step": int(host_sgm.numel() * 4),
            "d2h_bytes_per_step": int(host_vol.numel() * 4 + host_fp.numel() * 4)}
 
+    # accuracy against the float64 restatement of the same operators (evaluated in the
+    # CPU leg, after every timed region): a central 8-slice slab of the FDK volume with
+    # every view, and 4 evenly spaced views of the projection, for every variant
+    checks = Fp64Checks() if (rank == 0 and world == 1 and not args.no_cpu) else None
+    accuracy = {"fdk": {}, "fp": {}}
+    ref_vol = pipe.run(sgm).clone()
+    ref_fp = ops.fp(fpg, ref_vol, dtype=fp_dtype).clone()
+    z0, z1 = w["nz"] // 2 - 4, w["nz"] // 2 + 4
+    fp_views = spread(w["views"], 4)
+    if checks is not None:
+        sgm_host = sgm.cpu().numpy()
+        vol_host = ref_vol.cpu().numpy()
+        taps64 = hann_from_ramp(geometry.recon_taps(o))
+        checks.fdk_slab(accuracy["fdk"], args.storage, o, sgm_host, taps64, z0, z1, vol_host[z0:z1])
+        checks.fp_views(accuracy["fp"], args.storage, o, vol_host, fp_views, ref_fp[:, fp_views].cpu().numpy())
+
     # mixed precision: tensor-core split-bf16 filter, bf16 backprojection operand, bf16
     # forward-projection cells; the whole step, then FDK-only variants
     mixed = None
     # the mixed-precision, 2D, iterative and widened sections run in single-GPU runs
     # (they do not enter the metric; with several ranks they would only repeat per rank)
     if args.storage == "f32" and not args.no_mixed and world == 1:
-        ref_vol = pipe.run(sgm).clone()
-        ref_fp = ops.fp(fpg, ref_vol).clone()
         plain_ms = float(st[0] + st[1] + st[2])
         mixed = {"fdk_plain_ms": round(plain_ms, 3)}
         pm = fbp.FdkPipeline(o, device=dev, storage="bf16", filter_impl="tc")
@@ -360,6 +409,13 @@ def run_gpu(args, w):
             "fp_rel_l2_vs_plain": float(torch.linalg.vector_norm(fp_m - ref_fp) / torch.linalg.vector_norm(ref_fp)),
             "storage": "two-part split-bf16 tcgen05 row filter; bf16 backprojection coefficients; bf16 FP cells",
         }
+        if checks is not None:
+            checks.fdk_slab(mixed["step"], "fdk", o, sgm_host, taps64, z0, z1, mv[z0:z1].cpu().numpy())
+            # the projector's own error: 16-bit cells of the plain FDK volume
+            for name, dt in (("fp_bf16_cells", ops.MCT_BF16), ("fp_f16_cells", ops.MCT_F16)):
+                mixed[name] = {}
+                got = ops.fp(fpg, ref_vol, dtype=dt)[:, fp_views].cpu().numpy()
+                checks.fp_views(mixed[name], "fp", o, vol_host, fp_views, got)
         del pm, ph, live, fp_m
         for name, storage, impl in (("simt_filter_f32", "f32", "simt"), ("tc2_filter_f32", "f32", "tc"),
                                     ("tc2_filter_bf16_bp", "bf16", "tc"), ("tc2_filter_f16_bp", "f16", "tc")):
@@ -384,24 +440,29 @@ def run_gpu(args, w):
             rel = float(torch.linalg.vector_norm(mv - ref_vol) / torch.linalg.vector_norm(ref_vol))
             mixed[name] = {"fdk_ms": round(mms, 3), "weight_filter_ms": round(f0.elapsed_time(f1), 3),
                            "speedup_fdk": round(plain_ms / mms, 3), "rel_l2_vs_plain": rel}
+            if checks is not None:
+                checks.fdk_slab(mixed[name], "fdk", o, sgm_host, taps64, z0, z1, mv[z0:z1].cpu().numpy())
             del pm
 
     cgls = piccs = c1 = served = None
     if w is WORKLOAD and not args.no_mixed and world == 1:
-        c1 = c1_bench(dev, stream, barrier)
+        c1 = c1_bench(dev, stream, barrier, checks)
     widened = None
     if not args.no_cgls and w is WORKLOAD and world == 1:
-        cgls = irn_bench(dev, stream, barrier)
-        piccs = piccs_bench(dev, stream, barrier)
+        cgls = irn_bench(dev, stream, barrier, checks)
+        piccs = piccs_bench(dev, stream, barrier, checks)
         widened = widen_bench(dev, stream, barrier)
     if not args.no_serve and w is WORKLOAD and world == 1:
-        del pipe, fpg, sgm, fp_out, scans, host_sgm, host_vol, host_fp
+        del pipe, fpg, sgm, fp_out, scans, host_sgm, host_vol, host_fp, ref_vol, ref_fp
         torch.cuda.empty_cache()
         served = serve_bench(dev)
 
+    # CPU leg (after every timed region): the timed CPU baseline, then the float64
+    # checks of the results collected above
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(w, o, budget_s=args.cpu_seconds)
+        cpu["fp64_checks_s"] = round(checks.run(), 2)
 
     if rank == 0:
         line = {
@@ -423,9 +484,10 @@ def run_gpu(args, w):
             "bp_gups": round(nvox * w["views"] / (st[2] / 1e3) / 1e9, 2),
             "fp_gups": round(nvox * w["views"] / (st[3] / 1e3) / 1e9, 2),
             "fp_samples_per_s": round(n_samples / (st[3] / 1e3), 1), "fp_in_volume_samples": n_samples,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "roofline": roofline, "roofline_second_kernel": roofline_other, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches),
             "clocks": clk.summary(), "mixed": mixed, "irn_cgls_tv": cgls, "irn_cgls_piccs": piccs,
-            "fbp_2d_fan": c1, "serving": served, "widened": widened,
+            "fbp_2d_fan": c1, "serving": served, "widened": widened, "accuracy": accuracy,
         }
         print(json.dumps(line))
     if world > 1:
@@ -443,8 +505,9 @@ C4 = dict(nu=1024, nv=128, views=90, nx=512, nz=128, du=0.8, dv=0.8, px=0.4, pz=
           step=0.2, n_ell=20, photons=1e5, seed=2026)
 
 
-def c1_bench(dev, stream, barrier, reps=50):
-    """2D fan-beam FBP, plain and mixed: GUPS, error vs plain and RMSE vs the phantom."""
+def c1_bench(dev, stream, barrier, checks=None, reps=50):
+    """2D fan-beam FBP, plain and mixed: GUPS, error vs plain, RMSE vs the phantom, and
+    (checks) the whole image against the float64 restatement of the same FBP."""
     import torch
     from reconstruction_program_taichi_gb300 import fbp, geometry, ops
     o = parse(C1)
@@ -473,11 +536,30 @@ def c1_bench(dev, stream, barrier, reps=50):
             ref = vol.clone()
         else:
             r["rel_l2_vs_plain"] = float(torch.linalg.vector_norm(vol - ref) / torch.linalg.vector_norm(ref))
+        if checks is not None:
+            checks.fdk_slab(r, "fbp", o, sgm.cpu().numpy(), hann_from_ramp(geometry.recon_taps(o)), 0, 1,
+                            vol.cpu().numpy())
         out[name] = r
     return out
 
 
-def irn_bench(dev, stream, barrier):
+def ir_operator_checks(checks, target, ir, sy, sgm, ph, zc):
+    """Queue the FP64 checks of one IR system's operators at its storage precision:
+    the masked projector on 4 evenly spaced views of the phantom, and the driver's
+    backprojector of the masked measured sinogram on an 8-slice central slab."""
+    if checks is None:
+        return
+    g = sy.dg.geom
+    views = spread(g.views, 4)
+    vol = ph.cpu().numpy()
+    got = sy.fp(ph)[:, views].cpu().numpy()
+    checks.fp_views(target, "fp", ir, vol, views, got, mask=sy.mask[:, views].cpu().numpy(), ir=True)
+    sm = (sgm * sy.mask).contiguous()
+    bp = sy.bp(sm)
+    checks.bp_unmatched_slab(target, "bp", ir, sm.cpu().numpy(), zc - 4, zc + 4, bp[zc - 4:zc + 4].cpu().numpy())
+
+
+def irn_bench(dev, stream, barrier, checks=None):
     """IRN-CGLS-TV, 20 reweightings x 10 CG iterations (the reference driver's loop,
     run_mgfbp_iterative_recon_IRN_CGLS.py:157-172) on 512x512x64 @0.4 mm, 360 views,
     1024x64 detector, lambda 1e-3, beta_TV 1e-6, with the reference operator pair
@@ -490,10 +572,14 @@ def irn_bench(dev, stream, barrier):
                      "(231 P^T P), zero start, Poisson 1e5",
            "operator": "reference pair (masked FP + per-view BP)"}
     ph = None
-    for storage in ("float32", "bfloat16", "float16"):
+    # (result key, gather storage, measured-sinogram storage); "float16_sinogram" is the
+    # configuration's own precision plan: FP16 sinogram storage, float32 accumulation
+    variants = (("float32", "float32", "float32"), ("bfloat16", "bfloat16", "float32"),
+                ("float16", "float16", "float32"), ("float16_sinogram", "float16", "float16"))
+    for key, storage, sino in variants:
         cfg = make_config(C3)
         cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 20, "NumberOfIterations": 10,
-                    "StoragePrecision": storage})
+                    "StoragePrecision": storage, "SinogramPrecision": sino})
         ir = Mgfbp_ir(cfg, device=dev, verbose=False)
         sy = ir.system
         sgm = noisy(ops.project_ellipsoids(sy.dg, ellipsoids(C3)), C3["photons"], C3["seed"])
@@ -515,17 +601,20 @@ def irn_bench(dev, stream, barrier):
             yy, xx = torch.meshgrid(torch.arange(n_, device=dev) - (n_ - 1) / 2,
                                     torch.arange(n_, device=dev) - (n_ - 1) / 2, indexing="ij")
             fov = (yy ** 2 + xx ** 2 <= (0.95 * n_ / 2) ** 2).expand_as(ph).contiguous()
-        out[storage] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
-                        "rmse_vs_phantom": rmse(x, ph, fov), "finite": bool(torch.isfinite(x).all())}
+        out[key] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
+                    "rmse_vs_phantom": rmse(x, ph, fov), "finite": bool(torch.isfinite(x).all()),
+                    "gather_storage": storage, "sinogram_storage": sino}
+        if key != "float16_sinogram":
+            ir_operator_checks(checks, out[key], ir, sy, sgm, ph, C3["nz"] // 2)
         del ir, sy, sgm, x
     f = out["float32"]
-    for k in ("bfloat16", "float16"):
+    for k in ("bfloat16", "float16", "float16_sinogram"):
         out[k]["speedup"] = round(f["s_total"] / out[k]["s_total"], 3)
         out[k]["rmse_ratio"] = round(out[k]["rmse_vs_phantom"] / f["rmse_vs_phantom"], 5)
     return out
 
 
-def piccs_bench(dev, stream, barrier):
+def piccs_bench(dev, stream, barrier, checks=None):
     """IRN-CGLS-PICCS (alpha 0.5, lambda 1e-3, 30 reweightings x 8 CG iterations) on
     512x512x128 @0.4 mm with a 1024x128 detector: prior = FDK of 1440 views of phantom
     A, target = 90 views of A plus 3 extra seeded ellipsoids; float32 and bf16 gather
@@ -575,6 +664,7 @@ def piccs_bench(dev, stream, barrier):
             sec = e0.elapsed_time(e1) / 1e3
             out[storage] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
                             "rmse_vs_phantom": rmse(x, truth, fov), "finite": bool(torch.isfinite(x).all())}
+            ir_operator_checks(checks, out[storage], ir, sy, sgm, truth, C4["nz"] // 2)
             del ir, sy, sgm, x, pr
     finally:
         os.remove(prior_file)
@@ -696,6 +786,49 @@ def widen_bench(dev, stream, barrier):
     return out
 
 
+def cg_step_bench(dev):
+    """One TV reweighting and a 3-iteration CG solve at the C3 geometry (float32): the
+    CG kernels (projector, backprojector, TV weights, fused stencil and inner product,
+    vector updates) launched a few times each.  Returns the solve's milliseconds."""
+    import torch
+    from reconstruction_program_taichi_gb300 import ops
+    from reconstruction_program_taichi_gb300.ir import Mgfbp_ir
+    cfg = make_config(C3)
+    cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6})
+    ir = Mgfbp_ir(cfg, device=dev, verbose=False)
+    sy = ir.system
+    sgm = noisy(ops.project_ellipsoids(sy.dg, ellipsoids(C3)), C3["photons"], C3["seed"])
+    x0 = phantom(C3, dev)
+    sy.bpb = sy.bp_b(sgm)
+    wr = ops.tv_weights(sy.dg, x0, 1e-6)
+    lr = 1e-3 * ir.pixel_count_ratio
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sy.cgls(x0, [], [(lr, wr)], 3)
+    e1.record()
+    torch.cuda.synchronize()
+    return round(e0.elapsed_time(e1), 3)
+
+
+def helical_once(dev):
+    """One helical FBP by rebinning (1024x64 detector, 3 rounds x 720 views, pitch 1,
+    512x512 slices); returns its milliseconds."""
+    import torch
+    from reconstruction_program_taichi_gb300.helical import Mgfbp_helical
+    w = WORKLOAD
+    hcfg = make_config(dict(w, nv=64, views=2160))
+    hcfg.update(TotalScanAngle=1080, HelicalPitch=1.0)
+    hel = Mgfbp_helical(hcfg, device=dev, verbose=False)
+    g = torch.Generator(device=dev).manual_seed(5)
+    sgm = torch.rand((64, 2160, w["nu"]), device=dev, generator=g)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    hel.reconstruct(sgm, save_rebinned=False)
+    e1.record()
+    torch.cuda.synchronize()
+    return round(e0.elapsed_time(e1), 3)
+
+
 def adjoint_pair_bench(dev, stream, barrier):
     """The autograd pair at 512x512x64, 360 views: the projector and its exact adjoint,
     which scatters through the cell-space buffer (default) or straight into the volume."""
@@ -740,12 +873,17 @@ def circular_pmatrices(w):
     return np.concatenate(out)
 
 
-def serve_bench(dev, n_req=256, seed=7, mean_gap_ms=150.0):
+def serve_bench(dev, n_req=256, seed=7, mean_gap_ms=150.0, n_sat=96):
     """Serving stream: n_req requests with Poisson arrivals (seeded), mixing 2D fan FBP
     (256^2-1024^2, 360-1440 views), cone-beam FDK (256^3-512^3, 360-1080 views) and
     10-iteration CGLS at 256^3, under a 150 GB HBM budget; sinograms resident on the
-    device (as written by an acquisition pipeline), results returned as device tensors;
-    p50/p99 latency and GUPS."""
+    device (as written by an acquisition pipeline), results returned as device tensors.
+    Run for the plain float32 path and the mixed-precision path (two-part tensor-core
+    filter with bf16 backprojection coefficients; bf16 projector cells in CGLS): p50/p99
+    latency, GUPS, and per request class the RMSE of the result against its phantom.
+    Then a saturated run of each (its slots built first by one request per class, then
+    n_sat requests submitted at once): the GUPS the server sustains with the GPU kept
+    busy."""
     import torch
     from reconstruction_program_taichi_gb300 import config, geometry, ops
     from reconstruction_program_taichi_gb300.serve import ReconServer
@@ -760,7 +898,7 @@ def serve_bench(dev, n_req=256, seed=7, mean_gap_ms=150.0):
     classes.append(("cgls", dict(WORKLOAD, nx=256, nz=256, px=0.8, pz=0.8, nu=512, nv=256, du=1.6, dv=1.6,
                                  views=360, seed=seed + 1)))
     weights = np.array([0.4 / 9] * 9 + [0.4 / 4] * 4 + [0.2])
-    # one noisy sinogram per class, made on the device and kept on the host
+    # one noisy sinogram per class, made and kept on the device
     objs, sgms = [], []
     for kind, w in classes:
         o = parse(w)
@@ -775,64 +913,126 @@ def serve_bench(dev, n_req=256, seed=7, mean_gap_ms=150.0):
     torch.cuda.empty_cache()
     kinds = rng.choice(len(classes), size=n_req, p=weights / weights.sum())
     gaps = rng.exponential(mean_gap_ms / 1e3, size=n_req)
+    sat_kinds = rng.choice(len(classes), size=n_sat, p=weights / weights.sum())
     x0 = {}
-    srv = ReconServer(device=dev, hbm_budget_gb=150.0, batch=4, max_slots_per_class=2)
-    t0 = time.perf_counter()
-    futs = []
-    for i, c in enumerate(kinds):
-        target = t0 + gaps[: i + 1].sum()
-        now = time.perf_counter()
-        if target > now:
-            time.sleep(target - now)
+
+    def class_rmse(c, vol):
+        kind, w = classes[c]
+        ph = phantom(w, dev)
+        if kind == "cgls":
+            n_ = w["nx"]
+            yy, xx = torch.meshgrid(torch.arange(n_, device=dev) - (n_ - 1) / 2,
+                                    torch.arange(n_, device=dev) - (n_ - 1) / 2, indexing="ij")
+            live = (yy ** 2 + xx ** 2 <= (0.95 * n_ / 2) ** 2).expand_as(ph).contiguous()
+        else:
+            live = vol != 0
+        r = rmse(vol, ph, live)
+        del ph, live
+        return r
+
+    def submit(srv, c, storage):
         kind, w = classes[c]
         if kind == "cgls":
             if c not in x0:
                 x0[c] = torch.zeros((w["nz"], w["nx"], w["nx"]), dtype=torch.float32, device=dev)
-            futs.append(srv.submit_cgls(objs[c], sgms[c], x0[c], 10))
-        else:
-            futs.append(srv.submit_fbp(objs[c], sgms[c]))
-    ok = 0
-    for i, f in enumerate(futs):
-        f.result(timeout=600)
-        futs[i] = None  # drop the device result
-        ok += 1
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    counts = {"fbp_2d": int(sum(1 for c in kinds if c < 9)), "fdk": int(sum(1 for c in kinds if 9 <= c < 13)),
-              "cgls10": int(sum(1 for c in kinds if c == 13))}
-    return {"config": f"{n_req} requests, Poisson arrivals (mean gap {mean_gap_ms} ms), 2D FBP 256^2-1024^2 x "
-                      "360-1440 views, FDK 256^3-512^3 x 360-1080 views, CGLS-10 at 256^3; HBM budget 150 GB; "
-                      "batch 4, CUDA graphs",
-            "completed": ok, "mix": counts, "wall_s": round(wall, 3), "p50_ms": round(st["p50_ms"], 2),
-            "p99_ms": round(st["p99_ms"], 2), "mean_ms": round(st["mean_ms"], 2),
-            "queue_p50_ms": round(st["queue_p50_ms"], 2), "service_p50_ms": round(st["service_p50_ms"], 2),
-            "service_p99_ms": round(st["service_p99_ms"], 2), "gups": round(st["gups"], 2),
-            "slots": st["slots"], "classes": st["classes"], "evictions": st["evictions"],
-            "hbm_used_gb": round(st["hbm_used_gb"], 2)}
+            return srv.submit_cgls(objs[c], sgms[c], x0[c], 10, storage=storage)
+        return srv.submit_fbp(objs[c], sgms[c], storage=storage)
+
+    def run(storage, ks, gap_s):
+        srv = ReconServer(device=dev, hbm_budget_gb=150.0, batch=4, max_slots_per_class=2)
+        if gap_s is None:  # saturated: build the slots first (not timed)
+            for f in [submit(srv, c, storage) for c in sorted(set(int(c) for c in ks))]:
+                f.result(timeout=900)
+            srv.done.clear()
+        t0 = time.perf_counter()
+        futs = []
+        for i, c in enumerate(ks):
+            if gap_s is not None:
+                target = t0 + gap_s[: i + 1].sum()
+                now = time.perf_counter()
+                if target > now:
+                    time.sleep(target - now)
+            futs.append(submit(srv, c, storage))
+        per_class = {}
+        for i, f in enumerate(futs):
+            vol = f.result(timeout=900)
+            c = int(ks[i])
+            if gap_s is not None and c not in per_class:
+                per_class[c] = vol  # one result per class for its RMSE
+            futs[i] = None  # drop the device result
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        rm = {}
+        for c, vol in per_class.items():
+            kind, w = classes[c]
+            name = f"{kind}_{w['nx']}{'x' + str(w['nz']) if w.get('cone', True) else ''}_{w['views']}v"
+            rm[name] = class_rmse(c, vol)
+        del per_class
+        torch.cuda.empty_cache()
+        return st, wall, rm
+
+    out = {"config": f"{n_req} requests, Poisson arrivals (mean gap {mean_gap_ms} ms), 2D FBP 256^2-1024^2 x "
+                     "360-1440 views, FDK 256^3-512^3 x 360-1080 views, CGLS-10 at 256^3; HBM budget 150 GB; "
+                     f"batch 4, a CUDA graph per slot member; saturated runs: slots built first, then {n_sat} "
+                     "requests submitted at once",
+           "mix": {"fbp_2d": int(sum(1 for c in kinds if c < 9)), "fdk": int(sum(1 for c in kinds if 9 <= c < 13)),
+                   "cgls10": int(sum(1 for c in kinds if c == 13))}}
+    for name, storage in (("plain", "f32"), ("mixed", "bf16")):
+        st, wall, rm = run(storage, kinds, gaps)
+        sat, sat_wall, _ = run(storage, sat_kinds, None)
+        out[name] = {"storage": storage, "wall_s": round(wall, 3), "p50_ms": round(st["p50_ms"], 2),
+                     "p99_ms": round(st["p99_ms"], 2), "mean_ms": round(st["mean_ms"], 2),
+                     "queue_p50_ms": round(st["queue_p50_ms"], 2), "service_p50_ms": round(st["service_p50_ms"], 2),
+                     "service_p99_ms": round(st["service_p99_ms"], 2), "gups": round(st["gups"], 2),
+                     "completed": st["requests"], "slots": st["slots"], "classes": st["classes"],
+                     "evictions": st["evictions"], "hbm_used_gb": round(st["hbm_used_gb"], 2),
+                     "rmse_vs_phantom": rm,
+                     "saturated": {"requests": sat["requests"], "wall_s": round(sat_wall, 3),
+                                   "gups": round(sat["gups"], 2), "p50_ms": round(sat["p50_ms"], 2),
+                                   "p99_ms": round(sat["p99_ms"], 2)}}
+    p, m = out["plain"], out["mixed"]
+    out["mixed_vs_plain"] = {"p50_ratio": round(m["p50_ms"] / p["p50_ms"], 3),
+                             "p99_ratio": round(m["p99_ms"] / p["p99_ms"], 3),
+                             "saturated_gups_ratio": round(m["saturated"]["gups"] / p["saturated"]["gups"], 3),
+                             "rmse_ratio_per_class": {k: round(m["rmse_vs_phantom"][k] / v, 5)
+                                                      for k, v in p["rmse_vs_phantom"].items()
+                                                      if k in m["rmse_vs_phantom"] and v > 0}}
+    return out
 
 
-# ---------------------------------------------------------------- CPU (reference) arm
+# ---------------------------------------------------------------- CPU leg: baseline and FP64 checks
 
-def cpu_sample(w, o, bp_views, fp_views, filt_rows):
-    """Time the OpenMP C restatement on a bounded sample of one step; returns
-    (seconds for the full step extrapolated, threads, description)."""
+def cpu_geom(w, o):
+    """The C restatement's geometry of workload w (FBP arrays) and the projector's
+    ray arrays."""
     from oracle import cpu_ref
     from reconstruction_program_taichi_gb300 import geometry
-    from reconstruction_program_taichi_gb300._lib import MCT_CONE, Geom
     u, v, ang = geometry.fbp_arrays(o)
-    g = Geom()
-    g.nu, g.nv, g.views, g.nx, g.nz, g.flags = w["nu"], w["nv"], w["views"], w["nx"], w["nz"], MCT_CONE
-    g.du, g.dv, g.px, g.pz, g.sid, g.sdd = w["du"], w["dv"], w["px"], w["pz"], w["sid"], w["sdd"]
-    g.u0, g.u_step, g.v0, g.v_step = u[0], u[1] - u[0], v[0], v[1] - v[0]
-    g.total_scan_angle, g.cz = o.total_scan_angle, o.img_center_z
-    g.fp_step = w["step"]
-    g.fp_steps = geometry.count_steps_v3(w["nx"], w["nz"], w["px"], w["pz"], w["step"])
+    g = cpu_ref.geom_from_config(o, u, v, geometry.count_steps_v3(w["nx"], w["nz"], w["px"], w["pz"], w["step"]))
+    fpu, fpv, _ = geometry.fpj_arrays(o)
+    return g, ang, fpu, fpv
+
+
+def spread(n, k):
+    """k evenly spaced indices of range(n), starting at a non-special offset."""
+    k = max(1, min(k, n))
+    return [int((i + 0.37) * n / k) % n for i in range(k)]
+
+
+def cpu_sample(w, o, bp_views, fp_views, filt_rows):
+    """Time the float32 OpenMP C restatement on a bounded sample of one step: the
+    direct row filter on filt_rows rows, the backprojection of bp_views views and the
+    forward projection of fp_views evenly spaced views, each extrapolated linearly to
+    the whole step (the cost per row and per view is uniform).  Returns (seconds for
+    the full step, threads, description, parts)."""
+    from oracle import cpu_ref
+    g, ang, fpu, fpv = cpu_geom(w, o)
     rng = np.random.default_rng(1)
     rows = w["nv"] * w["views"]
     x = rng.uniform(0, 1, (filt_rows, w["nu"])).astype(np.float32)
     y = np.empty_like(x)
-    taps = hann_from_ramp(geometry.recon_taps(o)).astype(np.float32)
+    taps = hann_from_ramp(recon_taps_of(o)).astype(np.float32)
     t0 = time.perf_counter()
     cpu_ref.filter_rows(g, x, taps, y, 0, filt_rows)
     t_f = (time.perf_counter() - t0) * rows / filt_rows
@@ -840,21 +1040,27 @@ def cpu_sample(w, o, bp_views, fp_views, filt_rows):
     vol = np.zeros((w["nz"], w["nx"], w["nx"]), np.float32)
     alive = np.ones(vol.shape, np.uint8)
     angf = ang.astype(np.float32)
+    j0 = spread(w["views"], 1)[0]
     t0 = time.perf_counter()
-    cpu_ref.fdk_bp(g, angf, F, vol, alive, 0, bp_views)
-    t_bp = (time.perf_counter() - t0) * w["views"] / bp_views
-    fpu, fpv, _ = geometry.fpj_arrays(o)
+    cpu_ref.fdk_bp(g, angf, F, vol, alive, j0, min(w["views"], j0 + bp_views))
+    t_bp = (time.perf_counter() - t0) * w["views"] / (min(w["views"], j0 + bp_views) - j0)
     out = np.zeros((w["nv"], w["views"], w["nu"]), np.float32)
     vol = rng.uniform(0, 0.02, vol.shape).astype(np.float32)
-    step = max(1, w["views"] // fp_views)
+    views = spread(w["views"], fp_views)
+    fpu32, fpv32 = fpu.astype(np.float32), fpv.astype(np.float32)
     t0 = time.perf_counter()
-    for j in range(0, step * fp_views, step):
-        cpu_ref.fp(g, angf, fpu.astype(np.float32), fpv.astype(np.float32), vol, out, j, j + 1)
-    t_fp = (time.perf_counter() - t0) * w["views"] / fp_views
-    desc = (f"OpenMP C restatement, {cpu_ref.threads()} threads: filter {filt_rows} of {rows} rows, "
-            f"backprojection {bp_views} of {w['views']} views, forward projection {fp_views} evenly spaced of "
-            f"{w['views']} views; each extrapolated linearly to the full step")
+    for j in views:
+        cpu_ref.fp(g, angf, fpu32, fpv32, vol, out, j, j + 1)
+    t_fp = (time.perf_counter() - t0) * w["views"] / len(views)
+    desc = (f"OpenMP C restatement (float32), {cpu_ref.threads()} threads: filter {filt_rows} of {rows} rows, "
+            f"backprojection of views {j0}-{j0 + bp_views - 1} of {w['views']}, forward projection of "
+            f"{len(views)} evenly spaced views {views}; each extrapolated linearly to the full step")
     return t_f + t_bp + t_fp, cpu_ref.threads(), desc, dict(filter_s=t_f, bp_s=t_bp, fp_s=t_fp)
+
+
+def recon_taps_of(o):
+    from reconstruction_program_taichi_gb300 import geometry
+    return geometry.recon_taps(o)
 
 
 def cpu_baseline(w, o, budget_s=20.0):
@@ -869,7 +1075,94 @@ def cpu_baseline(w, o, budget_s=20.0):
             "extrapolated_step_s": round(t, 2), "parts_s": {k: round(v, 2) for k, v in parts.items()}}
 
 
+class Fp64Checks:
+    """Results collected during the GPU sections (host copies: the input sinogram, a
+    slab of a volume, a few views of a projection) to be compared, after every timed
+    region, with the float64 C restatement of the same discrete operator on the same
+    inputs (bench.py runs it in its CPU leg).  Each check writes {"rel_l2", "max_abs",
+    ...} under "vs_fp64" into the result dict it belongs to."""
+
+    def __init__(self):
+        self.items = []
+
+    def fdk_slab(self, target, label, o, sgm, taps, z0, z1, got):
+        """FDK (axial) of slices [z0, z1) from the raw sinogram sgm (host float32
+        [nv, views, nu]) with filter taps; got: the GPU slab."""
+        self.items.append(("fdk", target, label, dict(o=o, sgm=sgm, taps=taps, z0=z0, z1=z1, got=got)))
+
+    def fp_views(self, target, label, o, vol, views, got, mask=None, ir=False):
+        """Forward projection of vol (host float32) for the listed views; got: the GPU
+        projection of those views [nv, len(views), nu]; ir: the IR driver's geometry
+        (its arrays, step count and effective-map mask)."""
+        self.items.append(("fp", target, label, dict(o=o, vol=vol, views=list(views), got=got, mask=mask, ir=ir)))
+
+    def bp_unmatched_slab(self, target, label, o, sgm, z0, z1, got):
+        """The IR driver's backprojector of sgm (host float32) over slices [z0, z1)."""
+        self.items.append(("bpu", target, label, dict(o=o, sgm=sgm, z0=z0, z1=z1, got=got)))
+
+    def run(self):
+        """Evaluate every check (float64, all host threads); returns the seconds spent."""
+        from oracle import cpu_ref
+        from reconstruction_program_taichi_gb300 import geometry
+        t0 = time.perf_counter()
+        cache = {}
+        for kind, target, label, a in self.items:
+            o = a["o"]
+            if kind == "fdk":
+                u, v, ang = geometry.fbp_arrays(o)
+                g = cpu_ref.geom_from_config(o, u, v)
+                key = ("fdk", id(a["sgm"]), id(a["taps"]), a["z0"], a["z1"])
+                if key not in cache:
+                    cache[key] = cpu_ref.fdk_slab_f64(g, ang, a["sgm"], a["taps"], a["z0"], a["z1"])
+                ref, rows = cache[key]
+                e = cpu_ref.errors(a["got"], ref)
+                e["zero_pattern_mismatches"] = int(np.sum((a["got"] == 0) != (ref == 0)))
+                e["sample"] = (f"slices {a['z0']}-{a['z1'] - 1} of {g.nz}, every voxel of them, every view "
+                               f"(detector rows {rows[0]}-{rows[1] - 1}, all that the slab reads)")
+            elif kind == "fp":
+                if a["ir"]:
+                    u, v, ang = geometry.ir_arrays(o)
+                    k = geometry.count_steps_ir(o.img_dim, o.img_dim_z, o.img_pix_size, o.img_voxel_height,
+                                                o.fpj_step_size, o.source_isocenter_dis)
+                    cz = np.asarray(o.array_img_center_z, dtype=np.float64)
+                    assert np.all(cz == cz[0]), "per-view image centres are not checked here"
+                    g = cpu_ref.geom_from_config(o, u, v, k).copy(cz=float(cz[0]))
+                else:
+                    u, v, ang = geometry.fpj_arrays(o)
+                    k = geometry.count_steps_v3(o.img_dim, o.img_dim_z, o.img_pix_size, o.img_voxel_height,
+                                                o.fpj_step_size)
+                    g = cpu_ref.geom_from_config(o, u, v, k)
+                g = g.copy(nv=o.det_elem_count_vertical_actual)
+                key = ("fp", id(a["vol"]), a["ir"], tuple(a["views"]))
+                if key not in cache:
+                    cache[key] = cpu_ref.fp_views_f64(g, ang, u, v, a["vol"], a["views"])
+                ref = cache[key]
+                if a["mask"] is not None:
+                    ref = np.where(a["mask"] == 1, ref, 0.0)
+                e = cpu_ref.errors(a["got"], ref)
+                e["sample"] = f"views {a['views']} of {g.views}, every ray"
+            else:
+                u, v, ang = geometry.ir_arrays(o)
+                g = cpu_ref.geom_from_config(o, u, v)
+                key = ("bpu", id(a["sgm"]), a["z0"], a["z1"])
+                if key not in cache:
+                    cache[key] = cpu_ref.bp_unmatched_slab_f64(g, ang, o.array_img_center_z, a["sgm"], a["z0"],
+                                                               a["z1"])
+                ref, rows = cache[key]
+                e = cpu_ref.errors(a["got"], ref)
+                e["zero_pattern_mismatches"] = int(np.sum((a["got"] == 0) != (ref == 0)))
+                e["sample"] = f"slices {a['z0']}-{a['z1'] - 1} of {g.nz}, every view"
+            target.setdefault("vs_fp64", {})[label] = {k_: (float(f"{v_:.4g}") if isinstance(v_, float) else v_)
+                                                       for k_, v_ in e.items()}
+        return time.perf_counter() - t0
+
+
 def run_reference(args, w):
+    """The reference arm: the reference's CPU implementation of the step (its Taichi
+    kernels need Taichi, which cannot be installed here, so the OpenMP C restatement
+    of those kernels, float32 like Taichi) on all host threads, each step a bounded
+    sample (filter rows, a block of backprojection views, evenly spaced forward-
+    projection views) extrapolated to the whole step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -880,7 +1173,7 @@ def run_reference(args, w):
         cpu_sample(w, o, 2, 1, 64)
     times = []
     for _ in range(args.steps):
-        t, thr, desc, parts = cpu_sample(w, o, 8, 1, 256)
+        t, thr, desc, parts = cpu_sample(w, o, 8, 2, 256)
         times.append(t)
     t = float(np.mean(times))
     units = 2.0 * w["nx"] * w["nx"] * w["nz"] * w["views"]
@@ -890,7 +1183,9 @@ def run_reference(args, w):
             "ms_per_step": round(t * 1e3, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (uniform random sinogram / volume; cost is data independent)",
             "config": {"workload": f"FDK+FP {w['nx']}x{w['nx']}x{w['nz']} vol, {w['views']} views, "
-                                   f"{w['nu']}x{w['nv']} det (bounded sample per step, extrapolated)"},
+                                   f"{w['nu']}x{w['nv']} det; per step a bounded sample (256 filter rows, 8 "
+                                   f"backprojection views, 2 evenly spaced forward-projection views), "
+                                   f"extrapolated to the full step"},
             "cpu_baseline": {"value": round(value, 4), "unit": "GUPS", "cores": thr, "kind": "port", "sample": desc},
             "e2e": {"value": round(value, 4), "unit": "GUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's Taichi kernels cannot run here (no taichi); this is the OpenMP C restatement "
@@ -912,9 +1207,10 @@ def main():
     ap.add_argument("--no-cgls", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--only", default=None, choices=["cgls", "adjoint"],
+    ap.add_argument("--only", default=None, choices=["cgls", "adjoint", "cg_step", "helical"],
                     help="cgls: only the IRN-CGLS-TV section; adjoint: only the projector / exact-adjoint "
-                         "pair (short runs for ncu captures of their kernels)")
+                         "pair; cg_step: one reweighted CG solve of 3 iterations at 512x512x64 / 360 views; "
+                         "helical: one helical FBP (short runs for ncu captures of their kernels)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -925,6 +1221,16 @@ def main():
         torch.cuda.set_device(dev)
         out = irn_bench(dev, torch.cuda.current_stream(dev), torch.cuda.synchronize)
         print(json.dumps({"irn_cgls_tv": out}))
+    elif args.only == "cg_step":
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"cg_step_ms": cg_step_bench(dev)}))
+    elif args.only == "helical":
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"helical_ms": helical_once(dev)}))
     elif args.only == "adjoint":
         import torch
         dev = torch.device("cuda", 0)

@@ -334,7 +334,10 @@ int mct_dot_f64(const float* a, const float* b, int64_t n, double* partials, dou
  * The per-block partial sums live in a fixed 512 KiB device array inside the
  * library, held by every GPU that loads it until the process exits, so
  * n <= 134,217,728; larger n returns MCT_E_INVALID.  The first call on a device
- * looks up that array's address (make it before any stream capture).  All calls
+ * looks up that array's address (make it before any stream capture) and keeps it for
+ * the process: it stays valid in the device's primary context (the runtime API's
+ * context) until that context is destroyed, so after a cudaDeviceReset, or from
+ * another context on the same device, use mct_dot_f64 instead.  All calls
  * share the array: calls that overlap on the GPU race and must be serialised by the
  * caller.  No cudaMalloc/cudaFree is made. */
 int mct_dot_f64_noalloc(const float* a, const float* b, int64_t n, double* result, void* stream);

@@ -81,7 +81,9 @@ noalloc_dot_finish_kernel(const double* __restrict__ partials, int nparts, doubl
 std::mutex g_na_mutex;
 double* g_na_ptr[NA_MAX_DEVICES] = {nullptr};
 
-// Device address of the scratch on the current device (looked up once per device).
+// Device address of the scratch on the current device, looked up once per device and
+// kept: it belongs to the device's primary context and is not refreshed after a
+// cudaDeviceReset (the header says so).
 int noalloc_scratch(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

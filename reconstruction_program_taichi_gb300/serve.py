@@ -9,10 +9,10 @@ Model
   * Requests of the same kind, storage precision (and CGLS iteration count) whose
     parsed configs agree in every attribute that can change the result (a digest of
     the whole parsed config, file names aside) share a *slot class*.  A slot owns
-    device buffers for up to `batch` requests, a CUDA stream, and CUDA graphs captured
-    once per occupancy (weight -> filter -> pack -> backproject for each sinogram, or
-    the full CGLS loop for each request), so a batch of k requests executes as one
-    graph launch that runs exactly k reconstructions.
+    device buffers for up to `batch` requests, a CUDA stream, and one CUDA graph per
+    member captured once (weight -> filter -> pack -> backproject of its sinogram, or its
+    whole CGLS solve), so a batch of k requests executes as k graph launches and runs
+    exactly k reconstructions.
   * Admission is continuous: a scheduler thread takes pending requests in arrival
     order, groups those whose slot class matches (up to `batch`), and starts them on
     a free slot; new slots are created while the HBM budget allows, and a slot is
@@ -150,24 +150,29 @@ class _Request:
 _IR_STORAGE = {"f32": "float32", "bf16": "bfloat16", "f16": "float16"}
 
 
-def _graph_capture(stream, body, pool):
-    """Warm body() on stream (first-call set-up and cached buffers outside the
-    capture), then capture it into a CUDA graph drawing on the shared memory pool."""
+def _capture_members(stream, bodies):
+    """One CUDA graph per batch member: body(i) is run once on stream for its
+    first-call set-up (cached buffers are created outside any capture), then every
+    member's body is captured into its own graph.  The graphs draw on one memory pool,
+    which is safe because a slot replays them one after another on its stream."""
     with torch.cuda.stream(stream):
-        body()
+        bodies[0]()
     stream.synchronize()
-    g = torch.cuda.CUDAGraph()
-    # thread-local capture: other slots keep running on their own threads and streams
-    with torch.cuda.graph(g, pool=pool, stream=stream, capture_error_mode="thread_local"):
-        body()
-    return g
+    pool = torch.cuda.graph_pool_handle()
+    graphs = []
+    for body in bodies:
+        g = torch.cuda.CUDAGraph()
+        # thread-local capture: other slots keep running on their own threads and streams
+        with torch.cuda.graph(g, pool=pool, stream=stream, capture_error_mode="thread_local"):
+            body()
+        graphs.append(g)
+    return graphs
 
 
 class _FbpSlot:
-    """Static buffers for `batch` FBP reconstructions of one slot class and one
-    captured graph per occupancy: a batch of k requests replays the graph of its first
-    k members only, so no member recomputes a stale input.  The graphs share one memory
-    pool (a slot runs one batch at a time).  The mixed-precision path (16-bit storage)
+    """Static buffers for `batch` FBP reconstructions of one slot class and one captured
+    graph per member: a batch of k requests replays the graphs of its first k members,
+    so no member recomputes a stale input.  The mixed-precision path (16-bit storage)
     uses the two-part tensor-core filter and 16-bit backprojection coefficients."""
 
     def __init__(self, obj, batch, storage, device, use_graph):
@@ -183,22 +188,18 @@ class _FbpSlot:
                         for _ in range(batch)]
         self.host_out = [torch.empty(self.pipes[0].dg.vol_shape, dtype=torch.float32, pin_memory=True)
                          for _ in range(batch)]
-        self.graphs = {}
+        self.graphs = []
         self.last_used = time.perf_counter()
         self.nbytes = sum(p.weighted.numel() * 4 + p.filtered.numel() * 4 + p.packed.numel() + p.vol.numel() * 4
                           + (p.tc._buf.numel() if p.tc is not None else 0)
                           for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
-            pool = torch.cuda.graph_pool_handle()
-            for k in range(1, batch + 1):
-                self.graphs[k] = _graph_capture(self.stream, lambda k=k: self._body(k), pool)
+            self.graphs = _capture_members(self.stream, [lambda i=i: self._member(i) for i in range(batch)])
 
-    def _body(self, k):
-        for p, i, o in zip(self.pipes[:k], self.inp[:k], self.out[:k]):
-            p.run(i, out=o)
+    def _member(self, i):
+        self.pipes[i].run(self.inp[i], out=self.out[i])
 
     def run(self, reqs):
-        k = len(reqs)
         dev_out = []
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
@@ -206,10 +207,11 @@ class _FbpSlot:
                     self.inp[i].copy_(r.sgm)
                 else:
                     self.inp[i].copy_(torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)))
-            if k in self.graphs:
-                self.graphs[k].replay()
-            else:
-                self._body(k)
+            for i in range(len(reqs)):
+                if self.graphs:
+                    self.graphs[i].replay()
+                else:
+                    self._member(i)
             for i, r in enumerate(reqs):
                 if r.on_device:
                     dev_out.append(self.out[i].clone())
@@ -231,8 +233,8 @@ class _CglsSlot:
     weights, as submit_cgls describes) for up to `batch` requests of one slot class.
     The members share one IrSystem (geometry tables, effective ray map, projector
     workspace, packed operand), which is safe because they run one after another on
-    the slot's stream; each member has static input and output buffers.  One graph is
-    captured per occupancy, so a batch of k requests is one graph launch of k solves."""
+    the slot's stream; each member has static input and output buffers and its own
+    captured graph of the whole solve, so a batch of k requests is k graph launches."""
 
     def __init__(self, obj, n_iter, storage, batch, device, use_graph):
         from .ir import IrSystem
@@ -258,29 +260,26 @@ class _CglsSlot:
         # temporaries of one solve (masked sinogram, P^T b, d, r, x, q)
         self.nbytes = (batch * (nsgm + 2 * nvol) + nvol + 2 * nsgm + _fp_workspace_bytes(dg, self.sys.fp_dtype)
                        + 2 * 4 * nsgm + nsgm + 5 * nvol)
-        self.graphs = {}
+        self.graphs = []
         if use_graph:
-            pool = torch.cuda.graph_pool_handle()
-            for k in range(1, batch + 1):
-                self.graphs[k] = _graph_capture(self.stream, lambda k=k: self._body(k), pool)
+            self.graphs = _capture_members(self.stream, [lambda i=i: self._member(i) for i in range(batch)])
 
-    def _body(self, k):
+    def _member(self, i):
         sy = self.sys
-        for i in range(k):
-            sy.bpb = sy.bp_b(self.sgm[i])
-            x = sy.cgls(self.x0[i], [], [(self.lr, self.wr)], self.n_iter)
-            self.out[i].copy_(x)
+        sy.bpb = sy.bp_b(self.sgm[i])
+        x = sy.cgls(self.x0[i], [], [(self.lr, self.wr)], self.n_iter)
+        self.out[i].copy_(x)
 
     def run(self, reqs):
-        k = len(reqs)
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
                 self.sgm[i].copy_(_to_device(r.sgm, self.device))
                 self.x0[i].copy_(_to_device(r.x0, self.device))
-            if k in self.graphs:
-                self.graphs[k].replay()
-            else:
-                self._body(k)
+            for i in range(len(reqs)):
+                if self.graphs:
+                    self.graphs[i].replay()
+                else:
+                    self._member(i)
             outs = [self.out[i].clone() if r.on_device else self.out[i].cpu().numpy() for i, r in enumerate(reqs)]
         self.stream.synchronize()
         self.last_used = time.perf_counter()

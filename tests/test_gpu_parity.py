@@ -303,6 +303,71 @@ def test_fp_adjoint_vs_oracle(kw, cuda):
         assert rel_l2(a[inner], ref[inner]) < TOL
 
 
+def _rays_near_faces(o, dg, eps=1e-3):
+    """[rows, views, cols] flags of the rays with a sample within eps voxel of a volume
+    face on some axis (where float32 and float64 sample positions can take the
+    reference's inside test different ways); positions as the oracle's march computes
+    them (float64)."""
+    u, v, ang = dg.host["u"], dg.host["v"], dg.host["angles"]
+    nx, nz, px, pz = o.img_dim, o.img_dim_z, o.img_pix_size, o.img_voxel_height
+    sid, sdd = o.source_isocenter_dis, o.source_det_dis
+    rows, nu = o.det_elem_count_vertical, len(u)
+    vd = (2 * px ** 2 + pz ** 2) ** 0.5
+    l_min = sid - (2 * (nx * px) ** 2 + (nz * pz) ** 2) ** 0.5 / 2.0
+    x0 = -(nx - 1.0) / 2.0 * px + o.img_center_x
+    y0 = (nx - 1.0) / 2.0 * px + o.img_center_y
+    ks = np.arange(dg.geom.fp_steps, dtype=np.float64)[:, None, None]
+    out = np.zeros(dg.sgm_shape, dtype=bool)
+    for j in range(o.view_num):
+        sz, ux, uy, uz, _ = P._ray_dirs(u, v, rows, sid, sdd, o.curved_dect, dg.geom.fp_z_per_view, j)
+        lk = ks * o.fpj_step_size * vd + l_min
+        x, y, z = sid + ux * lk, uy * lk, sz + uz * lk
+        cb, sb = math.cos(ang[j]), math.sin(ang[j])
+        fx = (x * cb - y * sb - x0) / px
+        fy = (y * cb + x * sb - y0) / (-px)
+        fz = (z - (-(nz - 1.0) / 2.0 * pz + o.array_img_center_z[j])) / pz
+        near = np.zeros(fx.shape, dtype=bool)
+        for f, n in ((fx, nx), (fy, nx), (fz, nz)):
+            near |= (np.abs(f) < eps) | (np.abs(f - (n - 1)) < eps)
+        inside = (fx > -1) & (fx < nx) & (fy > -1) & (fy < nx) & (fz > -1) & (fz < nz)
+        out[:, j, :] = (near & inside).any(axis=0)
+    return out
+
+
+@pytest.mark.parametrize("kw", [{}, {"CurvedDetector": True}, {"ImageDimension": 41,
+                                                                "DetectorElementCountHorizontal": 77}])
+def test_fp_adjoint_face_voxels_vs_oracle(kw, cuda):
+    """The adjoint's edge branches (the gather of voxels on the volume faces, which some
+    of their 8 cells do not exist for) held to the plain 1e-4 bound over the whole volume:
+    rays that come within 1e-3 voxel of a face, where float32 and float64 positions can
+    flip the reference's inside test, are masked out of both."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    o = _cone_obj(views=24, **kw)
+    dg = geometry.fpj_geometry(o)
+    rng = np.random.default_rng(18)
+    y = rng.uniform(0, 1, dg.sgm_shape).astype(np.float32)
+    near = _rays_near_faces(o, dg)
+    mask = ((rng.uniform(0, 1, dg.sgm_shape) > 0.2) & ~near).astype(np.float32)
+    assert 0.001 < near.mean() < 0.2  # few rays pass that close to a face
+    yt, mt = torch.from_numpy(y).cuda(), torch.from_numpy(mask).cuda()
+    u, v, ang = dg.host["u"], dg.host["v"], dg.host["angles"]
+    ref = np.zeros(dg.vol_shape, dtype=np.float64)
+    for j in range(o.view_num):
+        P.march(None, j, ang, u, v, nx=o.img_dim, nz=o.img_dim_z, px=o.img_pix_size, pz=o.img_voxel_height,
+                cx=o.img_center_x, cy=o.img_center_y, cz_view=o.array_img_center_z[j], sid=o.source_isocenter_dis,
+                sdd=o.source_det_dis, step=o.fpj_step_size, cone_beam=True, curved=o.curved_dect,
+                zpv=dg.geom.fp_z_per_view, rows=o.det_elem_count_vertical, K=dg.geom.fp_steps,
+                mask=mask[:, j, :], mode="adjoint", ray_values=y[:, j, :], out=ref)
+    faces = np.ones(dg.vol_shape, dtype=bool)
+    faces[1:-1, 1:-1, 1:-1] = False
+    assert np.abs(ref[faces]).sum() > 0.05 * np.abs(ref).sum()  # the faces carry weight
+    for ws in (True, None):
+        got = ops.fp_adjoint(dg, yt, mask=mt, workspace=ws).cpu().numpy()
+        assert rel_l2(got, ref) < TOL, ws
+        assert rel_l2(got[faces], ref[faces]) < TOL, ws
+
+
 def test_fp_adjoint_dot_product(cuda):
     """<A x, y> = <x, A^T y> to 1e-5 relative (float64 accumulation of the sums)."""
     import torch

@@ -136,9 +136,9 @@ def test_file_inputs_and_outputs(tmp_path, cuda):
 
 
 def test_batched_cgls_requests_match_alone(cuda):
-    """Several CGLS requests of one class run as one batch (one graph launch of k
-    solves on a slot that shares the projector workspace between members): each result
-    equals the request run alone."""
+    """Several CGLS requests of one class run as one batch (a captured graph per member
+    on a slot that shares the projector workspace between members): each result equals
+    the request run alone."""
     from reconstruction_program_taichi_gb300.serve import ReconServer
     rng = np.random.default_rng(31)
     cg = _cgls_obj(n=24, nz=8, nu=48, nv=12, views=30, DetectorElementHeight=1.0)
@@ -148,7 +148,7 @@ def test_batched_cgls_requests_match_alone(cuda):
     alone = [srv.submit_cgls(cg, s, x, 4).result(timeout=120) for s, x in zip(sg, x0)]
     srv.close()
     srv = ReconServer(batch=4, max_slots_per_class=1)
-    srv.submit_cgls(cg, sg[0], x0[0], 4).result(timeout=120)  # builds the slot (its 4 graphs)
+    srv.submit_cgls(cg, sg[0], x0[0], 4).result(timeout=120)  # builds the slot (a graph per member)
     futs = [srv.submit_cgls(cg, s, x, 4) for s, x in zip(sg, x0)]
     got = [f.result(timeout=120) for f in futs]
     st = srv.stats()
@@ -159,13 +159,13 @@ def test_batched_cgls_requests_match_alone(cuda):
 
 
 def test_partial_batch_runs_only_its_members(cuda):
-    """A batch of k requests on a slot of `batch` members replays the graph of its
-    first k members: the other members' outputs are not recomputed."""
+    """A batch of k requests on a slot of `batch` members replays the graphs of its
+    first k members only: the other members' outputs are not recomputed."""
     import torch
     from reconstruction_program_taichi_gb300.serve import _FbpSlot, _Request
     o = _cone_obj(n=40, nz=16, nu=72, nv=24, views=60)
     slot = _FbpSlot(o, 3, "f32", torch.device("cuda"), use_graph=True)
-    assert sorted(slot.graphs) == [1, 2, 3]
+    assert len(slot.graphs) == 3
     rng = np.random.default_rng(33)
     s = rng.uniform(0, 1, (24, 60, 72)).astype(np.float32)
     for t in slot.out[1:]:
