@@ -642,15 +642,20 @@ def piccs_bench(dev, stream, barrier, checks=None):
                             indexing="ij")
     fov = (yy ** 2 + xx ** 2 <= (0.95 * n_ / 2) ** 2).expand_as(truth).contiguous()
     out["prior_rmse_vs_target"] = rmse(prior, truth, fov)
+    # (result key, gather storage, iterate storage); "bf16_iterates" is the configuration's
+    # own precision plan: BF16 iterates, float64 reductions
+    variants = (("float32", "float32", "float32"), ("bfloat16", "bfloat16", "float32"),
+                ("float16", "float16", "float32"), ("bf16_iterates", "bfloat16", "bfloat16"))
     try:
-        for storage in ("float32", "bfloat16", "float16"):
+        for key, storage, iterate in variants:
             cfg = make_config(C4)
             cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 30, "NumberOfIterations": 8,
-                        "Alpha": 0.5, "PriorImageFile": prior_file, "StoragePrecision": storage})
+                        "Alpha": 0.5, "PriorImageFile": prior_file, "StoragePrecision": storage,
+                        "IterateStorage": iterate})
             ir = Mgfbp_ir_piccs(cfg, device=dev, verbose=False)
             sy = ir.system
             sgm = noisy(ops.project_ellipsoids(sy.dg, ell_t), C4["photons"], C4["seed"] + 7)
-            pr = torch.from_numpy(ir.img_prior).to(dev)
+            pr = torch.from_numpy(ir.img_prior.copy()).to(dev)
             sy.bpb = sy.bp_b(sgm)
             sy.cgls(pr, [], [(1e-3, torch.ones_like(pr))], 2)  # warm-up
             barrier()
@@ -662,14 +667,16 @@ def piccs_bench(dev, stream, barrier, checks=None):
             barrier()
             n = sy.ptp_calls - calls0
             sec = e0.elapsed_time(e1) / 1e3
-            out[storage] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
-                            "rmse_vs_phantom": rmse(x, truth, fov), "finite": bool(torch.isfinite(x).all())}
-            ir_operator_checks(checks, out[storage], ir, sy, sgm, truth, C4["nz"] // 2)
+            out[key] = {"s_total": round(sec, 3), "ptp": n, "s_per_iter": round(sec / n, 5),
+                        "rmse_vs_phantom": rmse(x, truth, fov), "finite": bool(torch.isfinite(x).all()),
+                        "gather_storage": storage, "iterate_storage": iterate}
+            if key != "bf16_iterates":
+                ir_operator_checks(checks, out[key], ir, sy, sgm, truth, C4["nz"] // 2)
             del ir, sy, sgm, x, pr
     finally:
         os.remove(prior_file)
     f = out["float32"]
-    for k in ("bfloat16", "float16"):
+    for k in ("bfloat16", "float16", "bf16_iterates"):
         out[k]["speedup"] = round(f["s_total"] / out[k]["s_total"], 3)
         out[k]["rmse_ratio"] = round(out[k]["rmse_vs_phantom"] / f["rmse_vs_phantom"], 5)
     return out
@@ -1207,8 +1214,9 @@ def main():
     ap.add_argument("--no-cgls", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--only", default=None, choices=["cgls", "adjoint", "cg_step", "helical"],
-                    help="cgls: only the IRN-CGLS-TV section; adjoint: only the projector / exact-adjoint "
+    ap.add_argument("--only", default=None, choices=["cgls", "piccs", "adjoint", "cg_step", "helical"],
+                    help="cgls: only the IRN-CGLS-TV section; piccs: only the IRN-CGLS-PICCS section; "
+                         "adjoint: only the projector / exact-adjoint "
                          "pair; cg_step: one reweighted CG solve of 3 iterations at 512x512x64 / 360 views; "
                          "helical: one helical FBP (short runs for ncu captures of their kernels)")
     args = ap.parse_args()
@@ -1221,6 +1229,12 @@ def main():
         torch.cuda.set_device(dev)
         out = irn_bench(dev, torch.cuda.current_stream(dev), torch.cuda.synchronize)
         print(json.dumps({"irn_cgls_tv": out}))
+    elif args.only == "piccs":
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        out = piccs_bench(dev, torch.cuda.current_stream(dev), torch.cuda.synchronize)
+        print(json.dumps({"irn_cgls_piccs": out}))
     elif args.only == "cg_step":
         import torch
         dev = torch.device("cuda", 0)

@@ -227,6 +227,13 @@ size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype);
 int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
                    void* workspace, int32_t dtype, void* stream);
 
+/* mct_fp_storage with a volume stored as vol_dtype: MCT_F32 is mct_fp_storage; MCT_BF16
+ * (bf16 CG iterates; cone beam with a workspace) is read by the copy kernels only, so
+ * the projector runs as for a float32 volume holding the same values.  No counterpart
+ * in the reference (its iterates are float32). */
+int mct_fp_storage_in(const mct_geom* g, const mct_tables* t, const void* vol, int32_t vol_dtype,
+                      const float* mask, float* sgm, void* workspace, int32_t dtype, void* stream);
+
 /* Exact transpose of mct_fp: vol += P^T sgm (vol is accumulated, not cleared).
  * No counterpart in the reference (its CGLS pairs mct_fp with the unmatched
  * backprojector below); used for matched-adjoint CGLS and autograd. */
@@ -351,6 +358,31 @@ int mct_cgls_update(int64_t n, const double* rr, const double* dq, float* x, flo
                     const float* d, const float* q, double* partials, double* rr_new, void* stream);
 int mct_cgls_direction(int64_t n, const double* rr, const double* rr_new, const float* r, float* d,
                        void* stream);
+
+/* ---- the CG vector operations on float32 or bf16 volumes (bf16 iterate storage).
+ * No counterpart in the reference (its iterates are float32 NumPy arrays).  Elements
+ * are widened to float32 for the arithmetic, reductions accumulate in float64, and
+ * stored results are rounded to the volume's type; the float64 sums use the stored
+ * values (|r|^2 of the rounded r, <d, q> of the rounded q).  dtype, x_dtype, vec_dtype
+ * and vol_dtype are MCT_F32 or MCT_BF16. */
+
+/* mct_bp_ref_unmatched_packed writing vol as vol_dtype (MCT_BF16: axial view mode, cone
+ * beam). */
+int mct_bp_ref_unmatched_packed_out(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
+                                    void* vol, int32_t vol_dtype, void* stream);
+/* mct_tv_weights of x stored as x_dtype (wr stays float32). */
+int mct_tv_weights_t(const mct_geom* g, const void* x, int32_t x_dtype, float beta, float* wr, void* stream);
+/* out = a*out_in + s * D^T W D x on vec_dtype volumes (wr float32); with partials and dot
+ * (both or neither) also *dot = sum x[i]*out[i] in float64, as mct_dtwd_dot. */
+int mct_dtwd_t(const mct_geom* g, const void* x, const float* wr, float s, const void* out_in, float a, void* out,
+               int32_t vec_dtype, double* partials, double* dot, void* stream);
+/* mct_dot_f64, mct_cgls_update and mct_cgls_direction on dtype volumes. */
+int mct_dot_f64_t(const void* a, const void* b, int64_t n, int32_t dtype, double* partials, double* result,
+                  void* stream);
+int mct_cgls_update_t(int64_t n, int32_t dtype, const double* rr, const double* dq, void* x, void* r,
+                      const void* d, const void* q, double* partials, double* rr_new, void* stream);
+int mct_cgls_direction_t(int64_t n, int32_t dtype, const double* rr, const double* rr_new, const void* r, void* d,
+                         void* stream);
 
 /* ---------------------------------------------------------------- synthetic data */
 

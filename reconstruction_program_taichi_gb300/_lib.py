@@ -110,6 +110,13 @@ SIGNATURES = {
     "mct_cgls_update": (ctypes.c_int, [_i64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mct_cgls_direction": (ctypes.c_int, [_i64, _P, _P, _P, _P, _P]),
     "mct_project_ellipsoids": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P]),
+    "mct_fp_storage_in": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P, _P, _i32, _P]),
+    "mct_bp_ref_unmatched_packed_out": (ctypes.c_int, [_G, _T, _P, _i32, _P, _i32, _P]),
+    "mct_tv_weights_t": (ctypes.c_int, [_G, _P, _i32, _f32, _P, _P]),
+    "mct_dtwd_t": (ctypes.c_int, [_G, _P, _P, _f32, _P, _f32, _P, _i32, _P, _P, _P]),
+    "mct_dot_f64_t": (ctypes.c_int, [_P, _P, _i64, _i32, _P, _P, _P]),
+    "mct_cgls_update_t": (ctypes.c_int, [_i64, _i32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mct_cgls_direction_t": (ctypes.c_int, [_i64, _i32, _P, _P, _P, _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -483,6 +483,13 @@ def parse_ir(self, cfg):
     if dp not in ("float32", "bfloat16", "float16"):
         _err("SinogramPrecision can only be float32, bfloat16 or float16!")
     self.sinogram_precision = dp
+    # storage of the CG iterates x, r, d, q between kernels (an addition): "float32"
+    # (default) or "bfloat16" (arithmetic in float32, reductions in float64, stored
+    # values rounded; cone beam with the reference backprojector in the axial view mode)
+    ip = cfg.get("IterateStorage", "float32")
+    if ip not in ("float32", "bfloat16"):
+        _err("IterateStorage can only be float32 or bfloat16!")
+    self.iterate_storage = ip
 
 
 def parse_piccs(self, cfg):

@@ -57,6 +57,25 @@ double div_factor(const mct_geom& g);
 
 __device__ __forceinline__ float bf16_to_f32(__nv_bfloat16 h) { return __bfloat162float(h); }
 
+// Elements of float32 or bf16 volumes (bf16 iterate storage): loads widen to float32,
+// stores round to nearest.
+template <typename T>
+__device__ __forceinline__ float ldv(const T* p, int64_t i);
+template <>
+__device__ __forceinline__ float ldv<float>(const float* p, int64_t i) { return p[i]; }
+template <>
+__device__ __forceinline__ float ldv<__nv_bfloat16>(const __nv_bfloat16* p, int64_t i) {
+    return __bfloat162float(p[i]);
+}
+template <typename T>
+__device__ __forceinline__ void stv(T* p, int64_t i, float v);
+template <>
+__device__ __forceinline__ void stv<float>(float* p, int64_t i, float v) { p[i] = v; }
+template <>
+__device__ __forceinline__ void stv<__nv_bfloat16>(__nv_bfloat16* p, int64_t i, float v) {
+    p[i] = __float2bfloat16_rn(v);
+}
+
 // Read-only, L1-cached loads.
 template <typename T>
 __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }

@@ -383,10 +383,11 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
 }
 
 // Largest |v| of the volume as float bits into *maxbits (zeroed by the caller).
-__global__ void vol_absmax_kernel(int64_t n, const float* __restrict__ v, uint32_t* __restrict__ maxbits) {
+template <typename TIN>
+__global__ void vol_absmax_kernel(int64_t n, const TIN* __restrict__ v, uint32_t* __restrict__ maxbits) {
     uint32_t m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        m = max(m, __float_as_uint(v[i]) & 0x7fffffffu);
+        m = max(m, __float_as_uint(ldv(v, i)) & 0x7fffffffu);
     m = __reduce_max_sync(0xffffffffu, m);
     if ((threadIdx.x & 31) == 0) atomicMax(maxbits, m);
 }
@@ -394,8 +395,8 @@ __global__ void vol_absmax_kernel(int64_t n, const float* __restrict__ v, uint32
 // 16-bit cell copies (layout above; float16 cells hold v * 2^e, see f16_scale_exp): cx[z][y][x] and cy[z][x][y] both hold the cell at
 // voxel (z, y, x); corners outside the volume are 0 (no in-volume sample uses them).
 // 32x32 tiles, the transposed copy through shared memory.
-template <bool F16>
-__global__ void cell16_kernel(int nx, int nz, const float* __restrict__ v, uint4* __restrict__ cx,
+template <bool F16, typename TIN = float>
+__global__ void cell16_kernel(int nx, int nz, const TIN* __restrict__ v, uint4* __restrict__ cx,
                               uint4* __restrict__ cy, const uint32_t* __restrict__ f16_max) {
     __shared__ uint4 tile[32][33];
     const int64_t plane = (int64_t)nx * nx;
@@ -403,7 +404,7 @@ __global__ void cell16_kernel(int nx, int nz, const float* __restrict__ v, uint4
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
     const float sc = F16 ? ldexpf(1.0f, f16_scale_exp(*f16_max)) : 1.0f;
     auto at = [&](int zz, int yy, int xx) -> float {
-        return (zz < nz && yy < nx && xx < nx) ? v[zz * plane + (int64_t)yy * nx + xx] * sc : 0.0f;
+        return (zz < nz && yy < nx && xx < nx) ? ldv(v, zz * plane + (int64_t)yy * nx + xx) * sc : 0.0f;
     };
     auto rb = [](float a) {
         return F16 ? __half2float(__float2half_rn(a)) : __bfloat162float(__float2bfloat16_rn(a));
@@ -435,14 +436,15 @@ __global__ void cell16_kernel(int nx, int nz, const float* __restrict__ v, uint4
 // V[z+1][y][x], V[z][y][x+1], V[z+1][y][x+1]} (fast axis y); corners outside the volume
 // are 0 (no in-volume sample uses them).  32x32 tiles, the transposed copy through
 // shared memory.
-__global__ void quad32_kernel(int nx, int nz, const float* __restrict__ v, float4* __restrict__ cx,
+template <typename TIN = float>
+__global__ void quad32_kernel(int nx, int nz, const TIN* __restrict__ v, float4* __restrict__ cx,
                               float4* __restrict__ cy) {
     __shared__ float4 tile[32][33];
     const int64_t plane = (int64_t)nx * nx;
     const int z = blockIdx.z;
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
     auto at = [&](int zz, int yy, int xx) -> float {
-        return (zz < nz && yy < nx && xx < nx) ? v[zz * plane + (int64_t)yy * nx + xx] : 0.0f;
+        return (zz < nz && yy < nx && xx < nx) ? ldv(v, zz * plane + (int64_t)yy * nx + xx) : 0.0f;
     };
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
         const int y = y0 + i, x = x0 + threadIdx.x;
@@ -794,11 +796,20 @@ size_t mct_fp_storage_workspace_size(const mct_geom* g, int32_t dtype) {
     return 2 * (size_t)g->nz * g->nx * g->nx * sizeof(uint4) + (dtype == MCT_F16 ? 16 : 0);
 }
 
-int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
-                   void* workspace, int32_t dtype, void* stream) {
+}  // extern "C"
+
+namespace {
+// The projector's launches with a float32 or bf16 volume (TIN); the bf16 volume is read
+// only by the copy kernels, so it needs cone beam and a workspace.
+template <typename TIN>
+int fp_storage_impl(const mct_geom* g, const mct_tables* t, const TIN* vol_in, const float* mask, float* sgm,
+                    void* workspace, int32_t dtype, void* stream) {
+    const float* vol = reinterpret_cast<const float*>(vol_in);  // read as float32 only when TIN is float
+    constexpr bool kIn32 = std::is_same<TIN, float>::value;
     FpParams p;
     MCT_TRY(make_params(g, p, "mct_fp"));
     MCT_REQUIRE(t && t->angles && t->u && t->v && vol && sgm, "mct_fp: NULL buffer");
+    MCT_REQUIRE(kIn32 || (p.cone && workspace), "mct_fp: a bf16 volume needs cone beam and a workspace");
     MCT_REQUIRE(!p.pmat || (t->pmat_a && t->pmat_xs), "mct_fp: projection-matrix tables missing");
     MCT_REQUIRE(workspace != (void*)vol, "mct_fp: workspace aliases the volume");
     MCT_REQUIRE(((uintptr_t)workspace & 15) == 0, "mct_fp: workspace must be 16-byte aligned");
@@ -828,7 +839,7 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
     if (p.cone && workspace && dtype == MCT_BF16) {
         uint4* cx = static_cast<uint4*>(workspace);
         uint4* cy = cx + n;
-        cell16_kernel<false><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy, nullptr);
+        cell16_kernel<false><<<tg, tb, 0, s>>>(g->nx, g->nz, vol_in, cx, cy, nullptr);
         MCT_TRY(launched("cell16_kernel"));
         fp_kernel<true, true, uint4><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
                                                             nullptr, cx, cy, mask, sgm, nullptr);
@@ -842,9 +853,9 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
             return MCT_E_CUDA;
         }
         const int64_t blocks = ((int64_t)n + 255) / 256;
-        vol_absmax_kernel<<<(int)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, s>>>((int64_t)n, vol, vmax);
+        vol_absmax_kernel<<<(int)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, s>>>((int64_t)n, vol_in, vmax);
         MCT_TRY(launched("vol_absmax_kernel"));
-        cell16_kernel<true><<<tg, tb, 0, s>>>(g->nx, g->nz, vol, cx, cy, vmax);
+        cell16_kernel<true><<<tg, tb, 0, s>>>(g->nx, g->nz, vol_in, cx, cy, vmax);
         MCT_TRY(launched("cell16_kernel"));
         fp_kernel<true, true, h16x8><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs, vol,
                                                             nullptr, reinterpret_cast<const h16x8*>(cx),
@@ -852,11 +863,12 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
     } else if (p.cone && workspace) {
         Quad16* cx = static_cast<Quad16*>(workspace);
         Quad16* cy = cx + n;
-        quad32_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, reinterpret_cast<float4*>(cx), reinterpret_cast<float4*>(cy));
+        quad32_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol_in, reinterpret_cast<float4*>(cx),
+                                        reinterpret_cast<float4*>(cy));
         MCT_TRY(launched("quad32_kernel"));
         fp_kernel<true, true, Quad16><<<grid, block, 0, s>>>(p, t->angles, t->u, t->v, t->cz, t->pmat_a, t->pmat_xs,
                                                              vol, nullptr, cx, cy, mask, sgm, nullptr);
-    } else {
+    } else if constexpr (kIn32) {
         float* vt = static_cast<float*>(workspace);
         if (vt) {
             transpose_xy_kernel<<<tg, tb, 0, s>>>(g->nx, g->nz, vol, vt);
@@ -872,6 +884,23 @@ int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, con
                                                                    nullptr);
     }
     return launched("fp_kernel");
+}
+}  // namespace
+
+extern "C" {
+
+int mct_fp_storage(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm,
+                   void* workspace, int32_t dtype, void* stream) {
+    return fp_storage_impl<float>(g, t, vol, mask, sgm, workspace, dtype, stream);
+}
+
+int mct_fp_storage_in(const mct_geom* g, const mct_tables* t, const void* vol, int32_t vol_dtype, const float* mask,
+                      float* sgm, void* workspace, int32_t dtype, void* stream) {
+    MCT_REQUIRE(vol_dtype == MCT_F32 || vol_dtype == MCT_BF16, "mct_fp_storage_in: vol_dtype must be MCT_F32 or MCT_BF16");
+    if (vol_dtype == MCT_F32)
+        return fp_storage_impl<float>(g, t, static_cast<const float*>(vol), mask, sgm, workspace, dtype, stream);
+    return fp_storage_impl<__nv_bfloat16>(g, t, static_cast<const __nv_bfloat16*>(vol), mask, sgm, workspace, dtype,
+                                          stream);
 }
 
 int mct_fp(const mct_geom* g, const mct_tables* t, const float* vol, const float* mask, float* sgm, void* workspace,

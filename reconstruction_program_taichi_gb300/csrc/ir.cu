@@ -144,10 +144,10 @@ template <typename QT>
 constexpr int ua_min_blocks() {
     return sizeof(QT) == 8 ? 3 : 2;
 }
-template <bool CONE, typename QT, typename PT>
+template <bool CONE, typename QT, typename PT, typename OT = float>
 __global__ void __launch_bounds__(UB_TX* UB_TY, ua_min_blocks<QT>())
 bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
-                          const void* __restrict__ packed, float* __restrict__ vol,
+                          const void* __restrict__ packed, OT* __restrict__ vol,
                           const uint32_t* __restrict__ f16_max) {
     const int nq = p.nu - 1;  // packed: nv rows of nu-1 coefficient sets per view
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, sid*cos b}
@@ -240,25 +240,27 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
     const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
 #pragma unroll
     for (int k = 0; k < UA_ZC; ++k)
-        if (zb + k < p.nz) vol[(zb + k) * plane + (int64_t)iy * p.nx + ix] = trunc ? 0.0f : acc[k] * unscale;
+        if (zb + k < p.nz) stv(vol, (zb + k) * plane + (int64_t)iy * p.nx + ix, trunc ? 0.0f : acc[k] * unscale);
 }
 
 // Forward differences (y, x, z) with zero at the far edge; z only when nz > 2.
 struct Grad {
     float gy, gx, gz;
 };
-__device__ __forceinline__ Grad grad_at(const float* __restrict__ x, int nx, int nz, int iz, int iy, int ix) {
+template <typename T>
+__device__ __forceinline__ Grad grad_at(const T* __restrict__ x, int nx, int nz, int iz, int iy, int ix) {
     const int64_t plane = (int64_t)nx * nx;
     const int64_t i = (int64_t)iz * plane + (int64_t)iy * nx + ix;
-    const float c = x[i];
+    const float c = ldv(x, i);
     Grad g;
-    g.gy = (iy < nx - 1) ? x[i + nx] - c : 0.0f;
-    g.gx = (ix < nx - 1) ? x[i + 1] - c : 0.0f;
-    g.gz = (nz > 2 && iz < nz - 1) ? x[i + plane] - c : 0.0f;
+    g.gy = (iy < nx - 1) ? ldv(x, i + nx) - c : 0.0f;
+    g.gx = (ix < nx - 1) ? ldv(x, i + 1) - c : 0.0f;
+    g.gz = (nz > 2 && iz < nz - 1) ? ldv(x, i + plane) - c : 0.0f;
     return g;
 }
 
-__global__ void tv_weights_kernel(int nx, int nz, float beta, const float* __restrict__ x, float* __restrict__ wr) {
+template <typename T>
+__global__ void tv_weights_kernel(int nx, int nz, float beta, const T* __restrict__ x, float* __restrict__ wr) {
     const int64_t n = (int64_t)nz * nx * nx;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % nx);
@@ -316,10 +318,10 @@ __device__ __forceinline__ double block_sum(double v);
 // out = a*out_in + s * (D^T W D x), run_mgfbp_iterative_recon_IRN_CGLS.py:267-286.
 // DOT: also the per-block float64 partial sums of x[i] * out[i] (the CG step's <d, q>
 // while q is being written; out may alias out_in).
-template <bool DOT>
+template <bool DOT, typename T = float>
 __global__ void __launch_bounds__(256)
-dtwd_kernel(int nx, int nz, const float* __restrict__ x, const float* __restrict__ wr, float s,
-            const float* out_in, float a, float* out, double* __restrict__ partials) {
+dtwd_kernel(int nx, int nz, const T* __restrict__ x, const float* __restrict__ wr, float s,
+            const T* out_in, float a, T* out, double* __restrict__ partials) {
     const int64_t n = (int64_t)nz * nx * nx;
     const int64_t plane = (int64_t)nx * nx;
     double dsum = 0.0;
@@ -327,27 +329,27 @@ dtwd_kernel(int nx, int nz, const float* __restrict__ x, const float* __restrict
         const int ix = (int)(i % nx);
         const int iy = (int)((i / nx) % nx);
         const int iz = (int)(i / plane);
-        const float c = x[i];
+        const float c = ldv(x, i);
         float r = 0.0f;
         if (iy >= 1 && iy <= nx - 2) {  // uxx = Ux[y] - Ux[y-1]
-            const float ux_c = wr[i] * (x[i + nx] - c);
-            const float ux_m = wr[i - nx] * (c - x[i - nx]);
+            const float ux_c = wr[i] * (ldv(x, i + nx) - c);
+            const float ux_m = wr[i - nx] * (c - ldv(x, i - nx));
             r -= ux_c - ux_m;
         }
         if (ix >= 1 && ix <= nx - 2) {
-            const float uy_c = wr[i] * (x[i + 1] - c);
-            const float uy_m = wr[i - 1] * (c - x[i - 1]);
+            const float uy_c = wr[i] * (ldv(x, i + 1) - c);
+            const float uy_m = wr[i - 1] * (c - ldv(x, i - 1));
             r -= uy_c - uy_m;
         }
         if (nz > 2 && iz >= 1 && iz <= nz - 2) {
-            const float uz_c = wr[i] * (x[i + plane] - c);
-            const float uz_m = wr[i - plane] * (c - x[i - plane]);
+            const float uz_c = wr[i] * (ldv(x, i + plane) - c);
+            const float uz_m = wr[i - plane] * (c - ldv(x, i - plane));
             r -= uz_c - uz_m;
         }
         float v = s * r;
-        if (a != 0.0f) v += a * out_in[i];
-        out[i] = v;
-        if (DOT) dsum += (double)c * (double)v;
+        if (a != 0.0f) v += a * ldv(out_in, i);
+        stv(out, i, v);
+        if (DOT) dsum += (double)c * (double)ldv(out, i);  // the stored value
     }
     if (DOT) {
         dsum = block_sum(dsum);
@@ -371,11 +373,23 @@ __device__ __forceinline__ double block_sum(double v) {
     return v;  // valid in thread 0
 }
 
+// Per thread four independent float64 accumulators (the products of two float32 values
+// are exact in float64, so each step is one DFMA): float64 has a fraction of the float32
+// rate on this GPU, and one dependent chain per thread left the kernel at 10 % issue.
+template <typename T = float>
 __global__ void __launch_bounds__(RED_THREADS)
-dot_partial_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t n, double* __restrict__ partials) {
-    double s = 0.0;
-    for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS)
-        s += (double)a[i] * (double)b[i];
+dot_partial_kernel(const T* __restrict__ a, const T* __restrict__ b, int64_t n, double* __restrict__ partials) {
+    const int64_t stride = (int64_t)gridDim.x * RED_THREADS;
+    int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        s0 = fma((double)ldv(a, i), (double)ldv(b, i), s0);
+        s1 = fma((double)ldv(a, i + stride), (double)ldv(b, i + stride), s1);
+        s2 = fma((double)ldv(a, i + 2 * stride), (double)ldv(b, i + 2 * stride), s2);
+        s3 = fma((double)ldv(a, i + 3 * stride), (double)ldv(b, i + 3 * stride), s3);
+    }
+    for (; i < n; i += stride) s0 = fma((double)ldv(a, i), (double)ldv(b, i), s0);
+    double s = (s0 + s1) + (s2 + s3);
     s = block_sum(s);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
@@ -404,28 +418,30 @@ finish_sum_kernel(const double* __restrict__ partials, int n, double* __restrict
 }
 
 // x += alpha d; r -= alpha q; partial sums of r^2 (alpha = rr/dq read on device)
+template <typename T = float>
 __global__ void __launch_bounds__(RED_THREADS)
-cgls_update_kernel(int64_t n, const double* __restrict__ rr, const double* __restrict__ dq, float* __restrict__ x,
-                   float* __restrict__ r, const float* __restrict__ d, const float* __restrict__ q,
+cgls_update_kernel(int64_t n, const double* __restrict__ rr, const double* __restrict__ dq, T* __restrict__ x,
+                   T* __restrict__ r, const T* __restrict__ d, const T* __restrict__ q,
                    double* __restrict__ partials) {
     const float alpha = (float)(*rr / *dq);
     double s = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS) {
-        const float di = d[i];
-        x[i] = x[i] + alpha * di;
-        const float ri = r[i] - alpha * q[i];
-        r[i] = ri;
+        const float di = ldv(d, i);
+        stv(x, i, ldv(x, i) + alpha * di);
+        stv(r, i, ldv(r, i) - alpha * ldv(q, i));
+        const float ri = ldv(r, i);  // the stored value
         s += (double)ri * (double)ri;
     }
     s = block_sum(s);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+template <typename T = float>
 __global__ void cgls_direction_kernel(int64_t n, const double* __restrict__ rr, const double* __restrict__ rr_new,
-                                      const float* __restrict__ r, float* __restrict__ d) {
+                                      const T* __restrict__ r, T* __restrict__ d) {
     const float beta = (float)(*rr_new / *rr);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        d[i] = r[i] + beta * d[i];
+        stv(d, i, ldv(r, i) + beta * ldv(d, i));
 }
 
 inline int ew_grid(int64_t n) {
@@ -469,6 +485,35 @@ int mct_bp_ref_unmatched(const mct_geom* g, const mct_tables* t, const float* sg
     dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UB_ZC - 1) / UB_ZC);
     bp_unmatched_kernel<0, float4, float2><<<grid, block, 0, as_stream(stream)>>>(p, t->angles, t->cz, g->cz, sgm,
                                                                                   nullptr, vol, nullptr);
+    return launched("bp_unmatched_kernel");
+}
+
+int mct_bp_ref_unmatched_packed_out(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
+                                    void* vol, int32_t vol_dtype, void* stream) {
+    if (vol_dtype == MCT_F32)
+        return mct_bp_ref_unmatched_packed(g, t, packed, dtype, static_cast<float*>(vol), stream);
+    UbParams p{};
+    MCT_TRY(unmatched_params(g, p));
+    MCT_REQUIRE(vol_dtype == MCT_BF16, "mct_bp_ref_unmatched_packed_out: vol_dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(t && t->angles && packed && vol, "mct_bp_ref_unmatched_packed_out: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16 || dtype == MCT_F16,
+                "mct_bp_ref_unmatched_packed_out: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
+    MCT_REQUIRE(g->view_mode == 1 && p.cone,
+                "mct_bp_ref_unmatched_packed_out: bf16 output needs the axial view mode and cone beam");
+    MCT_REQUIRE((int64_t)g->nv * (g->nu - 1) < ((int64_t)1 << 31), "mct_bp_ref_unmatched_packed_out: detector too large");
+    cudaStream_t s = as_stream(stream);
+    dim3 block(UB_TX, UB_TY);
+    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UA_ZC - 1) / UA_ZC);
+    __nv_bfloat16* out = static_cast<__nv_bfloat16*>(vol);
+    if (dtype == MCT_F32)
+        bp_unmatched_axial_kernel<true, float4, float2, __nv_bfloat16><<<grid, block, 0, s>>>(
+            p, t->angles, t->cz, g->cz, packed, out, nullptr);
+    else if (dtype == MCT_BF16)
+        bp_unmatched_axial_kernel<true, uint2, uint32_t, __nv_bfloat16><<<grid, block, 0, s>>>(
+            p, t->angles, t->cz, g->cz, packed, out, nullptr);
+    else
+        bp_unmatched_axial_kernel<true, h16x4, h16x2, __nv_bfloat16><<<grid, block, 0, s>>>(
+            p, t->angles, t->cz, g->cz, packed, out, f16_trailer(g, packed));
     return launched("bp_unmatched_kernel");
 }
 
@@ -611,6 +656,99 @@ int mct_cgls_update(int64_t n, const double* rr, const double* dq, float* x, flo
 int mct_cgls_direction(int64_t n, const double* rr, const double* rr_new, const float* r, float* d, void* stream) {
     MCT_REQUIRE(rr && rr_new && r && d && n >= 0, "mct_cgls_direction: bad arguments");
     cgls_direction_kernel<<<ew_grid(n), 256, 0, as_stream(stream)>>>(n, rr, rr_new, r, d);
+    return launched("cgls_direction_kernel");
+}
+
+// ---- the same vector operations on float32 or bf16 volumes (bf16 iterate storage)
+
+#define MCT_VEC_DTYPE(who, dt) MCT_REQUIRE((dt) == MCT_F32 || (dt) == MCT_BF16, "%s: vector dtype must be MCT_F32 or MCT_BF16", who)
+
+int mct_tv_weights_t(const mct_geom* g, const void* x, int32_t x_dtype, float beta, float* wr, void* stream) {
+    MCT_REQUIRE(g && x && wr && x != (const void*)wr && g->nx >= 1 && g->nz >= 1, "mct_tv_weights_t: bad arguments");
+    MCT_VEC_DTYPE("mct_tv_weights_t", x_dtype);
+    cudaStream_t s = as_stream(stream);
+    if (x_dtype == MCT_F32)
+        tv_weights_kernel<<<ew_grid(vol_elems(*g)), 256, 0, s>>>(g->nx, g->nz, beta, static_cast<const float*>(x), wr);
+    else
+        tv_weights_kernel<<<ew_grid(vol_elems(*g)), 256, 0, s>>>(g->nx, g->nz, beta,
+                                                                 static_cast<const __nv_bfloat16*>(x), wr);
+    return launched("tv_weights_kernel");
+}
+
+int mct_dtwd_t(const mct_geom* g, const void* x, const float* wr, float s, const void* out_in, float a, void* out,
+               int32_t vec_dtype, double* partials, double* dot, void* stream) {
+    MCT_REQUIRE(g && x && wr && out && out != x && out != (const void*)wr && g->nx >= 1 && g->nz >= 1,
+                "mct_dtwd_t: bad arguments");
+    MCT_REQUIRE(a == 0.0f || out_in, "mct_dtwd_t: out_in is NULL");
+    MCT_REQUIRE((partials == nullptr) == (dot == nullptr), "mct_dtwd_t: partials and dot go together");
+    MCT_VEC_DTYPE("mct_dtwd_t", vec_dtype);
+    cudaStream_t st = as_stream(stream);
+    const bool with_dot = dot != nullptr;
+    const int grid = with_dot ? RED_BLOCKS : ew_grid(vol_elems(*g));
+    if (vec_dtype == MCT_F32) {
+        auto xx = static_cast<const float*>(x);
+        auto oi = static_cast<const float*>(out_in);
+        auto oo = static_cast<float*>(out);
+        if (with_dot) dtwd_kernel<true, float><<<grid, 256, 0, st>>>(g->nx, g->nz, xx, wr, s, oi, a, oo, partials);
+        else dtwd_kernel<false, float><<<grid, 256, 0, st>>>(g->nx, g->nz, xx, wr, s, oi, a, oo, nullptr);
+    } else {
+        auto xx = static_cast<const __nv_bfloat16*>(x);
+        auto oi = static_cast<const __nv_bfloat16*>(out_in);
+        auto oo = static_cast<__nv_bfloat16*>(out);
+        if (with_dot) dtwd_kernel<true, __nv_bfloat16><<<grid, 256, 0, st>>>(g->nx, g->nz, xx, wr, s, oi, a, oo, partials);
+        else dtwd_kernel<false, __nv_bfloat16><<<grid, 256, 0, st>>>(g->nx, g->nz, xx, wr, s, oi, a, oo, nullptr);
+    }
+    MCT_TRY(launched("dtwd_kernel"));
+    if (!with_dot) return MCT_OK;
+    finish_sum_kernel<<<1, RED_THREADS, 0, st>>>(partials, RED_BLOCKS, dot);
+    return launched("finish_sum_kernel");
+}
+
+int mct_dot_f64_t(const void* a, const void* b, int64_t n, int32_t dtype, double* partials, double* result,
+                  void* stream) {
+    MCT_REQUIRE(a && b && partials && result && n >= 0, "mct_dot_f64_t: bad arguments");
+    MCT_VEC_DTYPE("mct_dot_f64_t", dtype);
+    cudaStream_t s = as_stream(stream);
+    if (dtype == MCT_F32)
+        dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(static_cast<const float*>(a),
+                                                              static_cast<const float*>(b), n, partials);
+    else
+        dot_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(static_cast<const __nv_bfloat16*>(a),
+                                                              static_cast<const __nv_bfloat16*>(b), n, partials);
+    MCT_TRY(launched("dot_partial_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, s>>>(partials, RED_BLOCKS, result);
+    return launched("finish_sum_kernel");
+}
+
+int mct_cgls_update_t(int64_t n, int32_t dtype, const double* rr, const double* dq, void* x, void* r, const void* d,
+                      const void* q, double* partials, double* rr_new, void* stream) {
+    MCT_REQUIRE(rr && dq && x && r && d && q && partials && rr_new && n >= 0, "mct_cgls_update_t: bad arguments");
+    MCT_VEC_DTYPE("mct_cgls_update_t", dtype);
+    cudaStream_t s = as_stream(stream);
+    if (dtype == MCT_F32)
+        cgls_update_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, rr, dq, static_cast<float*>(x), static_cast<float*>(r),
+                                                              static_cast<const float*>(d),
+                                                              static_cast<const float*>(q), partials);
+    else
+        cgls_update_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(
+            n, rr, dq, static_cast<__nv_bfloat16*>(x), static_cast<__nv_bfloat16*>(r),
+            static_cast<const __nv_bfloat16*>(d), static_cast<const __nv_bfloat16*>(q), partials);
+    MCT_TRY(launched("cgls_update_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, s>>>(partials, RED_BLOCKS, rr_new);
+    return launched("finish_sum_kernel");
+}
+
+int mct_cgls_direction_t(int64_t n, int32_t dtype, const double* rr, const double* rr_new, const void* r, void* d,
+                         void* stream) {
+    MCT_REQUIRE(rr && rr_new && r && d && n >= 0, "mct_cgls_direction_t: bad arguments");
+    MCT_VEC_DTYPE("mct_cgls_direction_t", dtype);
+    cudaStream_t s = as_stream(stream);
+    if (dtype == MCT_F32)
+        cgls_direction_kernel<<<ew_grid(n), 256, 0, s>>>(n, rr, rr_new, static_cast<const float*>(r),
+                                                         static_cast<float*>(d));
+    else
+        cgls_direction_kernel<<<ew_grid(n), 256, 0, s>>>(n, rr, rr_new, static_cast<const __nv_bfloat16*>(r),
+                                                         static_cast<__nv_bfloat16*>(d));
     return launched("cgls_direction_kernel");
 }
 

@@ -48,6 +48,12 @@ class IrSystem:
         self.dtype = kinds[storage]
         self.fp_dtype = self.dtype if self.dg.geom.flags & ops.MCT_CONE else ops.MCT_F32
         self.data_dtype = kinds[getattr(obj, "sinogram_precision", "float32")]
+        self.iter_dtype = {"float32": torch.float32, "bfloat16": torch.bfloat16}[
+            getattr(obj, "iterate_storage", "float32")]
+        if self.iter_dtype != torch.float32 and (self.matched or not (self.dg.geom.flags & ops.MCT_CONE)
+                                                 or self.dg.geom.view_mode != 1):
+            raise ConfigError("ERROR: IterateStorage bfloat16 needs cone beam, the reference backprojector and the "
+                              "axial view mode")
         self.mask = ops.effective_map(self.dg)
         f32 = dict(dtype=torch.float32, device=self.device)
         self.fp_buf = torch.empty(self.dg.sgm_shape, **f32)
@@ -104,14 +110,18 @@ class IrSystem:
         is of the size of P^T b, and rounding x_seed to bf16 would perturb the right-hand
         side like measurement noise; the per-iteration products P^T P d use the storage
         precision."""
-        d = self.ptp(x_seed, full_precision=True)
-        torch.sub(self.bpb, d, out=d)  # d = P^T b - P^T P x0
+        x0 = x_seed if x_seed.dtype == torch.float32 else x_seed.float()
+        d = self.ptp(x0, full_precision=True)
+        torch.sub(self.bpb, d, out=d)  # d = P^T b - P^T P x0 (float32 whatever the storage)
         for s, w, y in rhs_terms:
             self.dtwd_acc(y, w, s, d)
         for s, w in op_terms:
-            self.dtwd_acc(x_seed, w, -s, d)
+            self.dtwd_acc(x0, w, -s, d)
+        it = self.iter_dtype
+        if it != torch.float32:  # iterates stored rounded to bf16 from here on
+            d = d.to(it)
         r = d.clone()
-        x = x_seed.clone()
+        x = x_seed.to(it, copy=True)
         q = torch.empty_like(x)
         rr, rr_new = self._rr, self._rr_new
         ops.dot(r, r, out=rr)
@@ -136,7 +146,7 @@ class IrSystem:
         obj = self.obj
         diff = self.fp(x) - sgm * self.mask
         data = 0.5 * float(ops.dot(diff, diff)) / obj.sgm_total_pixel_count
-        return data + lam * float(ops.tv_penalty(self.dg, x, beta)) / obj.img_total_pixel_count
+        return data + lam * float(ops.tv_penalty(self.dg, x.float(), beta)) / obj.img_total_pixel_count
 
 
 class Mgfbp_ir:  # noqa: N801 - reference name
@@ -214,7 +224,7 @@ class Mgfbp_ir:  # noqa: N801 - reference name
             if self.compute_loss:
                 self.loss = np.append(self.loss, sy.loss_tv(x, sgm_dev, self.coef_lambda, self.beta_tv))
         self.num_iter_runned = sy.ptp_calls
-        return x
+        return x.float()
 
     def MainFunction(self, img_recon_seed):  # noqa: N802 - reference name
         """run_mgfbp_iterative_recon_IRN_CGLS.py:138-176."""
@@ -262,7 +272,7 @@ class Mgfbp_ir_piccs(Mgfbp_ir):  # noqa: N801 - reference name
             ops.tv_weights(sy.dg, diff, self.beta_tv, out=wrp)
             x = sy.cgls(x, [(s_pr, wrp, prior_dev)], [(s_tv, wr), (s_pr, wrp)], self.num_iter)
         self.num_iter_runned = sy.ptp_calls
-        return x
+        return x.float()
 
     def MainFunction(self):  # noqa: N802 - reference name
         """run_mgfbp_iterative_recon_IRN_CGLS_piccs.py:70-110."""

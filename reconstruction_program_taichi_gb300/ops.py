@@ -23,6 +23,17 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+_VEC = {torch.float32: MCT_F32, torch.bfloat16: MCT_BF16}
+
+
+def _vec_dtype(t, name, shape=None):
+    """MCT_F32 / MCT_BF16 of a float32 or bf16 volume (bf16 CG iterates)."""
+    if not isinstance(t, torch.Tensor) or t.dtype not in _VEC:
+        raise TypeError(f"{name} must be a float32 or bfloat16 CUDA tensor")
+    _check(t, name, shape, dtype=t.dtype)
+    return _VEC[t.dtype]
+
+
 def _check(t, name, shape=None, dtype=torch.float32):
     if not isinstance(t, torch.Tensor) or not t.is_cuda:
         raise TypeError(f"{name} must be a CUDA tensor")
@@ -200,10 +211,15 @@ def pack_sinogram(dg, sgm, dtype=MCT_F32, out=None):
 
 
 def bp_unmatched_packed(dg, packed, dtype=MCT_F32, out=None):
+    """The IR driver's backprojector of a packed sinogram; out may be bf16 (axial cone
+    beam), rounded from the float32 sums."""
     if out is None:
         out = torch.empty(dg.vol_shape, dtype=torch.float32, device=packed.device)
-    _check(out, "out", dg.vol_shape)
-    _lib.call("mct_bp_ref_unmatched_packed", dg.g(), dg.t(), _ptr(packed), dtype, _ptr(out), _stream())
+    odt = _vec_dtype(out, "out", dg.vol_shape)
+    if odt == MCT_F32:
+        _lib.call("mct_bp_ref_unmatched_packed", dg.g(), dg.t(), _ptr(packed), dtype, _ptr(out), _stream())
+    else:
+        _lib.call("mct_bp_ref_unmatched_packed_out", dg.g(), dg.t(), _ptr(packed), dtype, _ptr(out), odt, _stream())
     return out
 
 
@@ -235,15 +251,19 @@ def fp_workspace(dg, dtype=MCT_F32):
 def fp(dg, vol, mask=None, out=None, workspace=True, dtype=MCT_F32):
     """P vol.  workspace=True uses the geometry's cached gather-copy buffer (coalesced
     gathers for every view); None runs without it.  dtype=MCT_BF16 or MCT_F16 (cone
-    beam) stores the gather copies as 16-bit cells (mct_fp_storage)."""
-    _check(vol, "vol", dg.vol_shape)
+    beam) stores the gather copies as 16-bit cells (mct_fp_storage).  vol may be bf16
+    (bf16 iterates; cone beam with the workspace)."""
+    vdt = _vec_dtype(vol, "vol", dg.vol_shape)
     if mask is not None:
         _check(mask, "mask", dg.sgm_shape)
     if out is None:
         out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=vol.device)
     _check(out, "out", dg.sgm_shape)
     ws = fp_workspace(dg, dtype) if workspace is True else workspace
-    if dtype == MCT_F32:
+    if vdt != MCT_F32:
+        _lib.call("mct_fp_storage_in", dg.g(), dg.t(), _ptr(vol), vdt, _ptr(mask), _ptr(out), _ptr(ws), int(dtype),
+                  _stream())
+    elif dtype == MCT_F32:
         _lib.call("mct_fp", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), _stream())
     else:
         _lib.call("mct_fp_storage", dg.g(), dg.t(), _ptr(vol), _ptr(mask), _ptr(out), _ptr(ws), int(dtype), _stream())
@@ -330,31 +350,48 @@ def bp_unmatched(dg, sgm, out=None):
 
 
 def tv_weights(dg, x, beta, out=None):
-    _check(x, "x", dg.vol_shape)
+    """WR = 1/sqrt(|D x|^2 + beta) as float32; x float32 or bf16."""
+    xdt = _vec_dtype(x, "x", dg.vol_shape)
     if out is None:
-        out = torch.empty_like(x)
-    _lib.call("mct_tv_weights", dg.g(), _ptr(x), float(beta), _ptr(out), _stream())
+        out = torch.empty(dg.vol_shape, dtype=torch.float32, device=x.device)
+    _check(out, "out", dg.vol_shape)
+    if xdt == MCT_F32:
+        _lib.call("mct_tv_weights", dg.g(), _ptr(x), float(beta), _ptr(out), _stream())
+    else:
+        _lib.call("mct_tv_weights_t", dg.g(), _ptr(x), xdt, float(beta), _ptr(out), _stream())
     return out
 
 
 def dtwd(dg, x, wr, s=1.0, out_in=None, a=0.0, out=None):
-    """out = a*out_in + s * D^T W D x."""
-    _check(x, "x", dg.vol_shape)
+    """out = a*out_in + s * D^T W D x (x, out_in, out all float32 or all bf16; wr float32)."""
+    xdt = _vec_dtype(x, "x", dg.vol_shape)
     _check(wr, "wr", dg.vol_shape)
     if out is None:
         out = torch.empty_like(x)
-    _lib.call("mct_dtwd", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(out_in), float(a), _ptr(out), _stream())
+    if xdt == MCT_F32:
+        _lib.call("mct_dtwd", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(out_in), float(a), _ptr(out), _stream())
+    else:
+        for t, n in ((out, "out"), (out_in, "out_in")):
+            if t is not None and _vec_dtype(t, n, dg.vol_shape) != xdt:
+                raise TypeError(f"{n} must have the dtype of x")
+        _lib.call("mct_dtwd_t", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(out_in), float(a), _ptr(out), xdt, None,
+                  None, _stream())
     return out
 
 
 def dtwd_dot(dg, x, wr, s, acc, dot_out):
     """acc += s * D^T W D x (in place) and dot_out = <x, acc> (float64 device scalar),
-    in one pass."""
-    _check(x, "x", dg.vol_shape)
+    in one pass (x and acc float32 or both bf16)."""
+    xdt = _vec_dtype(x, "x", dg.vol_shape)
     _check(wr, "wr", dg.vol_shape)
-    _check(acc, "acc", dg.vol_shape)
-    _lib.call("mct_dtwd_dot", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(acc), 1.0, _ptr(acc),
-              _ptr(reduce_scratch(x.device)), _ptr(dot_out), _stream())
+    if _vec_dtype(acc, "acc", dg.vol_shape) != xdt:
+        raise TypeError("acc must have the dtype of x")
+    if xdt == MCT_F32:
+        _lib.call("mct_dtwd_dot", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(acc), 1.0, _ptr(acc),
+                  _ptr(reduce_scratch(x.device)), _ptr(dot_out), _stream())
+    else:
+        _lib.call("mct_dtwd_t", dg.g(), _ptr(x), _ptr(wr), float(s), _ptr(acc), 1.0, _ptr(acc), xdt,
+                  _ptr(reduce_scratch(x.device)), _ptr(dot_out), _stream())
     return dot_out
 
 
@@ -381,21 +418,42 @@ def tv_penalty(dg, x, beta, out=None):
 
 
 def dot(a, b, out=None):
-    """float64 inner product of two float32 tensors, as a device scalar."""
-    _check(a, "a")
-    _check(b, "b", tuple(a.shape))
+    """float64 inner product of two float32 (or two bf16) tensors, as a device scalar."""
+    adt = _vec_dtype(a, "a")
+    if _vec_dtype(b, "b", tuple(a.shape)) != adt:
+        raise TypeError("a and b must have the same dtype")
     if out is None:
         out = torch.empty((), dtype=torch.float64, device=a.device)
-    _lib.call("mct_dot_f64", _ptr(a), _ptr(b), a.numel(), _ptr(reduce_scratch(a.device)), _ptr(out), _stream())
+    if adt == MCT_F32:
+        _lib.call("mct_dot_f64", _ptr(a), _ptr(b), a.numel(), _ptr(reduce_scratch(a.device)), _ptr(out), _stream())
+    else:
+        _lib.call("mct_dot_f64_t", _ptr(a), _ptr(b), a.numel(), adt, _ptr(reduce_scratch(a.device)), _ptr(out),
+                  _stream())
     return out
+
+
+def _same_vec_dtype(*ts):
+    dts = {_vec_dtype(t, "vector") for t in ts}
+    if len(dts) != 1:
+        raise TypeError("CG vectors must share one dtype (float32 or bfloat16)")
+    return dts.pop()
 
 
 def cgls_update(rr, dq, x, r, d, q, rr_new):
     """alpha = rr/dq; x += alpha d; r -= alpha q; rr_new = |r|^2 (device scalars)."""
-    _lib.call("mct_cgls_update", x.numel(), _ptr(rr), _ptr(dq), _ptr(x), _ptr(r), _ptr(d), _ptr(q),
-              _ptr(reduce_scratch(x.device)), _ptr(rr_new), _stream())
+    vdt = _same_vec_dtype(x, r, d, q)
+    if vdt == MCT_F32:
+        _lib.call("mct_cgls_update", x.numel(), _ptr(rr), _ptr(dq), _ptr(x), _ptr(r), _ptr(d), _ptr(q),
+                  _ptr(reduce_scratch(x.device)), _ptr(rr_new), _stream())
+    else:
+        _lib.call("mct_cgls_update_t", x.numel(), vdt, _ptr(rr), _ptr(dq), _ptr(x), _ptr(r), _ptr(d), _ptr(q),
+                  _ptr(reduce_scratch(x.device)), _ptr(rr_new), _stream())
 
 
 def cgls_direction(rr, rr_new, r, d):
     """d = r + (rr_new/rr) d."""
-    _lib.call("mct_cgls_direction", d.numel(), _ptr(rr), _ptr(rr_new), _ptr(r), _ptr(d), _stream())
+    vdt = _same_vec_dtype(r, d)
+    if vdt == MCT_F32:
+        _lib.call("mct_cgls_direction", d.numel(), _ptr(rr), _ptr(rr_new), _ptr(r), _ptr(d), _stream())
+    else:
+        _lib.call("mct_cgls_direction_t", d.numel(), vdt, _ptr(rr), _ptr(rr_new), _ptr(r), _ptr(d), _stream())

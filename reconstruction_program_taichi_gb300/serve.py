@@ -199,28 +199,38 @@ class _FbpSlot:
     def _member(self, i):
         self.pipes[i].run(self.inp[i], out=self.out[i])
 
-    def run(self, reqs):
-        dev_out = []
+    def run(self, reqs, done=None):
+        """Reconstruct reqs (at most `batch`); returns their results in order.  done(i,
+        result), when given, is called for every member but the last as soon as that
+        member's result is ready."""
+        pending = []
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
                 if r.on_device:
                     self.inp[i].copy_(r.sgm)
                 else:
                     self.inp[i].copy_(torch.from_numpy(np.ascontiguousarray(r.sgm, dtype=np.float32)))
-            for i in range(len(reqs)):
                 if self.graphs:
                     self.graphs[i].replay()
                 else:
                     self._member(i)
-            for i, r in enumerate(reqs):
                 if r.on_device:
-                    dev_out.append(self.out[i].clone())
+                    res = self.out[i].clone()
                 else:
-                    dev_out.append(None)
+                    res = None
                     self.host_out[i].copy_(self.out[i], non_blocking=True)
-        self.stream.synchronize()
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
+                pending.append((ev, res))
+        outs = []
+        for i, (ev, res) in enumerate(pending):
+            ev.synchronize()
+            out = res if res is not None else self.host_out[i].numpy().copy()
+            if done is not None and i + 1 < len(pending):
+                done(i, out)
+            outs.append(out)
         self.last_used = time.perf_counter()
-        return [d if d is not None else self.host_out[i].numpy().copy() for i, d in enumerate(dev_out)]
+        return outs
 
 
 def _fp_workspace_bytes(dg, dtype):
@@ -270,18 +280,28 @@ class _CglsSlot:
         x = sy.cgls(self.x0[i], [], [(self.lr, self.wr)], self.n_iter)
         self.out[i].copy_(x)
 
-    def run(self, reqs):
+    def run(self, reqs, done=None):
+        """As _FbpSlot.run: results in order, done(i, result) early for all but the last."""
+        pending = []
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
                 self.sgm[i].copy_(_to_device(r.sgm, self.device))
                 self.x0[i].copy_(_to_device(r.x0, self.device))
-            for i in range(len(reqs)):
                 if self.graphs:
                     self.graphs[i].replay()
                 else:
                     self._member(i)
-            outs = [self.out[i].clone() if r.on_device else self.out[i].cpu().numpy() for i, r in enumerate(reqs)]
-        self.stream.synchronize()
+                res = self.out[i].clone()
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
+                pending.append((ev, res, r.on_device))
+        outs = []
+        for i, (ev, res, on_device) in enumerate(pending):
+            ev.synchronize()
+            out = res if on_device else res.cpu().numpy()
+            if done is not None and i + 1 < len(pending):
+                done(i, out)
+            outs.append(out)
         self.last_used = time.perf_counter()
         return outs
 
@@ -514,7 +534,7 @@ class ReconServer:
         """Worker of one batch: builds the slot first when the scheduler reserved the
         budget for a new one (outside the lock, so finishing batches are not held up),
         then runs the batch and returns the slot."""
-        outs, err = None, None
+        outs, err, early = None, None, set()
         try:
             torch.cuda.set_device(self.device)
             if slot is None:
@@ -531,29 +551,46 @@ class ReconServer:
                             self.used += slot.nbytes - reserved
             for r in group:
                 _resolve_inputs(r)
-            outs = slot.run(group)
+            early = set()
+
+            def member_done(i, out):
+                # a member before the batch's last: recorded, then delivered at once
+                r = group[i]
+                r.t_done = time.perf_counter()
+                with self.cv:
+                    self.done.append(r)
+                early.add(i)
+                self._deliver(r, out)
+
+            outs = slot.run(group, member_done)
             now = time.perf_counter()
-            for r in group:
-                r.t_done = now
+            for i, r in enumerate(group):
+                if i not in early:
+                    r.t_done = now
         except Exception as e:  # a failed batch fails its own requests only
             err = e
             self.errors.append(e)
-        # record completion and free the slot before any caller can observe the result
+        # record completion and free the slot before any caller can observe the last result
         with self.cv:
             if outs is not None:
-                self.done.extend(group)
+                self.done.extend(r for i, r in enumerate(group) if i not in early)
             self.busy -= 1
             if slot is not None:
                 self.free_slots.setdefault(key, []).append(slot)
             self.cv.notify_all()
         for i, r in enumerate(group):
             if outs is not None:
-                if r.out_path is not None:
-                    try:
-                        self._io.submit(self._write_result, r, outs[i])
-                    except RuntimeError:  # I/O threads already shut down (close without waiting)
-                        self._write_result(r, outs[i])
-                else:
-                    r.future.set_result(outs[i])
+                if i not in early:
+                    self._deliver(r, outs[i])
             elif not r.future.done():
                 r.future.set_exception(err)
+
+    def _deliver(self, r, out):
+        """Resolve r's future with out (after writing out_path, on an I/O thread)."""
+        if r.out_path is not None:
+            try:
+                self._io.submit(self._write_result, r, out)
+            except RuntimeError:  # I/O threads already shut down (close without waiting)
+                self._write_result(r, out)
+        else:
+            r.future.set_result(out)

@@ -687,3 +687,70 @@ def test_run_mgfbp_ir_admm_matches_reference(tmp_path, cuda):
     assert rel_l2(vy.cpu().numpy(), z["v_x"]) < 1e-3 and rel_l2(vx.cpu().numpy(), z["v_y"]) < 1e-3
     assert rel_l2(py.cpu().numpy(), z["p_x"]) < 1e-3 and rel_l2(px.cpu().numpy(), z["p_y"]) < 1e-3
     assert ir.num_iter_runned == int(z["ptp_calls"])
+
+
+def test_bf16_iterate_kernels_match_rounded_numpy(cuda):
+    """The CG vector kernels on bf16 volumes: float32 arithmetic on the widened values,
+    float64 sums of the stored (rounded) values, results rounded to bf16 -- checked
+    against NumPy applying the same rounding."""
+    import torch
+    from reconstruction_program_taichi_gb300 import config, geometry, ops
+    o = _cone_obj(n=24, nz=10, nu=48, nv=16, views=20)
+    config.parse_ir(o, {"Lambda": 1e-3})
+    dg = geometry.ir_geometry(o)
+    g = torch.Generator(device="cuda").manual_seed(41)
+    mk = lambda: (torch.rand(dg.vol_shape, device="cuda", generator=g) - 0.3).to(torch.bfloat16)  # noqa: E731
+    x, r, d, q = mk(), mk(), mk(), mk()
+    f = lambda t: t.float().cpu().numpy().astype(np.float64)  # noqa: E731
+    bf = lambda a: torch.from_numpy(np.asarray(a, np.float32)).to(torch.bfloat16).float().numpy()  # noqa: E731
+    dot = float(ops.dot(r, d))
+    assert abs(dot - float((f(r) * f(d)).sum())) <= 1e-10 * abs(dot)
+    rr = ops.dot(r, r)
+    dq = ops.dot(d, q)
+    alpha = np.float32(float(rr) / float(dq))
+    x0, r0, d0, q0 = f(x), f(r), f(d), f(q)
+    rr_new = torch.empty((), dtype=torch.float64, device="cuda")
+    ops.cgls_update(rr, dq, x, r, d, q, rr_new)
+    xw = bf(x0.astype(np.float32) + alpha * d0.astype(np.float32))
+    rw = bf(r0.astype(np.float32) - alpha * q0.astype(np.float32))
+    assert np.array_equal(f(x).astype(np.float32), xw) and np.array_equal(f(r).astype(np.float32), rw)
+    assert abs(float(rr_new) - float((rw.astype(np.float64) ** 2).sum())) <= 1e-10 * float(rr_new)
+    beta = np.float32(float(rr_new) / float(rr))
+    ops.cgls_direction(rr, rr_new, r, d)
+    assert np.array_equal(f(d).astype(np.float32), bf(rw + beta * d0.astype(np.float32)))
+    # D^T W D on bf16 against the float32 path on the same (bf16-representable) values
+    wr = torch.rand(dg.vol_shape, device="cuda", generator=g)
+    out16 = ops.dtwd(dg, d, wr, 0.7, out_in=q, a=1.0, out=torch.empty_like(d))
+    out32 = ops.dtwd(dg, d.float(), wr, 0.7, out_in=q.float(), a=1.0)
+    assert torch.equal(out16, out32.to(torch.bfloat16))
+    dq2 = torch.empty((), dtype=torch.float64, device="cuda")
+    acc = q.clone()
+    ops.dtwd_dot(dg, d, wr, 0.7, acc, dq2)
+    assert torch.equal(acc, out16)
+    assert abs(float(dq2) - float((f(d) * f(acc)).sum())) <= 1e-10 * abs(float(dq2))
+    assert torch.equal(ops.tv_weights(dg, d, 1e-6), ops.tv_weights(dg, d.float(), 1e-6))
+
+
+def test_bf16_iterates_solve_close_to_float32(tmp_path, cuda):
+    """IRN-CGLS-PICCS with the iterates stored in bf16 (projector, backprojector and
+    vector kernels on bf16 volumes; float64 scalars) stays close to the float32 solve,
+    and the projector of a bf16 volume equals the projector of its float32 widening."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    from reconstruction_program_taichi_gb300.ir import Mgfbp_ir_piccs
+    z = load_golden("ir_piccs")
+    outs = []
+    for it in ("float32", "bfloat16"):
+        cfg = dict(z["config"], IterateStorage=it, NumberOfIRNIterations=2, NumberOfIterations=4)
+        path = tmp_path / f"prior_{it}.raw"
+        z["prior"].astype(np.float32).tofile(path)
+        cfg["PriorImageFile"] = str(path)
+        ir = Mgfbp_ir_piccs(cfg, verbose=False)
+        sgm = torch.from_numpy(z["input_sgm"].astype(np.float32)).cuda()
+        prior = torch.from_numpy(ir.img_prior.copy()).cuda()
+        outs.append(ir.solve_piccs(sgm, prior).cpu().numpy())
+        if it == "bfloat16":
+            sy = ir.system
+            v = torch.rand(sy.dg.vol_shape, device="cuda").to(torch.bfloat16)
+            assert torch.equal(ops.fp(sy.dg, v), ops.fp(sy.dg, v.float()))
+    assert rel_l2(outs[1], outs[0]) < 2e-2

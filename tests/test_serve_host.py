@@ -41,10 +41,15 @@ class _FakeSlot:
         self.obj = obj
         self.last_used = time.perf_counter()
 
-    def run(self, reqs):
+    def run(self, reqs, done=None):
         _FakeSlot.runs.append(len(reqs))
-        time.sleep(0.01)
-        return [np.asarray(r.sgm, np.float64).sum(axis=(0, 1)) for r in reqs]
+        outs = []
+        for i, r in enumerate(reqs):
+            time.sleep(0.01)
+            outs.append(np.asarray(r.sgm, np.float64).sum(axis=(0, 1)))
+            if done is not None and i + 1 < len(reqs):
+                done(i, outs[-1])
+        return outs
 
 
 @pytest.fixture
