@@ -25,7 +25,10 @@ struct FpParams {
     float stepvd, l_min, inv_px, inv_pz;
     float x0, y0, zoff;  // voxel (0,0) centre x, y; z0 = zoff + cz_view
     float zpv;
-    int vshift;  // fp_kernel: a block holds 2^vshift views x 8 / 2^vshift detector rows
+    // fp_kernel ray tiling: a block of 256 rays is 2^bcs detector columns x 2^vshift
+    // views x 2^(8 - bcs - vshift) detector rows, a warp 2^wcs columns x 2^(5 - wcs)
+    // of the block's (view, row) slots
+    int vshift, bcs, wcs;
 };
 
 struct Ray {
@@ -162,20 +165,21 @@ __device__ __forceinline__ bool spread_along_y(const FpParams& p, int j, const f
 // Grid of every ray kernel: x = 32-column detector tiles, y = views, z = 8-row
 // detector tiles.  Blocks are scheduled x, then y, then z, so the blocks resident at
 // one time cover many views of the same detector rows; those rays cross only a thin
-// z-slab of the volume, which then stays in L2 across views.  fp_kernel may instead
-// take 2^vshift consecutive views x 8 / 2^vshift rows per block (y = view groups,
-// z = row tiles); each ray's arithmetic is the same either way.
+// z-slab of the volume, which then stays in L2 across views.  fp_kernel with copies
+// instead takes tiles of 16 columns x 2^vshift consecutive views x 2^(4 - vshift)
+// rows (x = column tiles, y = view groups, z = row tiles), each warp 4 columns x 8
+// (view, row) slots; each ray's arithmetic is the same either way.
 //
-// One thread per ray (u, v) of view j = blockIdx.y.  vol is [z][y][x]; vol_t, when
+// One thread per ray (u, v) of view j.  vol is [z][y][x]; vol_t, when
 // given, is the same volume as [z][x][y]: views whose detector columns spread along
-// y read vol_t so that the 32 rays of a warp touch consecutive addresses.  With ZP
+// y read vol_t so that neighbouring rays touch consecutive addresses.  With ZP
 // (cone beam, workspace given) the volume is read from copies zp_x ([z][y][x]) and
 // zp_y ([z][x][y]): float32 quads (two adjacent 16-byte elements per cell reload) or
 // 16-bit cells (the whole 2x2x2 trilinear cell in one 16-byte element), below.
 
 // float32 quad copy, indexed in a (slow s, fast f) frame: (s, f) = (y, x) for views whose
 // detector columns spread along x (copy cx, [z][y][x]) and (x, y) for the others (copy
-// cy, [z][x][y]), so that the 32 rays of a warp read neighbouring elements.  Element
+// cy, [z][x][y]), so that neighbouring rays read neighbouring elements.  Element
 // (z, s, f) holds the z-pairs of the voxel and of its neighbour along s,
 //   {V(z, s, f), V(z+1, s, f), V(z, s+1, f), V(z+1, s+1, f)}    (16 bytes),
 // and the neighbour along f is the next element: a cell reload is two adjacent 16-byte
@@ -202,12 +206,13 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 }
 
 // Resident blocks per SM that the register allocation of fp_kernel targets.  The
-// float32 cone-beam path waits on L2 and needs its warps: with quad copies and 8 views
-// per block, 5 blocks (48 registers) take 267.3 ms at 512x512x256 / 1080 views, 4
-// blocks 273.8 ms, 6 blocks (40 registers, spilling) 317.1 ms; the fan-beam path keeps
-// 40 registers (6 blocks).  The 16-bit paths are issue-bound
-// and gain from registers: 1 (80 registers, 3 blocks of 256) gives bf16 237.4 ms
-// against 254.9 with 5 blocks, float16 274.4 against 291.7.
+// float32 cone-beam path waits on L1 and needs its warps: with quad copies and the
+// 16 x 16-view tiles, 5 blocks (48 registers) take 237.2 ms at 512x512x256 / 1080
+// views, 4 blocks 240.2 ms (8-view tiles: 5 blocks 267.3, 4 blocks 273.8, 6 blocks,
+// 40 registers with spills, 317.1); the fan-beam path keeps 40 registers (6 blocks).
+// The 16-bit paths are issue-bound and gain from registers: 1 (80 registers, 3 blocks
+// of 256) gives bf16 237.4 ms against 254.9 with 5 blocks (8-view tiles), float16
+// 274.4 against 291.7; with the 16-column tiles 1 and 2 blocks are equal (224.0).
 template <bool CONE, typename ZT>
 struct FpMinBlocks {
     static constexpr int value = (std::is_same<ZT, uint4>::value || std::is_same<ZT, h16x8>::value) ? 1
@@ -222,10 +227,17 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
           const float* __restrict__ pxs, const float* __restrict__ vol, const float* __restrict__ vol_t,
           const ZT* __restrict__ zp_x, const ZT* __restrict__ zp_y, const float* __restrict__ mask,
           float* __restrict__ sgm, const uint32_t* __restrict__ f16_max) {
-    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    // ray of this thread: column tx and (view, row) slot ty of the block's tile, warps
+    // of 2^wcs columns x 2^(5 - wcs) slots
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int gpr = p.bcs - p.wcs;  // log2 of the warps across the tile's columns
+    const int tx = ((warp & ((1 << gpr) - 1)) << p.wcs) + (lane & ((1 << p.wcs) - 1));
+    const int ty = ((warp >> gpr) << (5 - p.wcs)) + (lane >> p.wcs);
+    const int iu = (blockIdx.x << p.bcs) + tx;
     const int vs = p.vshift;
-    const int iv = blockIdx.z * (blockDim.y >> vs) + (threadIdx.y >> vs);
-    const int j = (blockIdx.y << vs) + (threadIdx.y & ((1 << vs) - 1));
+    const int iv = (blockIdx.z << (8 - p.bcs - vs)) + (ty >> vs);
+    const int j = (blockIdx.y << vs) + (ty & ((1 << vs) - 1));
     if (iu >= p.nu || iv >= p.nv || j >= p.views) return;
     const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
     if (mask && mask[oidx] != 1.0f) {
@@ -338,32 +350,33 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
             else acc += val;
         };
         // Interior samples (at least 1e-3 voxel inside on every axis).  With copies
-        // the floors come from the 1.5 * 2^23 rounding constant, on the FMA pipe
-        // instead of the conversion unit (which otherwise limits the 16-bit kernels
-        // and costs the float32 one 5 ms at 512x512x256 / 1080 views).
-        // Round-to-nearest of f - 0.5 is floor(f), or floor(f) - 1 at an exact integer
-        // f, where the interpolant has the same value from either cell (weight 1 in the
-        // lower one); both cells lie inside the volume.  The element offset is summed in
-        // unsigned arithmetic (the bias terms wrap, the total is the offset, below 2^31).
+        // the floors come from adding M = 1.5 * 2^23 rounded toward -infinity (exactly
+        // M + floor(f) for |f| < 2^22), on the FMA pipe instead of the conversion unit
+        // (which otherwise limits the 16-bit kernels), and the x and y coordinates
+        // travel as one f32x2 pair: position, floor and weight are three packed
+        // operations for both axes.  The element offset is summed in unsigned arithmetic
+        // (the bias terms wrap, the total is the offset, below 2^31).
         constexpr bool kRoundFloor = ZP && !std::is_same<ZT, float2>::value;
         const float M = 12582912.0f;
         const unsigned MB = 0x4B400000u;  // bit pattern of M
-        const float hx0 = r.fx0 - 0.5f, hy0 = r.fy0 - 0.5f, hz0 = r.fz0 - 0.5f;
         const unsigned obias = CONE ? MB * (unsigned)(plane + sy + sx) : MB * (unsigned)(sy + sx) - (unsigned)(iv * plane);
+        const float2 dxy = make_float2(r.dfx, r.dfy), fxy0 = make_float2(r.fx0, r.fy0);
+        const float2 M2 = make_float2(M, M), nM2 = make_float2(-M, -M);
         auto sample_fast = [&](float fk) {
-            const float tx = fmaf(fk, r.dfx, hx0), ty = fmaf(fk, r.dfy, hy0);
-            const float mx = tx + M, my = ty + M;
-            const float xw = (tx - (mx - M)) + 0.5f, yw = (ty - (my - M)) + 0.5f;
-            unsigned off = (unsigned)__float_as_int(mx) * (unsigned)sx + (unsigned)__float_as_int(my) * (unsigned)sy - obias;
+            const float2 f = __ffma2_rn(make_float2(fk, fk), dxy, fxy0);  // fractional indices x, y
+            const float2 m = __fadd2_rd(f, M2);                            // M + floor(f)
+            const float2 fl = __fadd2_rn(m, nM2);                          // floor(f), exact
+            const float2 w = __fadd2_rn(f, make_float2(-fl.x, -fl.y));     // weights, exact
+            unsigned off = (unsigned)__float_as_int(m.x) * (unsigned)sx + (unsigned)__float_as_int(m.y) * (unsigned)sy - obias;
             float zw = 0.0f;
             if (CONE) {
-                const float tz = fmaf(fk, r.dfz, hz0);
-                const float mz = tz + M;
-                zw = (tz - (mz - M)) + 0.5f;
+                const float fz = fmaf(fk, r.dfz, r.fz0);
+                const float mz = __fadd_rd(fz, M);
+                zw = fz - (mz - M);
                 off += (unsigned)__float_as_int(mz) * (unsigned)plane;
             }
             load_cell((int)off);
-            acc += interp(xw, yw, zw);
+            acc += interp(w.x, w.y, zw);
         };
         int kis, kie;
         interior_range(p, r, CONE, kis, kie);
@@ -770,6 +783,9 @@ int make_params(const mct_geom* g, FpParams& p, const char* who) {
     p.y0 = (float)(-(g->nx - 1.0) / 2.0 * (-px) + g->cy);
     p.zoff = (float)(-(g->nz - 1.0) / 2.0 * (double)g->pz);
     p.zpv = g->fp_z_per_view;
+    p.vshift = 0;
+    p.bcs = 5;  // 32 columns x 8 rows of one view, warps of 32 columns
+    p.wcs = 5;
     return MCT_OK;
 }
 
@@ -828,13 +844,25 @@ int fp_storage_impl(const mct_geom* g, const mct_tables* t, const TIN* vol_in, c
         return MCT_OK;
     }
     dim3 tb(32, 8), tg((g->nx + 31) / 32, (g->nx + 31) / 32, g->nz);
-    // Blocks of 8 consecutive views x 1 detector row for float32 quad copies (at
-    // 512x512x256 / 1080 views: 267.3 ms; 4 views x 2 rows 276.9, 2 x 4 293.8, 1 x 8
-    // 306.5); 4 views x 2 rows for 16-bit cells (bf16 254.8 ms against 261.4 with 1 x 8);
-    // 8 rows of one view without copies.
-    p.vshift = (p.cone && workspace) ? (dtype == MCT_F32 ? 3 : 2) : 0;
-    const int vb = 1 << p.vshift, rb = 8 >> p.vshift;
-    dim3 block(32, 8), grid((g->nu + 31) / 32, (g->views + vb - 1) / vb, (g->nv + rb - 1) / rb);
+    // Ray tiles with copies: 16 detector columns x 16 consecutive views of one row
+    // (float32 quads) or 16 columns x 4 views x 4 rows (16-bit cells), warps of 4
+    // columns x 8 (view, row) slots.  The rays of neighbouring views cross nearly the
+    // same cells at the same step, so a compact warp touches fewer L1 lines per
+    // reload than 32 columns of one view.  Measured at 512x512x256 / 1080 views
+    // (float32 / bf16 ms): 32 columns x 8 views with warps of 32 columns 263.6 / 230.5,
+    // of 8 x 4 248.1 / 223.3, of 4 x 8 244.7 / 223.5; 16 x 16 views with warps of
+    // 4 x 8 237.2 / 224.0 (bf16 with 4 views x 4 rows: 222.2), 2 x 16 244.8 / 222.9,
+    // 8 x 4 240.8 / 224.2; 8 x 32 views with warps of 2 x 16 245.4 / 226.9, 1 x 32
+    // 255.9 / 227.1.  Short scans keep 4 views x 4 rows: float32 at 512x512x128 / 90
+    // views 12.96 ms against 14.34 with 16 views (512x512x64 / 360 views: 21.55 against
+    // 20.92).  Without copies: 32 columns x 8 rows of one view.
+    if (p.cone && workspace) {
+        p.vshift = (dtype == MCT_F32 && g->views >= 256) ? 4 : 2;
+        p.bcs = 4;
+        p.wcs = 2;
+    }
+    const int vb = 1 << p.vshift, rb = 1 << (8 - p.bcs - p.vshift), cb = 1 << p.bcs;
+    dim3 block(32, 8), grid((g->nu + cb - 1) / cb, (g->views + vb - 1) / vb, (g->nv + rb - 1) / rb);
     const size_t n = (size_t)g->nz * g->nx * g->nx;
     if (p.cone && workspace && dtype == MCT_BF16) {
         uint4* cx = static_cast<uint4*>(workspace);
