@@ -32,7 +32,10 @@ PROF = dict(WORKLOAD, views=36, nz=160)
 # the same with 180 views: enough views per detector-row tile for the projector's L2
 # reuse to resemble the benchmark's (about 3.5 GB on the device)
 PROF180 = dict(PROF, views=180)
-WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF, "prof180": PROF180}
+# 270 views: scans of 256 views or more take the projector's 16-view ray tiles, as at
+# 1080 views (about 4 GB on the device)
+PROF270 = dict(PROF, views=270)
+WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF, "prof180": PROF180, "prof270": PROF270}
 
 
 def make_config(w):
@@ -1208,7 +1211,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
-                    help="c2: the benchmark; small: quick checks; prof, prof180: short launches for ncu captures")
+                    help="c2: the benchmark; small: quick checks; prof, prof180, prof270: short launches for ncu "
+                         "captures")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cgls", action="store_true")

@@ -383,7 +383,11 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
         for (int k = r.ks; k < kis; ++k) sample(k, true);
         if constexpr (kRoundFloor) {
             float fk = (float)kis;
-#pragma unroll 4
+            // unrolled 4 times for float32 quads, twice for 16-bit cells (at 512x512x256 /
+            // 1080 views: float32 237.4 ms against 239.6 with 2; bf16 215.7 against 222.1
+            // with 4)
+            constexpr int kUnroll = kQuad ? 4 : 2;
+#pragma unroll kUnroll
             for (int k = kis; k <= kie; ++k, fk += 1.0f) sample_fast(fk);
         } else {
 #pragma unroll 4
