@@ -330,6 +330,23 @@ int mct_tv_penalty(const mct_geom* g, const float* x, float beta, double* partia
 /* Scratch bytes needed by the float64 reductions below. */
 size_t mct_reduce_scratch_size(void);
 
+/* The operator application of one CG step with the vector work in the backprojector's
+ * epilogue: q = P^T p + s1 * D^T W1 D d (+ s2 * D^T W2 D d when wr2 is given; no TV
+ * term when wr1 is NULL), each term added to the running value in that order, and
+ * *dq = sum d[i] * q[i] in float64 over the stored q (device scalar, overwritten), so
+ * q is written once and never re-read.  p is the packed sinogram of
+ * mct_bp_ref_unmatched_packed (dtype its storage type); d and q are volumes of
+ * vec_dtype (MCT_F32 or MCT_BF16), wr1 / wr2 float32.  Axial view mode, cone beam.
+ * partials: device scratch of mct_bp_cg_partials_size(g) bytes (one float64 per
+ * block, summed in a fixed order).  Replaces, per CG iteration of TikhonovSol
+ * (run_mgfbp_iterative_recon_IRN_CGLS.py:198-203; ..._piccs.py:120-125), the
+ * BackProjection of ForwardProjectionAndBackProjection (:288-316, kernel :372-474),
+ * the Dt_W_D terms (:267-286) and np.sum(d * q). */
+size_t mct_bp_cg_partials_size(const mct_geom* g);
+int mct_bp_ref_unmatched_packed_cg(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
+                                   const void* d, const float* wr1, float s1, const float* wr2, float s2, void* q,
+                                   int32_t vec_dtype, double* partials, double* dq, void* stream);
+
 /* *result = sum a[i]*b[i] in float64 (device scalar).  Replaces the np.sum inner
  * products of TikhonovSol run_mgfbp_iterative_recon_IRN_CGLS.py:202-203, 216. */
 int mct_dot_f64(const float* a, const float* b, int64_t n, double* partials, double* result,

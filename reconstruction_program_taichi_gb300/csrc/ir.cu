@@ -140,15 +140,61 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
 // operands, 80 for 8-byte ones) lets all UA_ZC gathers of a view issue before their
 // arithmetic, which hides the gather latency.
 constexpr int UA_ZC = 16;
+
+// (D^T W D x)[i] of run_mgfbp_iterative_recon_IRN_CGLS.py:267-286: forward differences
+// weighted by W, their transposed differences on the interior indices [1, n-2] of each
+// axis (z only when nz > 2), 0 on the borders.
+template <typename T>
+__device__ __forceinline__ float dtwd_at(const T* __restrict__ x, const float* __restrict__ wr, int nx, int nz,
+                                         int64_t i, int iz, int iy, int ix) {
+    const int64_t plane = (int64_t)nx * nx;
+    const float c = ldv(x, i);
+    float r = 0.0f;
+    if (iy >= 1 && iy <= nx - 2) {  // uxx = Ux[y] - Ux[y-1]
+        const float ux_c = wr[i] * (ldv(x, i + nx) - c);
+        const float ux_m = wr[i - nx] * (c - ldv(x, i - nx));
+        r -= ux_c - ux_m;
+    }
+    if (ix >= 1 && ix <= nx - 2) {
+        const float uy_c = wr[i] * (ldv(x, i + 1) - c);
+        const float uy_m = wr[i - 1] * (c - ldv(x, i - 1));
+        r -= uy_c - uy_m;
+    }
+    if (nz > 2 && iz >= 1 && iz <= nz - 2) {
+        const float uz_c = wr[i] * (ldv(x, i + plane) - c);
+        const float uz_m = wr[i - plane] * (c - ldv(x, i - plane));
+        r -= uz_c - uz_m;
+    }
+    return r;
+}
+
+// value as stored in a volume of type T (bf16 iterates: rounded to nearest)
+template <typename T>
+__device__ __forceinline__ float stored(float v);
+template <>
+__device__ __forceinline__ float stored<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float stored<__nv_bfloat16>(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
+// CG epilogue of the backprojector (the operator application of one CGLS step):
+// q = P^T p + s1 D^T W1 D d (+ s2 D^T W2 D d), and the block's float64 partial of <d, q>
+// over the stored q.  d and q are volumes of the kernel's output type.
+struct CgEpi {
+    const void* d;
+    const float* w1;
+    const float* w2;
+    float s1, s2;
+    double* partials;  // one per block, in blockIdx order
+};
 template <typename QT>
 constexpr int ua_min_blocks() {
     return sizeof(QT) == 8 ? 3 : 2;
 }
-template <bool CONE, typename QT, typename PT, typename OT = float>
+template <bool CONE, typename QT, typename PT, typename OT = float, bool EPI = false>
 __global__ void __launch_bounds__(UB_TX* UB_TY, ua_min_blocks<QT>())
 bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
                           const void* __restrict__ packed, OT* __restrict__ vol,
-                          const uint32_t* __restrict__ f16_max) {
+                          const uint32_t* __restrict__ f16_max, CgEpi epi = CgEpi{}) {
     const int nq = p.nu - 1;  // packed: nv rows of nu-1 coefficient sets per view
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, sid*cos b}
     __shared__ float tab_s[UB_VCHUNK];  // sid*sin b
@@ -235,9 +281,47 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
             }
         }
     }
-    if (!active) return;
     const int64_t plane = (int64_t)p.nx * p.nx;
     const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
+    if constexpr (EPI) {
+        // q = P^T p + s1 D^T W1 D d (+ s2 D^T W2 D d) in the order of the separate passes
+        // (each term added to the stored value), then <d, q> of the stored q.  The
+        // backprojection is stored first, as without the epilogue, and the terms are
+        // added in a compact loop over the thread's own slices (a loop that indexes
+        // acc[] at run time would move the accumulators to local memory, and an
+        // unrolled stencil costs the main loop registers).
+        const OT* d = static_cast<const OT*>(epi.d);
+        double dsum = 0.0;
+        if (active) {
+#pragma unroll
+            for (int k = 0; k < UA_ZC; ++k)
+                if (zb + k < p.nz) stv(vol, (zb + k) * plane + (int64_t)iy * p.nx + ix, trunc ? 0.0f : acc[k] * unscale);
+#pragma unroll 1
+            for (int k = 0; k < UA_ZC && zb + k < p.nz; ++k) {
+                const int64_t i = (zb + k) * plane + (int64_t)iy * p.nx + ix;
+                float v = ldv(vol, i);  // this thread's own store
+                if (epi.w1) v = __fadd_rn(__fmul_rn(epi.s1, dtwd_at(d, epi.w1, p.nx, p.nz, i, zb + k, iy, ix)), v);
+                if (epi.w2) v = __fadd_rn(__fmul_rn(epi.s2, dtwd_at(d, epi.w2, p.nx, p.nz, i, zb + k, iy, ix)), v);
+                stv(vol, i, v);
+                dsum += (double)ldv(d, i) * (double)stored<OT>(v);
+            }
+        }
+        // block sum over the 256 threads, then one partial per block
+        __shared__ double red[UB_TX * UB_TY / 32];
+        const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+        if (lane == 0) red[w] = dsum;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+#pragma unroll
+            for (int q = 0; q < UB_TX * UB_TY / 32; ++q) t += red[q];
+            epi.partials[((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
+        }
+        return;
+    }
+    if (!active) return;
 #pragma unroll
     for (int k = 0; k < UA_ZC; ++k)
         if (zb + k < p.nz) stv(vol, (zb + k) * plane + (int64_t)iy * p.nx + ix, trunc ? 0.0f : acc[k] * unscale);
@@ -330,22 +414,7 @@ dtwd_kernel(int nx, int nz, const T* __restrict__ x, const float* __restrict__ w
         const int iy = (int)((i / nx) % nx);
         const int iz = (int)(i / plane);
         const float c = ldv(x, i);
-        float r = 0.0f;
-        if (iy >= 1 && iy <= nx - 2) {  // uxx = Ux[y] - Ux[y-1]
-            const float ux_c = wr[i] * (ldv(x, i + nx) - c);
-            const float ux_m = wr[i - nx] * (c - ldv(x, i - nx));
-            r -= ux_c - ux_m;
-        }
-        if (ix >= 1 && ix <= nx - 2) {
-            const float uy_c = wr[i] * (ldv(x, i + 1) - c);
-            const float uy_m = wr[i - 1] * (c - ldv(x, i - 1));
-            r -= uy_c - uy_m;
-        }
-        if (nz > 2 && iz >= 1 && iz <= nz - 2) {
-            const float uz_c = wr[i] * (ldv(x, i + plane) - c);
-            const float uz_m = wr[i - plane] * (c - ldv(x, i - plane));
-            r -= uz_c - uz_m;
-        }
+        const float r = dtwd_at(x, wr, nx, nz, i, iz, iy, ix);
         float v = s * r;
         if (a != 0.0f) v += a * ldv(out_in, i);
         stv(out, i, v);
@@ -515,6 +584,53 @@ int mct_bp_ref_unmatched_packed_out(const mct_geom* g, const mct_tables* t, cons
         bp_unmatched_axial_kernel<true, h16x4, h16x2, __nv_bfloat16><<<grid, block, 0, s>>>(
             p, t->angles, t->cz, g->cz, packed, out, f16_trailer(g, packed));
     return launched("bp_unmatched_kernel");
+}
+
+size_t mct_bp_cg_partials_size(const mct_geom* g) {
+    if (!g || g->nx < 1 || g->nz < 1) return 0;
+    return (size_t)((g->nx + UB_TX - 1) / UB_TX) * (size_t)((g->nx + UB_TY - 1) / UB_TY) *
+           (size_t)((g->nz + UA_ZC - 1) / UA_ZC) * sizeof(double);
+}
+
+int mct_bp_ref_unmatched_packed_cg(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype,
+                                   const void* d, const float* wr1, float s1, const float* wr2, float s2, void* q,
+                                   int32_t vec_dtype, double* partials, double* dq, void* stream) {
+    UbParams p{};
+    MCT_TRY(unmatched_params(g, p));
+    MCT_REQUIRE(t && t->angles && packed && d && q && partials && dq, "mct_bp_ref_unmatched_packed_cg: NULL buffer");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16 || dtype == MCT_F16,
+                "mct_bp_ref_unmatched_packed_cg: dtype must be MCT_F32, MCT_BF16 or MCT_F16");
+    MCT_REQUIRE(vec_dtype == MCT_F32 || vec_dtype == MCT_BF16,
+                "mct_bp_ref_unmatched_packed_cg: vec_dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(g->view_mode == 1 && p.cone,
+                "mct_bp_ref_unmatched_packed_cg: the fused epilogue needs the axial view mode and cone beam");
+    MCT_REQUIRE(wr1 || !wr2, "mct_bp_ref_unmatched_packed_cg: wr2 given without wr1");
+    MCT_REQUIRE(q != d && q != (const void*)wr1 && q != (const void*)wr2 && q != packed,
+                "mct_bp_ref_unmatched_packed_cg: q aliases an input");
+    MCT_REQUIRE((int64_t)g->nv * (g->nu - 1) < ((int64_t)1 << 31), "mct_bp_ref_unmatched_packed_cg: detector too large");
+    cudaStream_t s = as_stream(stream);
+    dim3 block(UB_TX, UB_TY);
+    dim3 grid((g->nx + UB_TX - 1) / UB_TX, (g->nx + UB_TY - 1) / UB_TY, (g->nz + UA_ZC - 1) / UA_ZC);
+    const CgEpi e{d, wr1, wr2, s1, s2, partials};
+    const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
+    auto go = [&](auto out_tag) {
+        using OT = decltype(out_tag);
+        OT* out = static_cast<OT*>(q);
+        if (dtype == MCT_F32)
+            bp_unmatched_axial_kernel<true, float4, float2, OT, true><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz,
+                                                                                           packed, out, nullptr, e);
+        else if (dtype == MCT_BF16)
+            bp_unmatched_axial_kernel<true, uint2, uint32_t, OT, true><<<grid, block, 0, s>>>(
+                p, t->angles, t->cz, g->cz, packed, out, nullptr, e);
+        else
+            bp_unmatched_axial_kernel<true, h16x4, h16x2, OT, true><<<grid, block, 0, s>>>(p, t->angles, t->cz, g->cz,
+                                                                                         packed, out, fm, e);
+    };
+    if (vec_dtype == MCT_F32) go(float{});
+    else go(__nv_bfloat16{});
+    MCT_TRY(launched("bp_unmatched_kernel"));
+    finish_sum_kernel<<<1, RED_THREADS, 0, s>>>(partials, (int)(grid.x * grid.y * grid.z), dq);
+    return launched("finish_sum_kernel");
 }
 
 int mct_bp_ref_unmatched_packed(const mct_geom* g, const mct_tables* t, const void* packed, int32_t dtype, float* vol,

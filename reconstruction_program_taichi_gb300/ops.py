@@ -349,6 +349,31 @@ def bp_unmatched(dg, sgm, out=None):
     return out
 
 
+def bp_unmatched_packed_cg(dg, packed, dtype, d, terms, q, dq_out):
+    """One CG operator application with the vector work in the backprojector's
+    epilogue: q = P^T p + sum_t s_t D^T W_t D d (terms: up to two (s, W) pairs, added in
+    order) and dq_out = <d, q> (float64 device scalar) over the stored q.  Axial view
+    mode, cone beam; d and q both float32 or both bf16, each W float32."""
+    vdt = _vec_dtype(d, "d", dg.vol_shape)
+    if _vec_dtype(q, "q", dg.vol_shape) != vdt:
+        raise TypeError("q must have the dtype of d")
+    if len(terms) > 2:
+        raise ValueError("at most two D^T W D terms")
+    ws = [None, None]
+    ss = [0.0, 0.0]
+    for k, (sk, wk) in enumerate(terms):
+        _check(wk, "W", dg.vol_shape)
+        ws[k], ss[k] = wk, float(sk)
+    part = dg.__dict__.get("_cg_partials")
+    if part is None:
+        n = int(_lib.load().mct_bp_cg_partials_size(dg.g())) // 8
+        part = torch.empty(max(n, 1), dtype=torch.float64, device=dg.device)
+        dg.__dict__["_cg_partials"] = part
+    _lib.call("mct_bp_ref_unmatched_packed_cg", dg.g(), dg.t(), _ptr(packed), int(dtype), _ptr(d), _ptr(ws[0]), ss[0],
+              _ptr(ws[1]), ss[1], _ptr(q), vdt, _ptr(part), _ptr(dq_out), _stream())
+    return q
+
+
 def tv_weights(dg, x, beta, out=None):
     """WR = 1/sqrt(|D x|^2 + beta) as float32; x float32 or bf16."""
     xdt = _vec_dtype(x, "x", dg.vol_shape)

@@ -754,3 +754,60 @@ def test_bf16_iterates_solve_close_to_float32(tmp_path, cuda):
             v = torch.rand(sy.dg.vol_shape, device="cuda").to(torch.bfloat16)
             assert torch.equal(ops.fp(sy.dg, v), ops.fp(sy.dg, v.float()))
     assert rel_l2(outs[1], outs[0]) < 2e-2
+
+
+@pytest.mark.parametrize("n_terms", [0, 1, 2])
+@pytest.mark.parametrize("it", ["float32", "bfloat16"])
+def test_fused_cg_epilogue_matches_separate_passes(cuda, n_terms, it):
+    """The backprojector with the CG vector work in its epilogue
+    (mct_bp_ref_unmatched_packed_cg) against the separate passes it replaces: the
+    backprojection into q, q += s_k D^T W_k D d per TV term, and <d, q> in float64.
+    float32 iterates agree to float32 rounding; bf16 iterates to the one bf16 rounding
+    the fused q skips (the separate passes round q after each term)."""
+    import torch
+    from reconstruction_program_taichi_gb300 import config, geometry, ops
+    o = _cone_obj(n=40, nz=19, nu=80, nv=36, views=60)
+    config.parse_ir(o, {"Lambda": 1e-3})
+    dg = geometry.ir_geometry(o)
+    dt = {"float32": torch.float32, "bfloat16": torch.bfloat16}[it]
+    g = torch.Generator(device="cuda").manual_seed(7 + n_terms)
+    d = (torch.rand(dg.vol_shape, device="cuda", generator=g) - 0.4).to(dt)
+    terms = [(0.37 * (k + 1), torch.rand(dg.vol_shape, device="cuda", generator=g) + 0.1) for k in range(n_terms)]
+    sgm = torch.rand(dg.sgm_shape, device="cuda", generator=g)
+    for storage in (ops.MCT_F32, ops.MCT_BF16):
+        packed = ops.pack_sinogram(dg, sgm, dtype=storage)
+        ref = ops.bp_unmatched_packed(dg, packed, dtype=storage, out=torch.empty(dg.vol_shape, dtype=dt, device="cuda"))
+        for s, w in terms:
+            ops.dtwd(dg, d, w, s, out_in=ref, a=1.0, out=ref)
+        dq_ref = float(ops.dot(d, ref))
+        q = torch.full(dg.vol_shape, float("nan"), dtype=dt, device="cuda")
+        dq = torch.empty((), dtype=torch.float64, device="cuda")
+        ops.bp_unmatched_packed_cg(dg, packed, storage, d, terms, q, dq)
+        tol = 1e-6 if it == "float32" else 1e-2
+        assert torch.isfinite(q.float()).all()
+        assert rel_l2(q.float().cpu().numpy(), ref.float().cpu().numpy()) < tol
+        # <d, q> is the float64 sum over the stored q
+        exact = float((d.double() * q.double()).sum())
+        assert abs(float(dq) - exact) <= 1e-12 * abs(exact) + 1e-300
+        assert abs(float(dq) - dq_ref) <= (1e-6 if it == "float32" else 1e-2) * abs(dq_ref)
+
+
+def test_fused_cg_solve_matches_separate_passes(cuda):
+    """A whole IRN-CGLS-PICCS solve (two TV terms per operator) with the fused epilogue
+    against the same solve with the separate passes."""
+    import torch
+    from reconstruction_program_taichi_gb300.ir import Mgfbp_ir_piccs
+    z = load_golden("ir_piccs")
+    outs = []
+    for fuse in (True, False):
+        cfg = dict(z["config"], NumberOfIRNIterations=2, NumberOfIterations=4)
+        path = f"/tmp/mct_prior_fuse_{int(fuse)}.raw"
+        z["prior"].astype(np.float32).tofile(path)
+        cfg["PriorImageFile"] = path
+        ir = Mgfbp_ir_piccs(cfg, verbose=False)
+        ir.system.fuse = fuse
+        assert ir.system.fused_cg(2) == fuse
+        sgm = torch.from_numpy(z["input_sgm"].astype(np.float32)).cuda()
+        prior = torch.from_numpy(ir.img_prior.copy()).cuda()
+        outs.append(ir.solve_piccs(sgm, prior).cpu().numpy())
+    assert rel_l2(outs[0], outs[1]) < 1e-5
