@@ -27,8 +27,9 @@ struct FpParams {
     float zpv;
     // fp_kernel ray tiling: a block of 256 rays is 2^bcs detector columns x 2^vshift
     // views x 2^(8 - bcs - vshift) detector rows, a warp 2^wcs columns x 2^(5 - wcs)
-    // of the block's (view, row) slots
-    int vshift, bcs, wcs;
+    // of the block's (view, row) slots; blockIdx.y runs over 2^rs row tiles within
+    // each view group (the block order is column tile, row tile, view group, row group)
+    int vshift, bcs, wcs, rs;
 };
 
 struct Ray {
@@ -236,8 +237,9 @@ fp_kernel(FpParams p, const float* __restrict__ angles, const float* __restrict_
     const int ty = ((warp >> gpr) << (5 - p.wcs)) + (lane >> p.wcs);
     const int iu = (blockIdx.x << p.bcs) + tx;
     const int vs = p.vshift;
-    const int iv = (blockIdx.z << (8 - p.bcs - vs)) + (ty >> vs);
-    const int j = (blockIdx.y << vs) + (ty & ((1 << vs) - 1));
+    const int vg = blockIdx.y >> p.rs, rsub = blockIdx.y & ((1 << p.rs) - 1);  // view group, row tile in it
+    const int iv = ((((int)blockIdx.z << p.rs) + rsub) << (8 - p.bcs - vs)) + (ty >> vs);
+    const int j = (vg << vs) + (ty & ((1 << vs) - 1));
     if (iu >= p.nu || iv >= p.nv || j >= p.views) return;
     const int64_t oidx = ((int64_t)iv * p.views + j) * p.nu + iu;
     if (mask && mask[oidx] != 1.0f) {
@@ -790,6 +792,7 @@ int make_params(const mct_geom* g, FpParams& p, const char* who) {
     p.vshift = 0;
     p.bcs = 5;  // 32 columns x 8 rows of one view, warps of 32 columns
     p.wcs = 5;
+    p.rs = 0;
     return MCT_OK;
 }
 
@@ -860,13 +863,20 @@ int fp_storage_impl(const mct_geom* g, const mct_tables* t, const TIN* vol_in, c
     // 255.9 / 227.1.  Short scans keep 4 views x 4 rows: float32 at 512x512x128 / 90
     // views 12.96 ms against 14.34 with 16 views (512x512x64 / 360 views: 21.55 against
     // 20.92).  Without copies: 32 columns x 8 rows of one view.
+    // The 16-view tiles take 4 rows in turn per view group (row tile, then view group):
+    // neighbouring rows' rays cross nearly the same cells, and the outer rows' slab (up
+    // to ~50 planes) does not fit L2 across all views.  DRAM per launch at 512x512x256 /
+    // 1080 views: 31.3 GB with one row at a time, 19.1 GB with 2 (236.3 ms), 12.8 GB
+    // with 4 (237.8 ms against 237.6), 10.7 GB with 8 (238.7 ms); the 16-bit tiles already
+    // span 4 rows (2 more in turn: 219.7 against 215.9 ms).
     if (p.cone && workspace) {
         p.vshift = (dtype == MCT_F32 && g->views >= 256) ? 4 : 2;
         p.bcs = 4;
         p.wcs = 2;
+        p.rs = p.vshift == 4 ? 2 : 0;
     }
-    const int vb = 1 << p.vshift, rb = 1 << (8 - p.bcs - p.vshift), cb = 1 << p.bcs;
-    dim3 block(32, 8), grid((g->nu + cb - 1) / cb, (g->views + vb - 1) / vb, (g->nv + rb - 1) / rb);
+    const int vb = 1 << p.vshift, rb = 1 << (8 - p.bcs - p.vshift + p.rs), cb = 1 << p.bcs;
+    dim3 block(32, 8), grid((g->nu + cb - 1) / cb, ((g->views + vb - 1) / vb) << p.rs, (g->nv + rb - 1) / rb);
     const size_t n = (size_t)g->nz * g->nx * g->nx;
     if (p.cone && workspace && dtype == MCT_BF16) {
         uint4* cx = static_cast<uint4*>(workspace);
