@@ -576,9 +576,11 @@ def irn_bench(dev, stream, barrier, checks=None):
            "operator": "reference pair (masked FP + per-view BP)"}
     ph = None
     # (result key, gather storage, measured-sinogram storage); "float16_sinogram" is the
-    # configuration's own precision plan: FP16 sinogram storage, float32 accumulation
+    # configuration's own precision plan: the measured sinogram stored in FP16, the
+    # operator applications on 16-bit (bf16) gathers, float32 accumulation, float64 CG
+    # scalars
     variants = (("float32", "float32", "float32"), ("bfloat16", "bfloat16", "float32"),
-                ("float16", "float16", "float32"), ("float16_sinogram", "float16", "float16"))
+                ("float16", "float16", "float32"), ("float16_sinogram", "bfloat16", "float16"))
     for key, storage, sino in variants:
         cfg = make_config(C3)
         cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "NumberOfIRNIterations": 20, "NumberOfIterations": 10,
