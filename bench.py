@@ -798,15 +798,16 @@ def widen_bench(dev, stream, barrier):
     return out
 
 
-def cg_step_bench(dev):
-    """One TV reweighting and a 3-iteration CG solve at the C3 geometry (float32): the
-    CG kernels (projector, backprojector, TV weights, fused stencil and inner product,
-    vector updates) launched a few times each.  Returns the solve's milliseconds."""
+def cg_step_bench(dev, storage="float32"):
+    """One TV reweighting and a 3-iteration CG solve at the C3 geometry (gathers stored
+    as `storage`): the CG kernels (projector, backprojector, TV weights, stencil and
+    inner product -- in the backprojector's epilogue with 16-bit gathers -- vector
+    updates) launched a few times each.  Returns the solve's milliseconds."""
     import torch
     from reconstruction_program_taichi_gb300 import ops
     from reconstruction_program_taichi_gb300.ir import Mgfbp_ir
     cfg = make_config(C3)
-    cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6})
+    cfg.update({"Lambda": 1e-3, "BetaTV": 1e-6, "StoragePrecision": storage})
     ir = Mgfbp_ir(cfg, device=dev, verbose=False)
     sy = ir.system
     sgm = noisy(ops.project_ellipsoids(sy.dg, ellipsoids(C3)), C3["photons"], C3["seed"])
@@ -1245,7 +1246,8 @@ def main():
         import torch
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
-        print(json.dumps({"cg_step_ms": cg_step_bench(dev)}))
+        storage = {"f32": "float32", "bf16": "bfloat16", "f16": "float16"}[args.storage]
+        print(json.dumps({"cg_step_ms": cg_step_bench(dev, storage)}))
     elif args.only == "helical":
         import torch
         dev = torch.device("cuda", 0)

@@ -67,17 +67,20 @@ class IrSystem:
     def fp(self, x, out=None):
         return ops.fp(self.dg, x, mask=self.mask, out=out, dtype=self.fp_dtype)
 
-    def bp(self, sgm, out=None, dtype=None):
-        if self.matched:
-            return ops.fp_adjoint(self.dg, sgm, mask=self.mask, out=out)
-        # pack the sinogram into one-gather bilinear coefficients, then backproject
-        dtype = self.dtype if dtype is None else dtype
+    def _pack(self, sgm, dtype):
+        """The sinogram as one-gather bilinear coefficients of storage type dtype, in a
+        buffer kept per type."""
         packed = self.__dict__.setdefault("_packed", {})
         if dtype not in packed:
             packed[dtype] = torch.empty(max(ops.packed_bytes(self.dg, dtype), 16), dtype=torch.uint8,
                                         device=self.device)
-        ops.pack_sinogram(self.dg, sgm, dtype=dtype, out=packed[dtype])
-        return ops.bp_unmatched_packed(self.dg, packed[dtype], dtype=dtype, out=out)
+        return ops.pack_sinogram(self.dg, sgm, dtype=dtype, out=packed[dtype])
+
+    def bp(self, sgm, out=None, dtype=None):
+        if self.matched:
+            return ops.fp_adjoint(self.dg, sgm, mask=self.mask, out=out)
+        dtype = self.dtype if dtype is None else dtype
+        return ops.bp_unmatched_packed(self.dg, self._pack(sgm, dtype), dtype=dtype, out=out)
 
     def ptp(self, x, out=None, full_precision=False):
         """P^T P x (run_mgfbp_iterative_recon_IRN_CGLS.py:288-316).  full_precision
@@ -115,14 +118,8 @@ class IrSystem:
         """q = P^T P d + sum_k s_k D^T W_k D d and dq = <d, q>: FP, pack, then the
         backprojector with the TV terms and the inner product in its epilogue."""
         self.ptp_calls += 1
-        sgm = self.fp(d, out=self.fp_buf)
-        packed = self.__dict__.setdefault("_packed", {})
-        if self.dtype not in packed:
-            packed[self.dtype] = torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16), dtype=torch.uint8,
-                                             device=self.device)
-        ops.pack_sinogram(self.dg, sgm, dtype=self.dtype, out=packed[self.dtype])
-        return ops.bp_unmatched_packed_cg(self.dg, packed[self.dtype], self.dtype, d, [(s, w) for s, w in op_terms],
-                                          q, dq)
+        packed = self._pack(self.fp(d, out=self.fp_buf), self.dtype)
+        return ops.bp_unmatched_packed_cg(self.dg, packed, self.dtype, d, list(op_terms), q, dq)
 
     def dtwd_acc(self, x, wr, s, acc):
         """acc += s * D^T W D x (in place)."""
