@@ -133,6 +133,18 @@ int mct_filter_tc(const mct_geom* g, const float* weighted, int32_t dtype, void*
                   void* stream);
 int mct_filter_tc_status(const mct_geom* g, int32_t dtype, void* workspace, void* stream);
 
+/* Weighting and the tensor-core row filter in one call: the sinogram (strides and
+ * beam-hardening coefficients as mct_weight) is weighted element by element while it
+ * is split into mct_filter_tc's bf16 operand parts, so the weighted float32 sinogram is
+ * never written, then filtered into filtered [views][nv][nu] (workspace and dtype as
+ * mct_filter_tc, prepared by mct_filter_tc_prepare).  Results equal mct_weight followed
+ * by mct_filter_tc.  No vertical Gaussian: with one, call mct_weight, mct_vgauss and
+ * mct_filter_tc.  Replaces BHCorrection + WeightSgm + ConvolveSgmAndKernel
+ * (FilterSinogram) run_mgfbp.py:946-1046, 1282-1292. */
+int mct_weight_filter(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t row_stride,
+                      int64_t view_stride, const float* bh_coeffs, int32_t n_bh, int32_t dtype, void* workspace,
+                      float* filtered, void* stream);
+
 /* Bytes of the packed backprojection operand for storage type dtype. */
 size_t mct_packed_size(const mct_geom* g, int32_t dtype);
 

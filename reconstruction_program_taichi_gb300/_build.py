@@ -44,8 +44,9 @@ def build(verbose=False, extra=(), force=False):
     nvcc = nvcc_path()
     os.makedirs(OBJ, exist_ok=True)
     srcs = sources()
-    newest = max([os.path.getmtime(s) for s in srcs] + [os.path.getmtime(os.path.join(CSRC, "common.cuh")),
-                                                        os.path.getmtime(os.path.join(ROOT, "include", "mandoct_gb300.h"))])
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    newest = max([os.path.getmtime(s) for s in srcs + headers] +
+                 [os.path.getmtime(os.path.join(ROOT, "include", "mandoct_gb300.h"))])
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest and not extra:
         return LIB_PATH
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:

@@ -118,6 +118,7 @@ SIGNATURES = {
     "mct_cgls_update_t": (ctypes.c_int, [_i64, _i32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mct_cgls_direction_t": (ctypes.c_int, [_i64, _i32, _P, _P, _P, _P, _P]),
     "mct_bp_cg_partials_size": (ctypes.c_size_t, [_G]),
+    "mct_weight_filter": (ctypes.c_int, [_G, _T, _P, _i64, _i64, _P, _i32, _i32, _P, _P, _P]),
     "mct_bp_ref_unmatched_packed_cg": (ctypes.c_int, [_G, _T, _P, _i32, _P, _P, _f32, _P, _f32, _P, _i32, _P, _P,
                                                       _P]),
 }

@@ -5,46 +5,10 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "weight.cuh"
 
 namespace mct {
 namespace {
-
-struct WeightParams {
-    int nu, nv, views, curved, short_scan, n_bh, view_begin;
-    int64_t row_stride, view_stride;
-    float u0, u_step, v0, v_step, sdd, scan;
-    float num_rounds, remain;  // short-scan constants
-};
-
-// Parker / over-scan weight of one (view, column), run_mgfbp.py:971-1011.
-__device__ float parker(const WeightParams& p, float beta, float u) {
-    const float PI = (float)kPI;
-    float rot_dir = fabsf(p.scan) / p.scan;
-    float gamma = p.curved ? ((-1.0f) * u / p.sdd) * rot_dir : atan2f(-u, p.sdd) * rot_dir;
-    float gmax = p.remain - PI;
-    float nr = p.num_rounds, ra = p.remain;
-    float w = 0.0f;
-    if (ra <= PI && nr == 0.0f) {
-        w = 1.0f;
-    } else if (ra <= PI && nr >= 1.0f) {
-        if (0.0f <= beta && beta < ra) w = beta / ra;
-        else if (ra <= beta && beta < 2 * PI * nr) w = 1.0f;
-        else if (2 * PI * nr <= beta && beta <= (2 * PI * nr + ra)) w = (2 * PI * nr + ra - beta) / ra;
-    } else if (PI < ra && ra <= 2 * PI) {
-        if (0.0f <= beta && beta < (gmax - 2 * gamma)) {
-            w = sinf(PI / 2 * beta / (gmax - 2 * gamma));
-            w = w * w;
-        } else if ((gmax - 2 * gamma) <= beta && beta < (PI * (2 * nr + 1) - 2 * gamma)) {
-            w = 1.0f;
-        } else if ((PI * (2 * nr + 1) - 2 * gamma) <= beta && beta <= (PI * (2 * nr + 1) + gmax)) {
-            w = sinf(PI / 2 * (PI + gmax - (beta - PI * 2 * nr)) / (gmax + 2 * gamma));
-            w = w * w;
-        }
-    } else {
-        w = 1.0f;
-    }
-    return w;
-}
 
 // One block per (row, view) line of nu elements (grid-stride over lines), so the
 // line's row, view and source offset are computed once per line, not per element.
@@ -59,21 +23,8 @@ __global__ void weight_kernel(WeightParams p, const float* __restrict__ in, cons
         const float v = p.v0 + r * p.v_step;
         const float beta = p.short_scan ? fabsf(angles[p.view_begin + j] - angles[0]) : 0.0f;
         for (int c = threadIdx.x; c < p.nu; c += blockDim.x) {
-            float val = src[c];
-            if (p.n_bh > 0) {
-                float acc = 0.0f, pw = val;
-                for (int t = 0; t < p.n_bh; ++t) {
-                    acc += bh[t] * pw;
-                    pw *= val;
-                }
-                val = acc;
-            }
             const float u = p.u0 + c * p.u_step;
-            const float sdd = p.sdd;
-            if (p.curved) val = val * sdd * cosf((-1.0f) * u / sdd) * sdd / sqrtf(sdd * sdd + v * v);
-            else val = (val * sdd * sdd) / sqrtf(sdd * sdd + u * u + v * v);
-            if (p.short_scan) val *= parker(p, beta, u);
-            dst[c] = val;
+            dst[c] = weight_value(p, src[c], bh, u, weight_cos(p, u), weight_den(p, u, v), beta);
         }
     }
 }
@@ -92,7 +43,6 @@ weight4_kernel(WeightParams p, const float* __restrict__ in, const float* __rest
     const int j0 = blockIdx.x * WV;
     const int nj = min(WV, p.views - j0);
     const float v = p.v0 + r * p.v_step;
-    const float sdd = p.sdd;
     const int nu4 = p.nu >> 2;
     for (int c4 = threadIdx.x; c4 < nu4; c4 += blockDim.x) {
         float uu[4], cs[4], den[4];
@@ -100,8 +50,8 @@ weight4_kernel(WeightParams p, const float* __restrict__ in, const float* __rest
         for (int e = 0; e < 4; ++e) {
             const float u = p.u0 + (4 * c4 + e) * p.u_step;
             uu[e] = u;
-            cs[e] = p.curved ? cosf((-1.0f) * u / sdd) : 0.0f;
-            den[e] = p.curved ? sqrtf(sdd * sdd + v * v) : sqrtf(sdd * sdd + u * u + v * v);
+            cs[e] = weight_cos(p, u);
+            den[e] = weight_den(p, u, v);
         }
 #pragma unroll
         for (int jj = 0; jj < WV; ++jj) {
@@ -111,21 +61,7 @@ weight4_kernel(WeightParams p, const float* __restrict__ in, const float* __rest
                 const float beta = p.short_scan ? fabsf(angles[p.view_begin + j] - angles[0]) : 0.0f;
                 float o[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    float val = o[e];
-                    if (p.n_bh > 0) {
-                        float acc = 0.0f, pw = val;
-                        for (int t = 0; t < p.n_bh; ++t) {
-                            acc += bh[t] * pw;
-                            pw *= val;
-                        }
-                        val = acc;
-                    }
-                    if (p.curved) val = val * sdd * cs[e] * sdd / den[e];
-                    else val = (val * sdd * sdd) / den[e];
-                    if (p.short_scan) val *= parker(p, beta, uu[e]);
-                    o[e] = val;
-                }
+                for (int e = 0; e < 4; ++e) o[e] = weight_value(p, o[e], bh, uu[e], cs[e], den[e], beta);
                 *reinterpret_cast<float4*>(out + ((int64_t)r * p.views + j) * p.nu + 4 * c4) =
                     make_float4(o[0], o[1], o[2], o[3]);
             }
@@ -360,18 +296,7 @@ int mct_weight(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t
     MCT_REQUIRE(n_bh >= 0 && (n_bh == 0 || bh_coeffs), "mct_weight: bad BH coefficients");
     bool short_scan = (g->flags & MCT_SHORT_SCAN) != 0;
     MCT_REQUIRE(!short_scan || (t && t->angles), "mct_weight: short scan needs the angle table");
-    WeightParams p{};
-    p.nu = g->nu; p.nv = g->nv; p.views = g->views;
-    p.view_begin = g->view_begin;  // angles is the whole scan's table (view-chunked FBP)
-    p.curved = (g->flags & MCT_CURVED) != 0;
-    p.short_scan = short_scan;
-    p.n_bh = n_bh;
-    p.row_stride = row_stride; p.view_stride = view_stride;
-    p.u0 = g->u0; p.u_step = g->u_step; p.v0 = g->v0; p.v_step = g->v_step;
-    p.sdd = g->sdd; p.scan = g->total_scan_angle;
-    float PI = (float)kPI;
-    p.num_rounds = floorf(fabsf(p.scan) / (PI * 2));
-    p.remain = fabsf(p.scan) - p.num_rounds * PI * 2;
+    const WeightParams p = weight_params(g, row_stride, view_stride, n_bh);
     const bool vec4 = g->nu % 4 == 0 && row_stride % 4 == 0 && view_stride % 4 == 0 && g->nv <= 65535 &&
                       ((uintptr_t)sgm & 15) == 0 && ((uintptr_t)weighted & 15) == 0;
     if (vec4) {

@@ -28,6 +28,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "weight.cuh"
 
 namespace mct {
 namespace {
@@ -134,6 +135,44 @@ __global__ void split_a_kernel(const float* __restrict__ x, int64_t rows, int nu
         for (int c = 0; c < 8; ++c) {
             const int m = m0 + c;
             split_parts<NS>((R < rows && m < nu) ? x[R * nu + m] : 0.0f, v[c]);
+        }
+        store_parts<NS>(a.p, i, v);
+    }
+}
+
+// split_a_kernel reading the raw sinogram and weighting each element on the way
+// (weight_value, as the weighting kernels do), so the weighted float32 sinogram is never
+// written: operand row R = r * views + j is detector row r of view j, as in the
+// weighting kernels' output.
+template <int NS>
+__global__ void weight_split_a_kernel(WeightParams wp, const float* __restrict__ in, const float* __restrict__ bh,
+                                      const float* __restrict__ angles, int64_t rows, int nu, int KB, int64_t n_chunks,
+                                      Parts a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_chunks; i += (int64_t)gridDim.x * blockDim.x) {
+        int r8, kj, mi, kb;
+        int64_t mb;
+        tile_coords<NS, TC_BM>(i, KB, r8, kj, mi, kb, mb);
+        const int64_t R = mb * TC_BM + mi * 8 + r8;
+        const int m0 = kb * TcTiles<NS>::BK + kj * 8;
+        uint32_t v[8][NS];
+        if (R < rows) {
+            const int r = (int)(R / wp.views), j = (int)(R % wp.views);
+            const float* src = in + r * wp.row_stride + j * wp.view_stride;
+            const float vv = wp.v0 + r * wp.v_step;
+            const float beta = wp.short_scan ? fabsf(angles[wp.view_begin + j] - angles[0]) : 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int m = m0 + c;
+                float x = 0.0f;
+                if (m < nu) {
+                    const float u = wp.u0 + m * wp.u_step;
+                    x = weight_value(wp, __ldg(src + m), bh, u, weight_cos(wp, u), weight_den(wp, u, vv), beta);
+                }
+                split_parts<NS>(x, v[c]);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) split_parts<NS>(0.0f, v[c]);
         }
         store_parts<NS>(a.p, i, v);
     }
@@ -399,8 +438,11 @@ int tc_prepare(const mct_geom* g, const float* taps, void* ws, cudaStream_t s) {
     return launched("build_b_kernel");
 }
 
+// weighted: the weighted sinogram [nv][views][nu]; or, with wp, the raw sinogram
+// (strides in wp), weighted while it is split.
 template <int NS>
-int tc_run(const mct_geom* g, const float* weighted, void* ws, float* filtered, cudaStream_t s) {
+int tc_run(const mct_geom* g, const float* weighted, void* ws, float* filtered, cudaStream_t s,
+           const WeightParams* wp = nullptr, const float* bh = nullptr, const float* angles = nullptr) {
     Parts a{}, b{};
     int* flag;
     tc_workspace<NS>(g, &a, &b, &flag, ws);
@@ -408,8 +450,13 @@ int tc_run(const mct_geom* g, const float* weighted, void* ws, float* filtered, 
     MCT_REQUIRE(d.mb < 65535 * 32, "mct_filter_tc: too many rows");
     const int64_t chunks = (int64_t)d.mb * d.kb * (TcTiles<NS>::A_TILE / 16);
     const int grid = (int)std::min<int64_t>((chunks + 255) / 256, 152 * 32);
-    split_a_kernel<NS><<<grid, 256, 0, s>>>(weighted, d.rows, g->nu, d.kb, chunks, a);
-    MCT_TRY(launched("split_a_kernel"));
+    if (wp) {
+        weight_split_a_kernel<NS><<<grid, 256, 0, s>>>(*wp, weighted, bh, angles, d.rows, g->nu, d.kb, chunks, a);
+        MCT_TRY(launched("weight_split_a_kernel"));
+    } else {
+        split_a_kernel<NS><<<grid, 256, 0, s>>>(weighted, d.rows, g->nu, d.kb, chunks, a);
+        MCT_TRY(launched("split_a_kernel"));
+    }
     // opt in to the large dynamic shared memory (per device, idempotent)
     cudaError_t e = cudaFuncSetAttribute(tc_filter_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          TcTiles<NS>::SMEM);
@@ -453,6 +500,24 @@ int mct_filter_tc(const mct_geom* g, const float* weighted, int32_t dtype, void*
     MCT_REQUIRE(((uintptr_t)workspace & 1023) == 0, "mct_filter_tc: workspace must be 1 KiB aligned");
     return dtype == MCT_F32 ? tc_run<3>(g, weighted, workspace, filtered, as_stream(stream))
                             : tc_run<2>(g, weighted, workspace, filtered, as_stream(stream));
+}
+
+int mct_weight_filter(const mct_geom* g, const mct_tables* t, const float* sgm, int64_t row_stride,
+                      int64_t view_stride, const float* bh_coeffs, int32_t n_bh, int32_t dtype, void* workspace,
+                      float* filtered, void* stream) {
+    MCT_TRY(check_geom(g, "mct_weight_filter"));
+    MCT_REQUIRE(sgm && workspace && filtered, "mct_weight_filter: NULL buffer");
+    MCT_REQUIRE(n_bh >= 0 && (n_bh == 0 || bh_coeffs), "mct_weight_filter: bad BH coefficients");
+    MCT_REQUIRE(dtype == MCT_F32 || dtype == MCT_BF16, "mct_weight_filter: dtype must be MCT_F32 or MCT_BF16");
+    MCT_REQUIRE(((uintptr_t)workspace & 1023) == 0, "mct_weight_filter: workspace must be 1 KiB aligned");
+    const bool short_scan = (g->flags & MCT_SHORT_SCAN) != 0;
+    MCT_REQUIRE(!short_scan || (t && t->angles), "mct_weight_filter: short scan needs the angle table");
+    MCT_REQUIRE(row_stride >= 0 && view_stride >= 0, "mct_weight_filter: negative stride");
+    const WeightParams wp = weight_params(g, row_stride, view_stride, n_bh);
+    const float* angles = t ? t->angles : nullptr;
+    cudaStream_t s = as_stream(stream);
+    return dtype == MCT_F32 ? tc_run<3>(g, sgm, workspace, filtered, s, &wp, bh_coeffs, angles)
+                            : tc_run<2>(g, sgm, workspace, filtered, s, &wp, bh_coeffs, angles);
 }
 
 // 0 if no tensor-core filter launch on this workspace has timed out, else MCT_E_TIMEOUT

@@ -65,17 +65,35 @@ class FdkPipeline:
                                                       obj.det_elem_vertical_gauss_filter_size), **f32)
         self.bh = torch.tensor(obj.array_bh_coefficients, **f32) if obj.bool_bh_correction else None
         g = self.dg.geom
-        self.weighted = torch.empty(self.dg.sgm_shape, **f32)
+        self._weighted = None  # the weighted sinogram, allocated by the paths that write it
         self.smoothed = torch.empty(self.dg.sgm_shape, **f32) if self.gauss_v is not None else None
         self.filtered = torch.empty((g.views, g.nv, g.nu), **f32)
         self.packed = torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16), dtype=torch.uint8, device=dev)
         self.vol = torch.empty(self.dg.vol_shape, **f32)
 
+    @property
+    def weighted(self):
+        """Buffer of the weighted sinogram [rows, views, cols] (allocated on first use:
+        the tensor-core path without a vertical Gaussian weights while it filters)."""
+        if self._weighted is None:
+            self._weighted = torch.empty(self.dg.sgm_shape, dtype=torch.float32, device=self.device)
+        return self._weighted
+
+    def nbytes(self):
+        """Device bytes held by this pipeline's buffers."""
+        ts = [self._weighted, self.smoothed, self.filtered, self.packed, self.vol]
+        return sum(t.numel() * t.element_size() for t in ts if t is not None) + (
+            self.tc._buf.numel() if self.tc is not None else 0)
+
     def filter(self, sgm, row_stride=None, view_stride=None):
-        """Weighted and filtered view-major sinogram [views, rows, cols]."""
+        """Weighted and filtered view-major sinogram [views, rows, cols].  With the
+        tensor-core filter and no vertical Gaussian, the weighting runs while the
+        operand is split (one pass over the sinogram, no weighted copy)."""
         g = self.dg.geom
         if row_stride is None:
             row_stride, view_stride = g.views * g.nu, g.nu
+        if self.tc is not None and self.gauss_v is None and not self.kernel_none:
+            return self.tc.weight_filter(sgm, row_stride, view_stride, self.bh, out=self.filtered)
         w = ops.weight(self.dg, sgm, row_stride, view_stride, self.bh, out=self.weighted)
         if self.gauss_v is not None:
             w = ops.vgauss(self.dg, w, self.gauss_v, out=self.smoothed)

@@ -176,6 +176,23 @@ class TcFilter:
         _lib.call("mct_filter_tc", self.dg.g(), _ptr(weighted), self.dtype, self.ws, _ptr(out), _stream())
         return out
 
+    def weight_filter(self, sgm, row_stride, view_stride, bh=None, out=None):
+        """Weighting (BH, cosine, Parker) and this filter in one pass over the sinogram:
+        the weighting runs while the operand is split, the weighted float32 sinogram is
+        never written (mct_weight_filter).  Same result as weight() then __call__."""
+        g = self.dg.geom
+        _check(sgm, "sgm")
+        if out is None:
+            out = torch.empty((g.views, g.nv, g.nu), dtype=torch.float32, device=sgm.device)
+        _check(out, "out", (g.views, g.nv, g.nu))
+        n_bh = 0
+        if bh is not None:
+            _check(bh, "bh")
+            n_bh = bh.numel()
+        _lib.call("mct_weight_filter", self.dg.g(), self.dg.t(), _ptr(sgm), int(row_stride), int(view_stride),
+                  _ptr(bh), n_bh, self.dtype, self.ws, _ptr(out), _stream())
+        return out
+
     def status(self):
         """Raise if a bounded pipeline wait of an earlier launch timed out (syncs)."""
         _lib.call("mct_filter_tc_status", self.dg.g(), self.dtype, self.ws, _stream())

@@ -190,9 +190,7 @@ class _FbpSlot:
                          for _ in range(batch)]
         self.graphs = []
         self.last_used = time.perf_counter()
-        self.nbytes = sum(p.weighted.numel() * 4 + p.filtered.numel() * 4 + p.packed.numel() + p.vol.numel() * 4
-                          + (p.tc._buf.numel() if p.tc is not None else 0)
-                          for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
+        self.nbytes = sum(p.nbytes() for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
             self.graphs = _capture_members(self.stream, [lambda i=i: self._member(i) for i in range(batch)])
 
@@ -430,7 +428,7 @@ class ReconServer:
         o = req.obj
         nvol = o.img_dim * o.img_dim * o.img_dim_z * 4
         nsgm = o.det_elem_count_horizontal * o.det_elem_count_vertical_actual * o.view_num * 4
-        if req.kind == "fbp":  # input, weighted, filtered, packed (4x), tensor-core operand tiles
+        if req.kind == "fbp":  # input, filtered, packed (4x), tensor-core operand tiles (1.5x), bound
             return nsgm * 8 + 2 * nvol
         # CGLS member: sinogram, seed, result
         return nsgm + 2 * nvol

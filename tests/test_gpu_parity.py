@@ -811,3 +811,34 @@ def test_fused_cg_solve_matches_separate_passes(cuda):
         prior = torch.from_numpy(ir.img_prior.copy()).cuda()
         outs.append(ir.solve_piccs(sgm, prior).cpu().numpy())
     assert rel_l2(outs[0], outs[1]) < 1e-5
+
+
+@pytest.mark.parametrize("case", ["flat", "curved_short_bh", "strided"])
+@pytest.mark.parametrize("parts", [2, 3])
+def test_weight_filter_fused_matches_separate(cuda, case, parts):
+    """mct_weight_filter (the weighting applied while the tensor-core operand is split,
+    no weighted copy) against mct_weight followed by mct_filter_tc: the same element
+    operations, so the filtered sinograms are identical."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    from reconstruction_program_taichi_gb300._lib import MCT_BF16, MCT_F32
+    kw = {}
+    if case == "curved_short_bh":
+        kw = {"CurvedDetector": True, "TotalScanAngle": 220, "BeamHardeningCorrectionCoefficients": [0.0, 1.02, 0.03]}
+    o = _cone_obj(nu=72, nv=12, views=50, **kw)
+    dg = geometry.fbp_geometry(o)
+    g = dg.geom
+    taps = torch.tensor(geometry.recon_taps(o), dtype=torch.float32, device="cuda")
+    bh = torch.tensor(o.array_bh_coefficients, dtype=torch.float32, device="cuda") if o.bool_bh_correction else None
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    if case == "strided":  # view-major input [views][rows][cols], as post-log files arrive
+        raw = torch.rand((g.views, g.nv, g.nu), device="cuda", generator=gen)
+        rs, vs = g.nu, g.nv * g.nu
+    else:
+        raw = torch.rand(dg.sgm_shape, device="cuda", generator=gen)
+        rs, vs = g.views * g.nu, g.nu
+    tc = ops.TcFilter(dg, taps, MCT_F32 if parts == 3 else MCT_BF16)
+    ref = tc(ops.weight(dg, raw, rs, vs, bh))
+    got = tc.weight_filter(raw, rs, vs, bh)
+    tc.status()
+    assert torch.equal(got, ref)
