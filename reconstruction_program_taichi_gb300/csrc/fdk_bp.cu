@@ -23,6 +23,8 @@ namespace mct {
 namespace {
 
 constexpr int BP_TX = 32, BP_TY = 8, BP_ZC = 16, BP_VCHUNK = 1024;
+constexpr int BP_WX = 4;  // columns along x per warp (32 / BP_WX along y)
+static_assert(BP_TX % BP_WX == 0 && BP_TY % (32 / BP_WX) == 0, "warps tile the block");
 static_assert(BP_ZC % 2 == 0, "the 16-bit axial loop takes slices in pairs");
 // Minimum resident blocks per SM, i.e. a register budget of 65536 / (256 * minb) per
 // thread.  The axial kernel needs enough registers to issue all BP_ZC stencil gathers
@@ -72,10 +74,16 @@ __global__ void __launch_bounds__(BP_TX* BP_TY, bp_min_blocks<MODE, QT>())
 fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
               const void* __restrict__ packed, float* __restrict__ vol, const uint32_t* __restrict__ f16_max) {
     __shared__ float4 tab[BP_VCHUNK];  // {cos b, sin b, dbeta*div, unused}
-    const int ix = blockIdx.x * BP_TX + threadIdx.x;
-    const int iy = blockIdx.y * BP_TY + threadIdx.y;
-    const int zb = blockIdx.z * BP_ZC;
     const int tid = threadIdx.y * BP_TX + threadIdx.x;
+    // A warp is 4 columns along x x 8 along y of the block's 32 x 8: for one view its
+    // columns project onto fewer detector columns than a row of 32 (about 4|sin| + 8|cos|
+    // + 1 against 32|sin| + 1), so each gather touches fewer L1 lines.  At 512x512x256 /
+    // 1080 views: 52.19 -> 50.22 ms (float32), 49.07 -> 47.17 ms (bf16); warps of 16 x 2
+    // 51.62 / 48.50, 8 x 4 50.78 / 47.70; blocks of 16 x 16 or 8 x 32 no better.
+    const int warp = tid >> 5, lane = tid & 31;
+    const int ix = blockIdx.x * BP_TX + (warp % (BP_TX / BP_WX)) * BP_WX + (lane % BP_WX);
+    const int iy = blockIdx.y * BP_TY + (warp / (BP_TX / BP_WX)) * (32 / BP_WX) + lane / BP_WX;
+    const int zb = blockIdx.z * BP_ZC;
     const bool active = ix < p.nx && iy < p.nx;
     const int nq = p.nu - 1;  // packed columns; packed rows per view: nv (cone: row nv-1 is NaN)
 

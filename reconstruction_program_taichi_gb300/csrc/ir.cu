@@ -198,10 +198,15 @@ bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const fl
     const int nq = p.nu - 1;  // packed: nv rows of nu-1 coefficient sets per view
     __shared__ float4 tab[UB_VCHUNK];  // {cos b, sin b, cz_j, sid*cos b}
     __shared__ float tab_s[UB_VCHUNK];  // sid*sin b
-    const int ix = blockIdx.x * UB_TX + threadIdx.x;
-    const int iy = blockIdx.y * UB_TY + threadIdx.y;
-    const int zb = blockIdx.z * UA_ZC;
+    // a warp is 4 columns along x x 8 along y of the block's 32 x 8 (a view's gathers
+    // then span fewer detector columns; 512x512x64 / 360 views: float32 6.01 -> 5.79 ms,
+    // bf16 5.94 -> 5.91)
+    constexpr int WX = 4;
     const int tid = threadIdx.y * UB_TX + threadIdx.x;
+    const int wq = tid >> 5, lq = tid & 31;
+    const int ix = blockIdx.x * UB_TX + (wq % (UB_TX / WX)) * WX + (lq % WX);
+    const int iy = blockIdx.y * UB_TY + (wq / (UB_TX / WX)) * (32 / WX) + lq / WX;
+    const int zb = blockIdx.z * UA_ZC;
     const bool active = ix < p.nx && iy < p.nx;
     // same expressions as the general kernel with the axial mode's zero z-terms
     const float x = p.o_x + ix * p.ex_x + iy * p.ey_x + zb * p.ez_x;
