@@ -35,7 +35,11 @@ PROF180 = dict(PROF, views=180)
 # 270 views: scans of 256 views or more take the projector's 16-view ray tiles, as at
 # 1080 views (about 4 GB on the device)
 PROF270 = dict(PROF, views=270)
-WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF, "prof180": PROF180, "prof270": PROF270}
+# 180 views of a 256-slice volume: the float32 backprojector's geometry-sharing kernel
+# needs depths that are multiples of 128 slices, as at the benchmark (about 1.4 GB)
+PROF180Z = dict(PROF180, nz=256)
+WORKLOADS = {"c2": WORKLOAD, "small": SMALL, "prof": PROF, "prof180": PROF180, "prof270": PROF270,
+             "prof180z": PROF180Z}
 
 
 def make_config(w):
@@ -1214,8 +1218,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
-                    help="c2: the benchmark; small: quick checks; prof, prof180, prof270: short launches for ncu "
-                         "captures")
+                    help="c2: the benchmark; small: quick checks; prof, prof180, prof270, prof180z: short launches "
+                         "for ncu captures")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cgls", action="store_true")

@@ -327,8 +327,13 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
 // (256 threads over GV x 32 entries) and every warp reads its columns' entries: the
 // per-view work of a thread falls from ~35 instructions to two shared loads and the
 // slice offset of v.  Same arithmetic as fdk_bp_kernel's MODE 0 (identical results).
-// Measured at 512x512x256 / 1080 views with float32 operands: 50.6 -> 48.9 ms (GV 64;
-// 32: 49.8, 16: 51.5); with bf16 operands 47.9 -> 48.2, so those keep fdk_bp_kernel.
+// Measured at 512x512x256 / 1080 views with float32 operands: 50.2 -> 48.4 ms (GV 64;
+// 32: 49.8, 16: 51.5; 2 column groups x 4 chunks sharing, 50.1; 4 x 2, 54.1); with
+// bf16 operands 47.9 -> 48.2, so those keep fdk_bp_kernel, and so do volumes whose
+// depth is not a multiple of 128 slices (512x512x160 / 180 views: 6.70 against 5.04
+// ms, the last block of each column mostly idle).  The block's 8 slice chunks read 8
+// detector row bands, so the L1 hit rate falls (18 % against 86 % at 180 views); the
+// saved per-view instructions outweigh it on the benchmark volume only.
 constexpr int GZ = 8, GV = 64;
 template <typename QT>
 __global__ void __launch_bounds__(256, bp_min_blocks<0, QT>())
@@ -610,7 +615,7 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
     if (pm && g->view_mode == 1) launch_bp<3, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
     else if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
-    else if (axial_fast && cone && dtype == MCT_F32) {
+    else if (axial_fast && cone && dtype == MCT_F32 && g->nz % (GZ * BP_ZC) == 0) {
         dim3 gg((g->nx + 3) / 4, (g->nx + 7) / 8, (g->nz + GZ * BP_ZC - 1) / (GZ * BP_ZC));
         fdk_bp_geo_kernel<float4><<<gg, 256, 0, s>>>(p, t->angles, packed, vol, nullptr);
     }
