@@ -319,122 +319,6 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     }
 }
 
-// Axial cone beam with the per-(view, column) geometry shared by the block's warps:
-// a block is 32 columns (4 along x x 8 along y) x GZ = 8 chunks of BP_ZC slices, warp w
-// taking chunk w, so the geometry of a column (L, t, one reciprocal, u, the bilinear
-// column and weight, the magnification) depends on the view and column only.  Per run
-// of GV views the block computes each (view, column) entry once into shared memory
-// (256 threads over GV x 32 entries) and every warp reads its columns' entries: the
-// per-view work of a thread falls from ~35 instructions to two shared loads and the
-// slice offset of v.  Same arithmetic as fdk_bp_kernel's MODE 0 (identical results).
-// Measured at 512x512x256 / 1080 views with float32 operands: 50.2 -> 48.4 ms (GV 64;
-// 32: 49.8, 16: 51.5; 2 column groups x 4 chunks sharing, 50.1; 4 x 2, 54.1); with
-// bf16 operands 47.9 -> 48.2, so those keep fdk_bp_kernel, and so do volumes whose
-// depth is not a multiple of 128 slices (512x512x160 / 180 views: 6.70 against 5.04
-// ms, the last block of each column mostly idle).  The block's 8 slice chunks read 8
-// detector row bands, so the L1 hit rate falls (18 % against 86 % at 180 views); the
-// saved per-view instructions outweigh it on the benchmark volume only.
-constexpr int GZ = 8, GV = 64;
-template <typename QT>
-__global__ void __launch_bounds__(256, bp_min_blocks<0, QT>())
-fdk_bp_geo_kernel(BpParams p, const float* __restrict__ angles, const void* __restrict__ packed,
-                  float* __restrict__ vol, const uint32_t* __restrict__ f16_max) {
-    __shared__ float4 geo[GV][32];  // {ru, w, mag, vB} per (view, column)
-    __shared__ int guc[GV][32];      // bilinear detector column, or -1 when off the detector
-    __shared__ float4 tab[GV];
-    const int tid = threadIdx.x;
-    const int warp = tid >> 5, lane = tid & 31;
-    const int cx = lane & 3, cy = lane >> 2;  // this thread's column in the block's 4 x 8
-    const int ix = blockIdx.x * 4 + cx, iy = blockIdx.y * 8 + cy;
-    const int zb = (blockIdx.z * GZ + warp) * BP_ZC;
-    const bool active = ix < p.nx && iy < p.nx && zb < p.nz;
-    const int nq = p.nu - 1;
-    const float c0z = p.o_z + ix * p.px_z + iy * p.py_z + zb * p.pz_z;
-    float acc[BP_ZC];
-#pragma unroll
-    for (int k = 0; k < BP_ZC; ++k) acc[k] = 0.0f;
-    bool dead = !active;
-    const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
-    const unsigned nan_row = (unsigned)(p.nv - 1);
-    for (int jc = 0; jc < p.views; jc += GV) {
-        const int nvc = min(GV, p.views - jc);
-        __syncthreads();
-        if (tid < nvc) {
-            const int jg = p.view_begin + jc + tid;
-            const int vt = p.views_total;
-            float sn, cs;
-            sincosf(angles[jg] - p.img_rot, &sn, &cs);
-            const float db = (jg == vt - 1) ? fabsf(angles[vt - 1] - angles[0]) / (vt - 1) : fabsf(angles[jg + 1] - angles[jg]);
-            tab[tid] = make_float4(cs, sn, db * p.div * unscale, 0.0f);
-        }
-        __syncthreads();
-        // (view, column) geometry: 256 threads over nvc x 32 entries
-        for (int e = tid; e < nvc * 32; e += 256) {
-            const int q = e >> 5, col = e & 31;
-            const int gx = blockIdx.x * 4 + (col & 3), gy = blockIdx.y * 8 + (col >> 2);
-            const float x = p.o_x + gx * p.px_x + gy * p.py_x + (blockIdx.z * GZ * BP_ZC) * p.pz_x;
-            const float y = p.o_y + gx * p.px_y + gy * p.py_y + (blockIdx.z * GZ * BP_ZC) * p.pz_y;
-            const float4 tb = tab[q];
-            const float cb = tb.x, sb = tb.y;
-            const float L = p.sid - x * cb - y * sb;
-            const float t = -x * sb + y * cb;
-            const float rL = 1.0f / L;
-            const float mag = p.sdd * rL;
-            const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
-            const float ui = (u - p.u0) * p.inv_ustep;
-            int uc = -1;
-            float ru = 0.0f, w = 0.0f;
-            if (ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1)) {
-                const float uf = floorf(ui);
-                ru = ui - uf;
-                uc = (int)uf;
-                const float dw = p.curved ? 1.0f / (L * L + t * t) : rL * rL;
-                w = (p.sid * dw) * tb.z;
-            }
-            geo[q][col] = make_float4(ru, w, mag, (mag * p.pz_z) * p.kv);
-            guc[q][col] = uc;
-        }
-        __syncthreads();
-        if (dead) continue;
-        for (int q = 0; q < nvc; ++q) {
-            const int uc = guc[q][lane];
-            if (uc < 0) {
-                dead = true;
-                break;
-            }
-            const float4 gq = geo[q][lane];
-            const float ru = gq.x, w = gq.y, mag = gq.z, vB = gq.w;
-            const float vA = (mag * c0z - p.v0) * p.kv;
-            const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)(jc + q) * p.nv * nq + uc;
-            const float2 ru2 = make_float2(ru, ru);
-#pragma unroll
-            for (int k = 0; k < BP_ZC; ++k) {
-                const float vi = fmaf((float)k, vB, vA);
-                const float vf = floorf(vi);
-                const unsigned vr = min((unsigned)(int)vf, nan_row);
-                const float rv = vi - vf;
-                float2 lo, hi;
-                Quad<QT>::load(base + vr * (unsigned)nq, lo, hi);
-                const float2 s2 = __ffma2_rn(ru2, hi, lo);
-                acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
-            }
-        }
-    }
-    if (!active) return;
-    const int64_t plane = (int64_t)p.nx * p.nx;
-    float* out = vol + (int64_t)zb * plane + (int64_t)iy * p.nx + ix;
-#pragma unroll
-    for (int k = 0; k < BP_ZC; ++k) {
-        if (zb + k < p.nz) {
-            const bool off_detector = dead || acc[k] != acc[k];
-            if (p.accumulate)
-                out[(int64_t)k * plane] = off_detector ? __int_as_float(0x7fffffff) : out[(int64_t)k * plane] + acc[k];
-            else
-                out[(int64_t)k * plane] = off_detector ? 0.0f : acc[k];
-        }
-    }
-}
-
 __global__ void nan_to_zero_kernel(int64_t n, float* __restrict__ v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         if (v[i] != v[i]) v[i] = 0.0f;
@@ -615,10 +499,6 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
     const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
     if (pm && g->view_mode == 1) launch_bp<3, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
     else if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
-    else if (axial_fast && cone && dtype == MCT_F32 && g->nz % (GZ * BP_ZC) == 0) {
-        dim3 gg((g->nx + 3) / 4, (g->nx + 7) / 8, (g->nz + GZ * BP_ZC - 1) / (GZ * BP_ZC));
-        fdk_bp_geo_kernel<float4><<<gg, 256, 0, s>>>(p, t->angles, packed, vol, nullptr);
-    }
     else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else if (axial_fast) {
         MCT_REQUIRE(g->nx <= 65535, "mct_fdk_bp: fan beam images are at most 65535 pixels wide");
