@@ -88,6 +88,22 @@ def test_entry_points_reject_bad_arguments_before_any_launch():
         # unknown view mode
         ("mct_weight", (ctypes.byref(_valid_geom(view_mode=4)), ctypes.byref(t), FAKE, 0, 0, None, 0, FAKE, None),
          "view_mode"),
+        # the fused weighting + tensor-core filter: two storage types, a 1 KiB-aligned workspace
+        ("mct_weight_filter", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, 0, 0, None, 0, 2, FAKE, FAKE,
+                               None), "dtype"),
+        ("mct_weight_filter", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, 0, 0, None, 0, 0,
+                               ctypes.c_void_p(4096 + 512), FAKE, None), "1 KiB"),
+        # the CG step in the backprojector's epilogue: axial cone beam, float32 / bf16 vectors,
+        # the second TV term only with a first
+        ("mct_bp_ref_unmatched_packed_cg", (ctypes.byref(_valid_geom(view_mode=2)), ctypes.byref(t), FAKE, 0, FAKE,
+                                            FAKE, 1.0, None, 0.0, FAKE, 0, FAKE, FAKE, None), "axial"),
+        ("mct_bp_ref_unmatched_packed_cg", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, 0, FAKE, FAKE, 1.0,
+                                            None, 0.0, FAKE, 2, FAKE, FAKE, None), "vec_dtype"),
+        ("mct_bp_ref_unmatched_packed_cg", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, 0, FAKE, None, 0.0,
+                                            FAKE, 1.0, ctypes.c_void_p(8192), 0, FAKE, FAKE, None), "wr2"),
+        # a float16 volume is not an iterate type
+        ("mct_fp_storage_in", (ctypes.byref(_valid_geom()), ctypes.byref(t), FAKE, 2, None, FAKE, FAKE, 0, None),
+         "vol_dtype"),
     ]
     for name, args, text in cases:
         rc, msg = _status(name, *args)
@@ -122,3 +138,5 @@ def test_packed_and_workspace_sizes():
     assert lib.mct_fp_workspace_size(ctypes.byref(fan)) == 32 * 32 * 16 * 4
     assert lib.mct_fp_adjoint_workspace_size(ctypes.byref(g)) == 32 * 32 * 8 * 32
     assert lib.mct_fp_adjoint_workspace_size(ctypes.byref(fan)) == 32 * 32 * 16 * 16
+    # one float64 partial per block of the CG epilogue (32 x 8 columns x 16 slices)
+    assert lib.mct_bp_cg_partials_size(ctypes.byref(g)) == 1 * 4 * 1 * 8
