@@ -842,3 +842,29 @@ def test_weight_filter_fused_matches_separate(cuda, case, parts):
     got = tc.weight_filter(raw, rs, vs, bh)
     tc.status()
     assert torch.equal(got, ref)
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_fp_long_scan_tiles_vs_oracle(cuda, storage):
+    """Scans of 256 views or more take the projector's 16-column x 16-view tiles with 4
+    detector rows in turn per view group; here with a ragged detector (70 columns, 10
+    rows: neither a multiple of the tile) and 270 views (not a multiple of 16), against
+    the oracle on every view.  bf16 cells: within their storage rounding."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    o = _cone_obj(n=24, nz=12, nu=70, nv=10, views=270)
+    dg = geometry.fpj_geometry(o)
+    rng = np.random.default_rng(17)
+    vol = _smooth(rng, o.img_dim_z, o.img_dim)
+    dtype = {"f32": ops.MCT_F32, "bf16": ops.MCT_BF16}[storage]
+    got = ops.fp(dg, torch.from_numpy(vol).cuda(), dtype=dtype).cpu().numpy()
+    u, v, ang = dg.host["u"], dg.host["v"], dg.host["angles"]
+    ref = np.zeros_like(got, dtype=np.float64)
+    for j in range(o.view_num):
+        ref[:, j, :] = P.march(vol, j, ang, u, v, nx=o.img_dim, nz=o.img_dim_z, px=o.img_pix_size,
+                               pz=o.img_voxel_height, cx=o.img_center_x, cy=o.img_center_y,
+                               cz_view=o.array_img_center_z[j], sid=o.source_isocenter_dis, sdd=o.source_det_dis,
+                               step=o.fpj_step_size, cone_beam=True, curved=o.curved_dect,
+                               zpv=dg.geom.fp_z_per_view, rows=o.det_elem_count_vertical, K=dg.geom.fp_steps)
+    assert np.count_nonzero(ref) > 0.2 * ref.size
+    assert rel_l2(got, ref) < (TOL if storage == "f32" else 5e-3)
