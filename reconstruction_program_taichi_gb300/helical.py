@@ -141,17 +141,23 @@ class Mgfbp_helical(Mgfbp):  # noqa: N801 - reference name
         # 2. weighting + row filter over the stack (slices as rows)
         stack_obj = self.fan_object(nz)
         pipe = FdkPipeline(stack_obj, device=dev, storage="f32")
-        w = ops.weight(pipe.dg, stack, vc * nu, nu, pipe.bh, out=pipe.weighted)
-        if self.apply_gauss_vertical:
-            # the 1-row vertical convolution of the reference uses the first tap of the
-            # full-detector Gaussian it built in __init__ (run_mgfbp.py:298-309, 1020-1029)
-            g = gaussian_taps(self.det_elem_count_vertical_actual, self.det_elem_height,
-                              self.det_elem_vertical_gauss_filter_size)
-            w = w * float(np.float32(g[0])) * float(np.float32(self.det_elem_height))
-        if pipe.kernel_none:
-            filt = w.permute(1, 0, 2)
+        if not self.apply_gauss_vertical and pipe.tc is not None:
+            # weighting inside the tensor-core filter's operand split: [views][slices][cols]
+            filt = pipe.filter(stack, vc * nu, nu)
         else:
-            filt = ops.filter_rows(pipe.dg, w, pipe.taps, out=pipe.filtered)  # [views][slices][cols]
+            w = ops.weight(pipe.dg, stack, vc * nu, nu, pipe.bh, out=pipe.weighted)
+            if self.apply_gauss_vertical:
+                # the 1-row vertical convolution of the reference uses the first tap of the
+                # full-detector Gaussian it built in __init__ (run_mgfbp.py:298-309, 1020-1029)
+                g = gaussian_taps(self.det_elem_count_vertical_actual, self.det_elem_height,
+                                  self.det_elem_vertical_gauss_filter_size)
+                w = w * float(np.float32(g[0])) * float(np.float32(self.det_elem_height))
+            if pipe.kernel_none:
+                filt = w.permute(1, 0, 2)
+            elif pipe.tc is not None:
+                filt = pipe.tc(w, out=pipe.filtered)  # [views][slices][cols]
+            else:
+                filt = ops.filter_rows(pipe.dg, w, pipe.taps, out=pipe.filtered)
         if self.save_filtered_sinogram:  # the reference leaves the last slice's, as [views][1][cols]
             imwriteTiff(filt[:, nz - 1:nz, :].cpu().numpy(), self.output_dir + "/sgm_filtered_" + self.output_file)
         # 3. slice-major pack (one 1-row fan sinogram of vc views per slice) and
