@@ -55,35 +55,82 @@ class FdkPipeline:
         if filter_impl not in ("simt", "tc", "tc3"):
             raise ValueError("filter_impl must be 'tc3', 'tc' (tensor-core split bf16) or 'simt' (float32 FMA)")
         self.filter_impl = filter_impl
-        self.tc = None
         self._tc_dtype = MCT_F32 if filter_impl == "tc3" else MCT_BF16
-        if filter_impl in ("tc", "tc3") and not self.kernel_none:
-            self.tc = ops.TcFilter(self.dg, self.taps, self._tc_dtype)
+        # whether the row filter runs on the tensor cores; the filter object (its operand
+        # tiles are sized by the whole sinogram) and the full-size buffers below are
+        # allocated on first use, so that drivers that stream view chunks through this
+        # pipeline's geometry and taps (Mgfbp_v2) hold only their chunk buffers
+        self.uses_tc = filter_impl in ("tc", "tc3") and not self.kernel_none
+        self._tc = None
         self.gauss_v = None
         if obj.apply_gauss_vertical:
             self.gauss_v = torch.tensor(gaussian_taps(obj.det_elem_count_vertical_actual, obj.det_elem_height,
                                                       obj.det_elem_vertical_gauss_filter_size), **f32)
         self.bh = torch.tensor(obj.array_bh_coefficients, **f32) if obj.bool_bh_correction else None
-        g = self.dg.geom
         self._weighted = None  # the weighted sinogram, allocated by the paths that write it
-        self.smoothed = torch.empty(self.dg.sgm_shape, **f32) if self.gauss_v is not None else None
-        self.filtered = torch.empty((g.views, g.nv, g.nu), **f32)
-        self.packed = torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16), dtype=torch.uint8, device=dev)
-        self.vol = torch.empty(self.dg.vol_shape, **f32)
+        self._smoothed = self._filtered = self._packed = self._vol = None
+
+    def _buffer(self, name, make):
+        t = getattr(self, name)
+        if t is None:
+            t = make()
+            setattr(self, name, t)
+        return t
+
+    @property
+    def tc(self):
+        """The tensor-core row filter of this geometry and taps (None with the SIMT filter)."""
+        if self._tc is None and self.uses_tc:
+            self._tc = ops.TcFilter(self.dg, self.taps, self._tc_dtype)
+        return self._tc
 
     @property
     def weighted(self):
-        """Buffer of the weighted sinogram [rows, views, cols] (allocated on first use:
-        the tensor-core path without a vertical Gaussian weights while it filters)."""
-        if self._weighted is None:
-            self._weighted = torch.empty(self.dg.sgm_shape, dtype=torch.float32, device=self.device)
-        return self._weighted
+        """Buffer of the weighted sinogram [rows, views, cols] (the tensor-core path
+        without a vertical Gaussian weights while it filters and never needs it)."""
+        return self._buffer("_weighted", lambda: torch.empty(self.dg.sgm_shape, dtype=torch.float32,
+                                                             device=self.device))
+
+    @property
+    def smoothed(self):
+        if self.gauss_v is None:
+            return None
+        return self._buffer("_smoothed", lambda: torch.empty(self.dg.sgm_shape, dtype=torch.float32,
+                                                             device=self.device))
+
+    @property
+    def filtered(self):
+        g = self.dg.geom
+        return self._buffer("_filtered", lambda: torch.empty((g.views, g.nv, g.nu), dtype=torch.float32,
+                                                             device=self.device))
+
+    @property
+    def packed(self):
+        return self._buffer("_packed", lambda: torch.empty(max(ops.packed_bytes(self.dg, self.dtype), 16),
+                                                           dtype=torch.uint8, device=self.device))
+
+    @property
+    def vol(self):
+        return self._buffer("_vol", lambda: torch.empty(self.dg.vol_shape, dtype=torch.float32, device=self.device))
+
+    def allocate(self):
+        """Allocate now every buffer run() uses (callers that account device memory
+        before the first run: the serving slots)."""
+        fused = self.uses_tc and self.gauss_v is None
+        if not fused:
+            self.weighted
+        self.smoothed
+        self.filtered
+        self.packed
+        self.vol
+        self.tc
+        return self
 
     def nbytes(self):
-        """Device bytes held by this pipeline's buffers."""
-        ts = [self._weighted, self.smoothed, self.filtered, self.packed, self.vol]
+        """Device bytes held by this pipeline's buffers (those allocated so far)."""
+        ts = [self._weighted, self._smoothed, self._filtered, self._packed, self._vol]
         return sum(t.numel() * t.element_size() for t in ts if t is not None) + (
-            self.tc._buf.numel() if self.tc is not None else 0)
+            self._tc._buf.numel() if self._tc is not None else 0)
 
     def filter(self, sgm, row_stride=None, view_stride=None):
         """Weighted and filtered view-major sinogram [views, rows, cols].  With the
@@ -107,8 +154,7 @@ class FdkPipeline:
     def set_taps(self, taps):
         """Replace the filter taps (float64/float32 array of 2*nu-1 values)."""
         self.taps.copy_(torch.as_tensor(taps, dtype=torch.float32))
-        if self.tc is not None:
-            self.tc = ops.TcFilter(self.dg, self.taps, self._tc_dtype)
+        self._tc = None  # rebuilt from the new taps on first use
 
     def backproject(self, filtered, out=None):
         packed = ops.pack(self.dg, filtered, self.dtype, out=self.packed)
@@ -268,6 +314,15 @@ class Mgfbp_v2(Mgfbp):  # noqa: N801 - reference name
                 (dev_in[b][:, :n, :] if sino_layout else dev_in[b][:n]).copy_(dst, non_blocking=True)
                 copied[b].record(copy_stream)
 
+        tcs = {}  # tensor-core filters per chunk length (the operand tiles follow the rows)
+
+        def tc_for(cg, n):
+            if not pipe.uses_tc:
+                return None
+            if n not in tcs:
+                tcs[n] = ops.TcFilter(cg, pipe.taps, pipe._tc_dtype)
+            return tcs[n]
+
         for e in consumed:
             e.record(compute)
         stage(0)
@@ -278,13 +333,20 @@ class Mgfbp_v2(Mgfbp):  # noqa: N801 - reference name
             compute.wait_event(copied[b])
             cg = ops.ViewChunk(dg, j0, n, accumulate=True)
             rs, vs = (V * g.nu, g.nu) if sino_layout else (g.nu, g.nv * g.nu)
-            w = ops.weight(cg, dev_in[b], rs, vs, pipe.bh, out=weighted if n == V else None)
-            if smoothed is not None:
-                w = ops.vgauss(cg, w, pipe.gauss_v, out=smoothed if n == V else None)
-            if pipe.kernel_none:
-                f = w.permute(1, 0, 2).contiguous()
+            tc = tc_for(cg, n)
+            if tc is not None and smoothed is None:
+                # weighting inside the tensor-core filter's operand split
+                f = tc.weight_filter(dev_in[b], rs, vs, pipe.bh, out=filtered[:n], dg=cg)
             else:
-                f = ops.filter_rows(cg, w, pipe.taps, out=filtered[:n])
+                w = ops.weight(cg, dev_in[b], rs, vs, pipe.bh, out=weighted if n == V else None)
+                if smoothed is not None:
+                    w = ops.vgauss(cg, w, pipe.gauss_v, out=smoothed if n == V else None)
+                if pipe.kernel_none:
+                    f = w.permute(1, 0, 2).contiguous()
+                elif tc is not None:
+                    f = tc(w, out=filtered[:n])
+                else:
+                    f = ops.filter_rows(cg, w, pipe.taps, out=filtered[:n])
             pk = ops.pack(cg, f, pipe.dtype, out=packed)
             ops.fdk_bp(cg, pk, pipe.dtype, out=vol)
             consumed[b].record(compute)

@@ -176,11 +176,16 @@ class TcFilter:
         _lib.call("mct_filter_tc", self.dg.g(), _ptr(weighted), self.dtype, self.ws, _ptr(out), _stream())
         return out
 
-    def weight_filter(self, sgm, row_stride, view_stride, bh=None, out=None):
+    def weight_filter(self, sgm, row_stride, view_stride, bh=None, out=None, dg=None):
         """Weighting (BH, cosine, Parker) and this filter in one pass over the sinogram:
         the weighting runs while the operand is split, the weighted float32 sinogram is
-        never written (mct_weight_filter).  Same result as weight() then __call__."""
-        g = self.dg.geom
+        never written (mct_weight_filter).  Same result as weight() then __call__.  dg:
+        the geometry to weight for, when it is another view chunk of the same size as
+        the one this filter was built for (the weights depend on the chunk's views)."""
+        dg = self.dg if dg is None else dg
+        g = dg.geom
+        if (g.nv, g.views, g.nu) != (self.dg.geom.nv, self.dg.geom.views, self.dg.geom.nu):
+            raise ValueError("the geometry's sinogram size differs from this filter's")
         _check(sgm, "sgm")
         if out is None:
             out = torch.empty((g.views, g.nv, g.nu), dtype=torch.float32, device=sgm.device)
@@ -189,7 +194,7 @@ class TcFilter:
         if bh is not None:
             _check(bh, "bh")
             n_bh = bh.numel()
-        _lib.call("mct_weight_filter", self.dg.g(), self.dg.t(), _ptr(sgm), int(row_stride), int(view_stride),
+        _lib.call("mct_weight_filter", dg.g(), dg.t(), _ptr(sgm), int(row_stride), int(view_stride),
                   _ptr(bh), n_bh, self.dtype, self.ws, _ptr(out), _stream())
         return out
 

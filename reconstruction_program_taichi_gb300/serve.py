@@ -190,7 +190,7 @@ class _FbpSlot:
                          for _ in range(batch)]
         self.graphs = []
         self.last_used = time.perf_counter()
-        self.nbytes = sum(p.nbytes() for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
+        self.nbytes = sum(p.allocate().nbytes() for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
             self.graphs = _capture_members(self.stream, [lambda i=i: self._member(i) for i in range(batch)])
 
