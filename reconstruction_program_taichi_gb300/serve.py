@@ -186,11 +186,15 @@ class _FbpSlot:
             self.inp = [torch.zeros(shape, dtype=torch.float32, device=device) for _ in range(batch)]
             self.out = [torch.zeros(self.pipes[0].dg.vol_shape, dtype=torch.float32, device=device)
                         for _ in range(batch)]
+            # the pipelines' buffers and tensor-core filters (whose set-up kernel runs
+            # here, on the slot's stream), before the slot counts its bytes
+            for p in self.pipes:
+                p.allocate()
         self.host_out = [torch.empty(self.pipes[0].dg.vol_shape, dtype=torch.float32, pin_memory=True)
                          for _ in range(batch)]
         self.graphs = []
         self.last_used = time.perf_counter()
-        self.nbytes = sum(p.allocate().nbytes() for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
+        self.nbytes = sum(p.nbytes() for p in self.pipes) + sum(t.numel() * 4 for t in self.inp + self.out)
         if use_graph:
             self.graphs = _capture_members(self.stream, [lambda i=i: self._member(i) for i in range(batch)])
 
