@@ -792,7 +792,7 @@ def test_fused_cg_epilogue_matches_separate_passes(cuda, n_terms, it):
         assert abs(float(dq) - dq_ref) <= (1e-6 if it == "float32" else 1e-2) * abs(dq_ref)
 
 
-def test_fused_cg_solve_matches_separate_passes(cuda):
+def test_fused_cg_solve_matches_separate_passes(tmp_path, cuda):
     """A whole IRN-CGLS-PICCS solve (two TV terms per operator) with the fused epilogue
     against the same solve with the separate passes."""
     import torch
@@ -801,9 +801,9 @@ def test_fused_cg_solve_matches_separate_passes(cuda):
     outs = []
     for fuse in (True, False):
         cfg = dict(z["config"], NumberOfIRNIterations=2, NumberOfIterations=4)
-        path = f"/tmp/mct_prior_fuse_{int(fuse)}.raw"
+        path = tmp_path / f"prior_fuse_{int(fuse)}.raw"
         z["prior"].astype(np.float32).tofile(path)
-        cfg["PriorImageFile"] = path
+        cfg["PriorImageFile"] = str(path)
         ir = Mgfbp_ir_piccs(cfg, verbose=False)
         ir.system.fuse = fuse
         assert ir.system.fused_cg(2) == fuse
