@@ -868,3 +868,20 @@ def test_fp_long_scan_tiles_vs_oracle(cuda, storage):
                                zpv=dg.geom.fp_z_per_view, rows=o.det_elem_count_vertical, K=dg.geom.fp_steps)
     assert np.count_nonzero(ref) > 0.2 * ref.size
     assert rel_l2(got, ref) < (TOL if storage == "f32" else 5e-3)
+
+
+def test_view_streaming_holds_no_full_size_buffers(tmp_path, cuda):
+    """Mgfbp_v2 streams view chunks through its pipeline's geometry and taps: the
+    pipeline's full-size buffers (weighted, filtered, packed sinograms, the whole-sinogram
+    tensor-core operand tiles, its own volume) are never allocated, and the result
+    matches the whole-sinogram FBP."""
+    from reconstruction_program_taichi_gb300.config import ReadConfigFile
+    from reconstruction_program_taichi_gb300.fbp import Mgfbp, Mgfbp_v2
+    z = load_golden("fdk_cone")
+    path = _write_case(z, tmp_path, "fbp")
+    streamed = Mgfbp_v2(ReadConfigFile(path), verbose=False, views_per_chunk=7)
+    img = streamed.MainFunction()
+    assert streamed.pipeline.nbytes() == 0
+    whole = Mgfbp(ReadConfigFile(path), verbose=False).MainFunction()
+    assert np.array_equal(img == 0, whole == 0)
+    assert rel_l2(img, whole) < 1e-5
