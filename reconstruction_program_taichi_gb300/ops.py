@@ -116,9 +116,23 @@ def fdk_bp_finish(dg, vol):
 
 # ---------------------------------------------------------------- FBP / FDK
 
+def _check_strided(sgm, g, row_stride, view_stride):
+    """The strided sinogram (element (row, view, col) at row*row_stride +
+    view*view_stride + col) must lie inside sgm: the kernels read every element."""
+    _check(sgm, "sgm")
+    row_stride, view_stride = int(row_stride), int(view_stride)
+    if row_stride < 0 or view_stride < 0:
+        raise ValueError("sinogram strides must be non-negative")
+    last = (g.nv - 1) * row_stride + (g.views - 1) * view_stride + g.nu
+    if last > sgm.numel():
+        raise ValueError(f"sgm holds {sgm.numel()} elements; strides ({row_stride}, {view_stride}) over "
+                         f"{g.nv} rows x {g.views} views x {g.nu} columns address {last}")
+    return row_stride, view_stride
+
+
 def weight(dg, sgm, row_stride, view_stride, bh=None, out=None):
     """BH polynomial + cosine (+ Parker) weighting into [nv, views, nu]."""
-    _check(sgm, "sgm")
+    row_stride, view_stride = _check_strided(sgm, dg.geom, row_stride, view_stride)
     if out is None:
         out = torch.empty(dg.sgm_shape, dtype=torch.float32, device=sgm.device)
     _check(out, "out", dg.sgm_shape)
@@ -186,7 +200,7 @@ class TcFilter:
         g = dg.geom
         if (g.nv, g.views, g.nu) != (self.dg.geom.nv, self.dg.geom.views, self.dg.geom.nu):
             raise ValueError("the geometry's sinogram size differs from this filter's")
-        _check(sgm, "sgm")
+        row_stride, view_stride = _check_strided(sgm, g, row_stride, view_stride)
         if out is None:
             out = torch.empty((g.views, g.nv, g.nu), dtype=torch.float32, device=sgm.device)
         _check(out, "out", (g.views, g.nv, g.nu))

@@ -844,6 +844,28 @@ def test_weight_filter_fused_matches_separate(cuda, case, parts):
     assert torch.equal(got, ref)
 
 
+def test_strided_sinogram_must_cover_its_extent(cuda):
+    """A strided sinogram smaller than the extent its strides address is refused on the
+    host, before any kernel reads past its end (both weighting entry points)."""
+    import torch
+    from reconstruction_program_taichi_gb300 import geometry, ops
+    o = _cone_obj(nu=72, nv=12, views=50)
+    dg = geometry.fbp_geometry(o)
+    g = dg.geom
+    taps = torch.tensor(geometry.recon_taps(o), dtype=torch.float32, device="cuda")
+    tc = ops.TcFilter(dg, taps)
+    full = torch.rand((g.views, g.nv, g.nu), device="cuda")
+    rs, vs = g.nu, g.nv * g.nu  # view-major input
+    short = full.flatten()[:-1]
+    for call in (lambda s, r, v: ops.weight(dg, s, r, v), lambda s, r, v: tc.weight_filter(s, r, v)):
+        with pytest.raises(ValueError, match="address"):
+            call(short, rs, vs)
+        with pytest.raises(ValueError, match="non-negative"):
+            call(full, -rs, vs)
+        call(full, rs, vs)  # the exact extent is accepted
+    torch.cuda.synchronize()
+
+
 @pytest.mark.parametrize("storage", ["f32", "bf16"])
 def test_fp_long_scan_tiles_vs_oracle(cuda, storage):
     """Scans of 256 views or more take the projector's 16-column x 16-view tiles with 4
