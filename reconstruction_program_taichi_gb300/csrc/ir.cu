@@ -136,9 +136,8 @@ bp_unmatched_kernel(UbParams p, const float* __restrict__ angles, const float* _
 // (run_mgfbp_iterative_recon_IRN_CGLS.py:417-421) with the square root as d2 * rsqrt(d2).
 // A column that leaves the detector in u in some view is all zero in the reference
 // (SetTruncatedRegionToZero), so its thread stops there.  As in the FDK kernel, v and
-// z are affine in the slice index, and the register budget (128 for 16-byte
-// operands, 80 for 8-byte ones) lets all UA_ZC gathers of a view issue before their
-// arithmetic, which hides the gather latency.
+// z are affine in the slice index, and the register budget lets the UA_ZC gathers of
+// a view issue ahead of their arithmetic, which hides the gather latency.
 constexpr int UA_ZC = 16;
 
 // (D^T W D x)[i] of run_mgfbp_iterative_recon_IRN_CGLS.py:267-286: forward differences
@@ -186,12 +185,16 @@ struct CgEpi {
     float s1, s2;
     double* partials;  // one per block, in blockIdx order
 };
-template <typename QT>
+// Resident blocks per SM that the register allocation targets: 3 (80 registers) for
+// 8-byte operands and for 16-byte ones without the CG epilogue (with slices in pairs,
+// 512x512x64 / 360 views float32 5.67 ms with 2 blocks of 128 registers, 5.44 ms with
+// 3 blocks, bit-identical), 2 for 16-byte operands with the epilogue.
+template <typename QT, bool EPI>
 constexpr int ua_min_blocks() {
-    return sizeof(QT) == 8 ? 3 : 2;
+    return sizeof(QT) == 8 || !EPI ? 3 : 2;
 }
 template <bool CONE, typename QT, typename PT, typename OT = float, bool EPI = false>
-__global__ void __launch_bounds__(UB_TX* UB_TY, ua_min_blocks<QT>())
+__global__ void __launch_bounds__(UB_TX* UB_TY, ua_min_blocks<QT, EPI>())
 bp_unmatched_axial_kernel(UbParams p, const float* __restrict__ angles, const float* __restrict__ czv, float cz_const,
                           const void* __restrict__ packed, OT* __restrict__ vol,
                           const uint32_t* __restrict__ f16_max, CgEpi epi = CgEpi{}) {
