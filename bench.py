@@ -776,19 +776,19 @@ def widen_bench(dev, stream, barrier):
         verbose = False
 
     opts = {"curved": {"CurvedDetector": True}, "short_scan_220deg": {"TotalScanAngle": 220},
-            "coronal": {"ReconViewMode": "coronal"}, "pmatrix": None}
+            "coronal": {"ReconViewMode": "coronal"}, "sagittal": {"ReconViewMode": "sagittal"},
+            "pmatrix": {}, "pmatrix_coronal": {"ReconViewMode": "coronal"}}
     res = {}
     sgm = torch.from_numpy(rng.uniform(0, 1, (w["nv"], w["views"], w["nu"])).astype(np.float32)).to(dev)
     with tempfile.TemporaryDirectory() as d:
         for name, extra in opts.items():
             cfg = make_config(w)
-            if extra is None:
+            if name.startswith("pmatrix"):
                 path = os.path.join(d, "pmatrix.jsonc")
                 with open(path, "w") as f:
                     json.dump({"Value": [float(x) for x in circular_pmatrices(w)]}, f)
                 cfg["PMatrixFile"] = path
-            else:
-                cfg.update(extra)
+            cfg.update(extra)
             o = _Obj()
             mcfg.parse_fbp(o, cfg)
             pipe = FdkPipeline(o, device=dev)

@@ -38,12 +38,18 @@ constexpr int bp_min_blocks() {
 
 struct BpParams {
     int nx, nz, nu, nv, views, cone, curved;
+    // the kernel's index frame: a thread owns column (ix, iy) with ix in [0, nx), iy in
+    // [0, ncb), and slices iz in [0, nsl) at vol[iz * ss + iy * sb + ix].  Axial: (iy, iz)
+    // are the image's (i_y, i_z); coronal and sagittal: the image's (i_z, i_y), so that
+    // the slice axis is the one along z and x, y stay fixed per column
+    int ncb, nsl;
+    int64_t sb, ss;
     int view_begin, views_total, accumulate;  // view-chunked FBP (scan index of view 0, scan size)
     float sid, sdd, img_rot;
     float u0, inv_ustep;   // uidx = (u - u0) * inv_ustep
     float v0, kv;          // vidx = (mag*z - v0) * kv, kv = sign(v_step)/dv
     float div;             // redundancy factor
-    // voxel centre of (ix, iy, iz) = P + ix*EX + iy*EY + iz*EZ (rotated frame)
+    // voxel centre of (ix, iy, iz) of the kernel's frame = P + ix*EX + iy*EY + iz*EZ (rotated)
     float px_x, px_y, px_z;  // EX
     float py_x, py_y, py_z;  // EY
     float pz_x, pz_y, pz_z;  // EZ
@@ -65,10 +71,10 @@ __device__ __forceinline__ void fill_view_table(const BpParams& p, const float* 
     }
 }
 
-// MODE 0: axial, flat or curved detector, no projection matrix (u hoisted per column)
-// MODE 1: any view mode, no projection matrix (per-voxel u)
-// MODE 2: projection matrix geometry, any view mode (per-voxel matrix products)
-// MODE 3: projection matrix geometry, axial view mode (per-column matrix rows)
+// MODE 0: cone beam in any view mode, or axial fan beam; flat or curved detector, no
+//         projection matrix (u hoisted per column of the kernel's frame)
+// MODE 1: fan beam in the coronal or sagittal view mode (per-voxel u)
+// MODE 3: projection matrix geometry in any view mode (per-column matrix rows)
 template <int MODE, bool CONE, typename QT, typename PT>
 __global__ void __launch_bounds__(BP_TX* BP_TY, bp_min_blocks<MODE, QT>())
 fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
@@ -84,7 +90,7 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
     const int ix = blockIdx.x * BP_TX + (warp % (BP_TX / BP_WX)) * BP_WX + (lane % BP_WX);
     const int iy = blockIdx.y * BP_TY + (warp / (BP_TX / BP_WX)) * (32 / BP_WX) + lane / BP_WX;
     const int zb = blockIdx.z * BP_ZC;
-    const bool active = ix < p.nx && iy < p.nx;
+    const bool active = ix < p.nx && iy < p.ncb;
     const int nq = p.nu - 1;  // packed columns; packed rows per view: nv (cone: row nv-1 is NaN)
 
     // voxel centres of the ZC slices of this column: c_k = c0 + k * dc
@@ -171,14 +177,14 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
 #pragma unroll
                     for (int k = 0; k < BP_ZC; ++k) {
-                        if (zb + k < p.nz) {
+                        if (zb + k < p.nsl) {
                             const float2 pr = Pair<PT>::load(base + (int64_t)k * nq);
                             acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
                         }
                     }
                 }
             } else if (MODE == 3) {
-                // Axial view mode with projection matrices: x and y are fixed per column, so
+                // Projection matrices: in the kernel's frame x and y are fixed per column, so
                 // the matrix rows are affine in the slice index and the distance weight does
                 // not depend on z.  An untilted trajectory has no z term in the u and depth
                 // rows (P2 = P10 = 0 up to rounding left by the matrix processing): when
@@ -246,34 +252,21 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     }
                 }
             } else {
-                const float* P = pmat + 12 * (p.view_begin + j);
-                float P0 = 0, P1 = 0, P2 = 0, P3 = 0, P4 = 0, P5 = 0, P6 = 0, P7 = 0, P8 = 0, P9 = 0, P10 = 0, P11 = 0;
-                if (MODE == 2) {
-                    P0 = __ldg(P + 0); P1 = __ldg(P + 1); P2 = __ldg(P + 2); P3 = __ldg(P + 3);
-                    P4 = __ldg(P + 4); P5 = __ldg(P + 5); P6 = __ldg(P + 6); P7 = __ldg(P + 7);
-                    P8 = __ldg(P + 8); P9 = __ldg(P + 9); P10 = __ldg(P + 10); P11 = __ldg(P + 11);
-                }
-                // the voxel moves by (pz_x, pz_y, pz_z) per slice, so L and t are affine in k
+                // MODE 1 (fan beam, coronal or sagittal view mode): the voxel moves by
+                // (pz_x, pz_y) per slice, so L and t are affine in k; slice k reads
+                // detector row zb + k
+                static_assert(MODE != 1 || !CONE, "cone beam takes MODE 0 or 3 in every view mode");
                 const float L0 = p.sid - c0x * cb - c0y * sb, dL = -(p.pz_x * cb + p.pz_y * sb);
                 const float t0 = -c0x * sb + c0y * cb, dt = -p.pz_x * sb + p.pz_y * cb;
 #pragma unroll
                 for (int k = 0; k < BP_ZC; ++k) {
-                    if (zb + k >= p.nz || (dead >> k) & 1u) continue;
-                    const float x = fmaf((float)k, p.pz_x, c0x);
-                    const float y = fmaf((float)k, p.pz_y, c0y);
-                    const float z = fmaf((float)k, p.pz_z, c0z);
+                    if (zb + k >= p.nsl || (dead >> k) & 1u) continue;
                     const float L = fmaf((float)k, dL, L0);
                     const float t = fmaf((float)k, dt, t0);
-                    float mag, ui, rL = 0.0f;
-                    if (MODE == 2) {
-                        mag = 1.0f / (P8 * x + P9 * y + P10 * z + P11);
-                        ui = (P0 * x + P1 * y + P2 * z + P3) * mag;
-                    } else {
-                        rL = 1.0f / L;  // one reciprocal for the magnification and the flat distance weight
-                        mag = p.sdd * rL;
-                        const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
-                        ui = (u - p.u0) * p.inv_ustep;
-                    }
+                    const float rL = 1.0f / L;  // one reciprocal for the magnification and the flat distance weight
+                    const float mag = p.sdd * rL;
+                    const float u = p.curved ? p.sdd * atan2f(t, L) : mag * t;
+                    const float ui = (u - p.u0) * p.inv_ustep;
                     if (!(ui >= 0.0f && ui + 1.0f <= (float)(p.nu - 1))) {
                         dead |= 1u << k;
                         continue;
@@ -281,40 +274,24 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                     const float uf = floorf(ui);
                     const float ru = ui - uf;
                     const int uc = (int)uf;
-                    const float dw = p.curved ? 1.0f / (L * L + t * t) : (MODE == 2 ? 1.0f / (L * L) : rL * rL);
+                    const float dw = p.curved ? 1.0f / (L * L + t * t) : rL * rL;
                     const float w = (p.sid * dw) * tb.z;
-                    if (CONE) {
-                        const float vi = (MODE == 2) ? (P4 * x + P5 * y + P6 * z + P7) * mag : (mag * z - p.v0) * p.kv;
-                        const float vf = floorf(vi);
-                        const int vr = (int)vf;
-                        if (vr < 0 || vr > p.nv - 2) {
-                            dead |= 1u << k;
-                            continue;
-                        }
-                        const float rv = vi - vf;
-                        float2 lo, hi;
-                        Quad<QT>::load(reinterpret_cast<const QT*>(packed) + ((int64_t)j * p.nv + vr) * nq + uc, lo, hi);
-                        const float2 s2 = __ffma2_rn(make_float2(ru, ru), hi, lo);
-                        acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
-                    } else {
-                        const float2 pr = Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb + k) * nq + uc);
-                        acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
-                    }
+                    const float2 pr = Pair<PT>::load(reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb + k) * nq + uc);
+                    acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
                 }
             }
         }
     }
     if (!active) return;
-    const int64_t plane = (int64_t)p.nx * p.nx;
-    float* out = vol + (int64_t)zb * plane + (int64_t)iy * p.nx + ix;
+    float* out = vol + (int64_t)zb * p.ss + (int64_t)iy * p.sb + ix;
 #pragma unroll
     for (int k = 0; k < BP_ZC; ++k) {
-        if (zb + k < p.nz) {
+        if (zb + k < p.nsl) {
             const bool off_detector = ((dead >> k) & 1u) || acc[k] != acc[k];
             if (p.accumulate)  // a voxel off the detector in any chunk stays NaN until mct_fdk_bp_finish
-                out[(int64_t)k * plane] = off_detector ? __int_as_float(0x7fffffff) : out[(int64_t)k * plane] + acc[k];
+                out[(int64_t)k * p.ss] = off_detector ? __int_as_float(0x7fffffff) : out[(int64_t)k * p.ss] + acc[k];
             else
-                out[(int64_t)k * plane] = off_detector ? 0.0f : acc[k];
+                out[(int64_t)k * p.ss] = off_detector ? 0.0f : acc[k];
         }
     }
 }
@@ -488,24 +465,33 @@ extern "C" int mct_fdk_bp(const mct_geom* g, const mct_tables* t, const void* pa
         y = (float)(-a[0] * sr + a[1] * cr);
         z = (float)a[2];
     };
+    // The kernel's frame.  In the coronal and sagittal view modes the image's i_y axis is
+    // the one along z and its i_x, i_z axes lie in the (x, y) plane, so with cone beam the
+    // kernel takes (i_x, i_z) as the column and i_y as the slice axis: x and y are then
+    // fixed per column, as in the axial mode, and the same hoisted kernels apply (u, the
+    // weight and the truncation test once per column and view, v affine in the slice).
+    const int64_t plane = (int64_t)g->nx * g->nx;
+    const bool permuted = cone && g->view_mode != 1;
     rot(ax, p.px_x, p.px_y, p.px_z);
-    rot(ay, p.py_x, p.py_y, p.py_z);
-    rot(az, p.pz_x, p.pz_y, p.pz_z);
+    rot(permuted ? az : ay, p.py_x, p.py_y, p.py_z);
+    rot(permuted ? ay : az, p.pz_x, p.pz_y, p.pz_z);
     rot(a0, p.o_x, p.o_y, p.o_z);
+    p.ncb = permuted ? g->nz : g->nx;
+    p.nsl = permuted ? g->nx : g->nz;
+    p.sb = permuted ? plane : g->nx;
+    p.ss = permuted ? g->nx : plane;
     dim3 block(BP_TX, BP_TY);
-    dim3 grid((g->nx + BP_TX - 1) / BP_TX, (g->nx + BP_TY - 1) / BP_TY, (g->nz + BP_ZC - 1) / BP_ZC);
+    dim3 grid((g->nx + BP_TX - 1) / BP_TX, (p.ncb + BP_TY - 1) / BP_TY, (p.nsl + BP_ZC - 1) / BP_ZC);
+    MCT_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "mct_fdk_bp: volume too large for the launch grid");
     cudaStream_t s = as_stream(stream);
-    const bool axial_fast = g->view_mode == 1 && !pm;
     const uint32_t* fm = dtype == MCT_F16 ? f16_trailer(g, packed) : nullptr;
-    if (pm && g->view_mode == 1) launch_bp<3, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
-    else if (pm) launch_bp<2, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
-    else if (axial_fast && cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
-    else if (axial_fast) {
+    if (pm) launch_bp<3, true>(p, grid, block, s, t->angles, t->pmatrix, packed, dtype, vol, fm);
+    else if (cone) launch_bp<0, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
+    else if (g->view_mode == 1) {
         MCT_REQUIRE(g->nx <= 65535, "mct_fdk_bp: fan beam images are at most 65535 pixels wide");
         if (g->nz == 1) launch_bp_fan<1>(p, g, s, t->angles, packed, dtype, vol, fm);
         else launch_bp_fan<8>(p, g, s, t->angles, packed, dtype, vol, fm);
     }
-    else if (cone) launch_bp<1, true>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     else launch_bp<1, false>(p, grid, block, s, t->angles, nullptr, packed, dtype, vol, fm);
     return launched("fdk_bp_kernel");
 }

@@ -110,8 +110,13 @@ def _smooth(rng, nz, n):
 
 
 @pytest.mark.parametrize("kw", [{}, {"ReconViewMode": "coronal"}, {"CurvedDetector": True, "TotalScanAngle": 220},
-                                {"ImageDimension": 37, "ImageDimensionZ": 13, "DetectorElementCountHorizontal": 75}])
+                                {"ImageDimension": 37, "ImageDimensionZ": 13, "DetectorElementCountHorizontal": 75},
+                                {"ReconViewMode": "sagittal", "CurvedDetector": True, "ImageDimension": 37,
+                                 "ImageDimensionZ": 13, "DetectorElementCountHorizontal": 75}])
 def test_fdk_ops_vs_oracle(kw, cuda):
+    """FDK against the float64 oracle.  Coronal and sagittal volumes run the axial
+    kernel in a permuted frame (columns over the image's i_x, i_z; slices along i_y),
+    here also with extents that are not multiples of the block (37 x 37 x 13)."""
     import torch
     from reconstruction_program_taichi_gb300 import fbp, geometry
     o = _cone_obj(**kw)
@@ -201,8 +206,8 @@ def _circular_pmatrices(nu, nv, views, sid, sdd, du, dv, u_shift=0.3, v_shift=-0
 
 @pytest.mark.parametrize("mode", ["coronal", "sagittal"])
 def test_pmatrix_fdk_other_view_modes_vs_oracle(mode, tmp_path, cuda):
-    """Projection matrices in the coronal / sagittal view modes (per-voxel matrix
-    products) against the float64 oracle."""
+    """Projection matrices in the coronal / sagittal view modes (the per-column matrix
+    rows of the kernel's permuted frame) against the float64 oracle."""
     import torch
     from reconstruction_program_taichi_gb300 import fbp, geometry
     geo = dict(nu=64, nv=24, views=60, sid=300.0, sdd=550.0, du=0.8, dv=0.8)
@@ -892,14 +897,16 @@ def test_fp_long_scan_tiles_vs_oracle(cuda, storage):
     assert rel_l2(got, ref) < (TOL if storage == "f32" else 5e-3)
 
 
-def test_view_streaming_holds_no_full_size_buffers(tmp_path, cuda):
+@pytest.mark.parametrize("name", ["fdk_cone", "fdk_cone_postlog_coronal", "fdk_cone_sagittal_curved_short"])
+def test_view_streaming_holds_no_full_size_buffers(name, tmp_path, cuda):
     """Mgfbp_v2 streams view chunks through its pipeline's geometry and taps: the
     pipeline's full-size buffers (weighted, filtered, packed sinograms, the whole-sinogram
     tensor-core operand tiles, its own volume) are never allocated, and the result
-    matches the whole-sinogram FBP."""
+    matches the whole-sinogram FBP (also in the coronal and sagittal view modes, whose
+    chunks accumulate through the backprojector's permuted frame)."""
     from reconstruction_program_taichi_gb300.config import ReadConfigFile
     from reconstruction_program_taichi_gb300.fbp import Mgfbp, Mgfbp_v2
-    z = load_golden("fdk_cone")
+    z = load_golden(name)
     path = _write_case(z, tmp_path, "fbp")
     streamed = Mgfbp_v2(ReadConfigFile(path), verbose=False, views_per_chunk=7)
     img = streamed.MainFunction()
