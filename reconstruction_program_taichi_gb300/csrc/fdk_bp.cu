@@ -79,7 +79,11 @@ template <int MODE, bool CONE, typename QT, typename PT>
 __global__ void __launch_bounds__(BP_TX* BP_TY, bp_min_blocks<MODE, QT>())
 fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restrict__ pmat,
               const void* __restrict__ packed, float* __restrict__ vol, const uint32_t* __restrict__ f16_max) {
-    __shared__ float4 tab[BP_VCHUNK];  // {cos b, sin b, dbeta*div, unused}
+    // views per chunk of the shared tables; with projection matrices the chunk's 3x4
+    // matrices are staged too (12 floats a view), in chunks of a quarter the size
+    constexpr int VCH = MODE == 3 ? BP_VCHUNK / 4 : BP_VCHUNK;
+    __shared__ float4 tab[VCH];  // {cos b, sin b, dbeta*div, unused}
+    __shared__ __align__(16) float pms[MODE == 3 ? 12 * VCH : 4];
     const int tid = threadIdx.y * BP_TX + threadIdx.x;
     // A warp is 4 columns along x x 8 along y of the block's 32 x 8: for one view its
     // columns project onto fewer detector columns than a row of 32 (about 4|sin| + 8|cos|
@@ -105,10 +109,14 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
 
     // float16 operands hold values scaled by 2^e: fold 2^-e (exact) into the view weight
     const float unscale = IsF16<QT>::value ? ldexpf(1.0f, -f16_scale_exp(*f16_max)) : 1.0f;
-    for (int jc = 0; jc < p.views; jc += BP_VCHUNK) {
-        const int nvc = min(BP_VCHUNK, p.views - jc);
+    for (int jc = 0; jc < p.views; jc += VCH) {
+        const int nvc = min(VCH, p.views - jc);
         __syncthreads();
         fill_view_table(p, angles, tab, jc, nvc, tid, BP_TX * BP_TY, unscale);
+        if (MODE == 3) {
+            const float* src = pmat + 12 * (int64_t)(p.view_begin + jc);
+            for (int q = tid; q < 12 * nvc; q += BP_TX * BP_TY) pms[q] = __ldg(src + q);
+        }
         __syncthreads();
         if (!active || dead == 0xffffffffu) continue;
 
@@ -191,10 +199,11 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                 // 16 |B| < 2^-26 |A| for both, fmaf(k, B, A) rounds to A for every slice, so
                 // u and the magnification are the column's (as in MODE 0) and taking them
                 // once gives exactly the per-slice result.
-                const float* P = pmat + 12 * (p.view_begin + j);
-                const float P0 = __ldg(P + 0), P1 = __ldg(P + 1), P2 = __ldg(P + 2), P3 = __ldg(P + 3);
-                const float P4 = __ldg(P + 4), P5 = __ldg(P + 5), P6 = __ldg(P + 6), P7 = __ldg(P + 7);
-                const float P8 = __ldg(P + 8), P9 = __ldg(P + 9), P10 = __ldg(P + 10), P11 = __ldg(P + 11);
+                const float4* P = reinterpret_cast<const float4*>(pms + 12 * q);  // the view's matrix, staged
+                const float4 r0 = P[0], r1 = P[1], r2 = P[2];
+                const float P0 = r0.x, P1 = r0.y, P2 = r0.z, P3 = r0.w;
+                const float P4 = r1.x, P5 = r1.y, P6 = r1.z, P7 = r1.w;
+                const float P8 = r2.x, P9 = r2.y, P10 = r2.z, P11 = r2.w;
                 const float dz = p.pz_z;
                 const float Au = P0 * c0x + P1 * c0y + P2 * c0z + P3, Bu = P2 * dz;
                 const float Av = P4 * c0x + P5 * c0y + P6 * c0z + P7, Bv = P6 * dz;
