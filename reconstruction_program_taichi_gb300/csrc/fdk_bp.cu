@@ -5,12 +5,14 @@
 //     view in registers (the reference does a global read-modify-write per view);
 //   * the filtered sinogram is pre-packed so that the 2x2 bilinear stencil of a
 //     detector position is ONE 16-byte (f32) or 8-byte (bf16) load;
-//   * per-view cos/sin/weight tables live in shared memory;
-//   * axial slices share u across the column, so u, the distance weight and the
+//   * per-view cos/sin/weight tables (and projection matrices) live in shared memory;
+//   * the slices of a column share x and y (z runs along the image's i_z axis in the
+//     axial view mode and along i_y in the coronal and sagittal ones, whose columns
+//     the kernel takes over (i_x, i_z)), so u, the distance weight and the
 //     magnification are evaluated once per (column, view) and v is an affine
 //     function of the slice index.
 // Voxels that project outside the detector in any view are written as 0, as in the
-// reference (the view loop "breaks" with the voxel set to 0).  In the axial cone-beam
+// reference (the view loop "breaks" with the voxel set to 0).  In the cone-beam
 // path an off-detector row index is redirected to the packed operand's NaN row, so the
 // voxel's sum becomes NaN and is written as 0 without any per-slice bookkeeping (a
 // voxel whose sum is NaN because the sinogram itself holds NaN is written as 0 too,
