@@ -116,18 +116,23 @@ def fdk_bp_finish(dg, vol):
 
 # ---------------------------------------------------------------- FBP / FDK
 
-def _check_strided(sgm, g, row_stride, view_stride):
-    """The strided sinogram (element (row, view, col) at row*row_stride +
-    view*view_stride + col) must lie inside sgm: the kernels read every element."""
-    _check(sgm, "sgm")
+def strided_extent(nv, views, nu, row_stride, view_stride):
+    """Elements a strided sinogram must hold: element (row, view, col) sits at
+    row*row_stride + view*view_stride + col.  Raises on negative strides."""
     row_stride, view_stride = int(row_stride), int(view_stride)
     if row_stride < 0 or view_stride < 0:
         raise ValueError("sinogram strides must be non-negative")
-    last = (g.nv - 1) * row_stride + (g.views - 1) * view_stride + g.nu
+    return (nv - 1) * row_stride + (views - 1) * view_stride + nu
+
+
+def _check_strided(sgm, g, row_stride, view_stride):
+    """The strided sinogram must lie inside sgm: the kernels read every element."""
+    _check(sgm, "sgm")
+    last = strided_extent(g.nv, g.views, g.nu, row_stride, view_stride)
     if last > sgm.numel():
         raise ValueError(f"sgm holds {sgm.numel()} elements; strides ({row_stride}, {view_stride}) over "
                          f"{g.nv} rows x {g.views} views x {g.nu} columns address {last}")
-    return row_stride, view_stride
+    return int(row_stride), int(view_stride)
 
 
 def weight(dg, sgm, row_stride, view_stride, bh=None, out=None):

@@ -152,3 +152,17 @@ def test_pmatrix_processing_matches_reference(name, tmp_path):
     got = [o.source_isocenter_dis, o.source_det_dis, o.det_offset_horizontal, o.det_offset_vertical,
            o.total_scan_angle, o.img_center_z]
     np.testing.assert_allclose(got, z["pm_params"], rtol=1e-6, atol=1e-5)
+
+
+def test_strided_sinogram_extent():
+    """The element count a strided sinogram must hold, which the weighting entry points
+    check before any launch: both file layouts fill their buffer exactly, and a view
+    chunk of a larger [rows][views][cols] buffer reaches only its own last element."""
+    from reconstruction_program_taichi_gb300.ops import strided_extent
+    nv, views, nu = 12, 50, 72
+    assert strided_extent(nv, views, nu, views * nu, nu) == nv * views * nu  # [rows][views][cols]
+    assert strided_extent(nv, views, nu, nu, nv * nu) == nv * views * nu  # post-log [views][rows][cols]
+    assert strided_extent(nv, 7, nu, 120 * nu, nu) == (nv - 1) * 120 * nu + 7 * nu
+    for rs, vs in ((-1, nu), (nu, -nu)):
+        with pytest.raises(ValueError, match="non-negative"):
+            strided_extent(nv, views, nu, rs, vs)
