@@ -73,8 +73,8 @@ __device__ __forceinline__ void fill_view_table(const BpParams& p, const float* 
     }
 }
 
-// MODE 0: cone beam in any view mode, or axial fan beam; flat or curved detector, no
-//         projection matrix (u hoisted per column of the kernel's frame)
+// MODE 0: cone beam in any view mode; flat or curved detector, no projection matrix
+//         (u hoisted per column of the kernel's frame)
 // MODE 1: fan beam in the coronal or sagittal view mode (per-voxel u)
 // MODE 3: projection matrix geometry in any view mode (per-column matrix rows)
 template <int MODE, bool CONE, typename QT, typename PT>
@@ -127,7 +127,8 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
             const float4 tb = tab[q];
             const float cb = tb.x, sb = tb.y;
             if (MODE == 0) {
-                // u is shared by the whole column
+                // u is shared by the whole column (cone beam: axial fan beam has its own kernel)
+                static_assert(MODE != 0 || CONE, "MODE 0 is the cone-beam kernel");
                 const float L = p.sid - c0x * cb - c0y * sb;
                 const float t = -c0x * sb + c0y * cb;
                 const float rL = 1.0f / L;  // one reciprocal for the magnification and the flat distance weight
@@ -143,54 +144,43 @@ fdk_bp_kernel(BpParams p, const float* __restrict__ angles, const float* __restr
                 const int uc = (int)uf;
                 const float dw = p.curved ? 1.0f / (L * L + t * t) : rL * rL;
                 const float w = (p.sid * dw) * tb.z;
-                if (CONE) {
-                    const float vA = (mag * c0z - p.v0) * p.kv;
-                    const float vB = (mag * p.pz_z) * p.kv;
-                    const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq + uc;
-                    const float2 ru2 = make_float2(ru, ru);
-                    const unsigned nan_row = (unsigned)(p.nv - 1);
-                    if constexpr (sizeof(QT) == 8) {
-                        // 16-bit operands: slices in pairs, row index and weight as f32x2
-                        // (the same values; at 512x512x256 / 1080 views bf16 48.9 ms
-                        // against 49.7, float32 53.6 against 52.3, so float32 keeps the
-                        // scalar loop)
-                        const float2 vA2 = make_float2(vA, vA), vB2 = make_float2(vB, vB);
+                const float vA = (mag * c0z - p.v0) * p.kv;
+                const float vB = (mag * p.pz_z) * p.kv;
+                const QT* base = reinterpret_cast<const QT*>(packed) + (int64_t)j * p.nv * nq + uc;
+                const float2 ru2 = make_float2(ru, ru);
+                const unsigned nan_row = (unsigned)(p.nv - 1);
+                if constexpr (sizeof(QT) == 8) {
+                    // 16-bit operands: slices in pairs, row index and weight as f32x2
+                    // (the same values; at 512x512x256 / 1080 views bf16 48.9 ms
+                    // against 49.7, float32 53.6 against 52.3, so float32 keeps the
+                    // scalar loop)
+                    const float2 vA2 = make_float2(vA, vA), vB2 = make_float2(vB, vB);
 #pragma unroll
-                        for (int k = 0; k < BP_ZC; k += 2) {
-                            const float2 vi = __ffma2_rn(make_float2((float)k, (float)(k + 1)), vB2, vA2);
-                            const float vf0 = floorf(vi.x), vf1 = floorf(vi.y);
-                            const unsigned vr0 = min((unsigned)(int)vf0, nan_row);
-                            const unsigned vr1 = min((unsigned)(int)vf1, nan_row);
-                            const float2 rv = __fadd2_rn(vi, make_float2(-vf0, -vf1));
-                            float2 lo0, hi0, lo1, hi1;
-                            Quad<QT>::load(base + vr0 * (unsigned)nq, lo0, hi0);
-                            Quad<QT>::load(base + vr1 * (unsigned)nq, lo1, hi1);
-                            const float2 s0 = __ffma2_rn(ru2, hi0, lo0), s1 = __ffma2_rn(ru2, hi1, lo1);
-                            acc[k] = fmaf(w, fmaf(rv.x, s0.y, s0.x), acc[k]);
-                            acc[k + 1] = fmaf(w, fmaf(rv.y, s1.y, s1.x), acc[k + 1]);
-                        }
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < BP_ZC; ++k) {
-                            const float vi = fmaf((float)k, vB, vA);
-                            const float vf = floorf(vi);
-                            // rows outside [0, nv-2] (negative ones wrap around) read the NaN row
-                            const unsigned vr = min((unsigned)(int)vf, nan_row);
-                            const float rv = vi - vf;
-                            float2 lo, hi;
-                            Quad<QT>::load(base + vr * (unsigned)nq, lo, hi);
-                            const float2 s2 = __ffma2_rn(ru2, hi, lo);
-                            acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
-                        }
+                    for (int k = 0; k < BP_ZC; k += 2) {
+                        const float2 vi = __ffma2_rn(make_float2((float)k, (float)(k + 1)), vB2, vA2);
+                        const float vf0 = floorf(vi.x), vf1 = floorf(vi.y);
+                        const unsigned vr0 = min((unsigned)(int)vf0, nan_row);
+                        const unsigned vr1 = min((unsigned)(int)vf1, nan_row);
+                        const float2 rv = __fadd2_rn(vi, make_float2(-vf0, -vf1));
+                        float2 lo0, hi0, lo1, hi1;
+                        Quad<QT>::load(base + vr0 * (unsigned)nq, lo0, hi0);
+                        Quad<QT>::load(base + vr1 * (unsigned)nq, lo1, hi1);
+                        const float2 s0 = __ffma2_rn(ru2, hi0, lo0), s1 = __ffma2_rn(ru2, hi1, lo1);
+                        acc[k] = fmaf(w, fmaf(rv.x, s0.y, s0.x), acc[k]);
+                        acc[k + 1] = fmaf(w, fmaf(rv.y, s1.y, s1.x), acc[k + 1]);
                     }
                 } else {
-                    const PT* base = reinterpret_cast<const PT*>(packed) + ((int64_t)j * p.nv + zb) * nq + uc;
 #pragma unroll
                     for (int k = 0; k < BP_ZC; ++k) {
-                        if (zb + k < p.nsl) {
-                            const float2 pr = Pair<PT>::load(base + (int64_t)k * nq);
-                            acc[k] = fmaf(w, fmaf(ru, pr.y, pr.x), acc[k]);
-                        }
+                        const float vi = fmaf((float)k, vB, vA);
+                        const float vf = floorf(vi);
+                        // rows outside [0, nv-2] (negative ones wrap around) read the NaN row
+                        const unsigned vr = min((unsigned)(int)vf, nan_row);
+                        const float rv = vi - vf;
+                        float2 lo, hi;
+                        Quad<QT>::load(base + vr * (unsigned)nq, lo, hi);
+                        const float2 s2 = __ffma2_rn(ru2, hi, lo);
+                        acc[k] = fmaf(w, fmaf(rv, s2.y, s2.x), acc[k]);
                     }
                 }
             } else if (MODE == 3) {
