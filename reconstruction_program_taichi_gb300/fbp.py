@@ -328,8 +328,9 @@ class Mgfbp_v2(Mgfbp):  # noqa: N801 - reference name
         stage(0)
         for i, (j0, j1) in enumerate(chunks):
             n, b = j1 - j0, i % 2
-            if i + 1 < len(chunks):
-                stage(i + 1)
+            # chunk i's kernels are queued first, then the host stages chunk i + 1 (which
+            # waits for chunk i - 1 to release its buffers), so the GPU works on chunk i
+            # while the CPU copies the next one into pinned memory
             compute.wait_event(copied[b])
             cg = ops.ViewChunk(dg, j0, n, accumulate=True)
             rs, vs = (V * g.nu, g.nu) if sino_layout else (g.nu, g.nv * g.nu)
@@ -350,6 +351,8 @@ class Mgfbp_v2(Mgfbp):  # noqa: N801 - reference name
             pk = ops.pack(cg, f, pipe.dtype, out=packed)
             ops.fdk_bp(cg, pk, pipe.dtype, out=vol)
             consumed[b].record(compute)
+            if i + 1 < len(chunks):
+                stage(i + 1)
         ops.fdk_bp_finish(dg, vol)
         return vol
 
