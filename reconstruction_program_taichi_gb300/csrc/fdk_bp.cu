@@ -341,7 +341,11 @@ fdk_bp_fan_kernel(BpParams p, const float* __restrict__ angles, const void* __re
         fill_view_table(p, angles, tab, jc, nvc, tid, 32 * FB_G, unscale);
         __syncthreads();
         if (!active || dead) continue;
-#pragma unroll 2
+        // views in flight per thread: a one-slice thread has one short dependent chain
+        // per view (helical FBP, 140 slices of 512^2 x 720 views, bit-identical: 51.45
+        // ms unrolled 2, 48.85 unrolled 4, 49.63 unrolled 8)
+        constexpr int kViewUnroll = ZC == 1 ? 4 : 2;
+#pragma unroll kViewUnroll
         for (int q = g; q < nvc; q += FB_G) {
             const int j = jc + q;
             const float4 tb = tab[q];
